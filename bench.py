@@ -1,0 +1,315 @@
+#!/usr/bin/env python3
+"""Benchmark: bit-exact range-sum answers/s of the plain version-tree replay on GB300.
+
+Workload (default): the trip-log-shaped single tree -- 300,000 states (extend
+with p=0.9, fork from a uniform earlier state otherwise), 40,000,000 int64 delta
+events with Zipf s=1.2 keys over 65,536 cells, 50,000,000 range-sum queries at
+uniform states with uniform intervals; seeded synthetic data (see
+biworlddb-artifact_gb300/workloads.py).  One step = one full replay of that
+workload: ingest, tree linearisation, block plan, carry scan and block sweep.
+
+* value: answers/s with inputs resident in HBM (CUDA events around K steps).
+* e2e:   the same through the public API with pinned host buffers: every step
+  copies parent/events/queries host->device and the answers device->host.
+* roofline: the dominant kernel (the block sweep) -- algorithmic bytes per launch
+  (16 B per event record + 12 B per query record + 8 B per answer) over its mean
+  launch time, measured with CUDA events on the launch stream over the timed
+  region, against the measured HBM copy bandwidth.
+* cpu_baseline: the oracle's preorder apply/undo replay (the reference's tree
+  path, batch_engine_v7.hpp:1021-1059, ported) on the first states of the same
+  workload, 1 thread.
+
+Inputs (1.24 GB) exceed L2 (129 MB), so no explicit L2 flush is done between steps.
+
+--impl reference times the reference's CPU implementation of the path (the
+ported preorder replay; the reference's block-parallel executor only supports
+chains, batch_engine_v7.hpp:708) on a bounded sample and prints the same line.
+Under torchrun with N>1 every rank runs an independent replica (weak scaling);
+rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "bit-exact range-sum answers/s (plain version-tree replay)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="trip_tree")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--blocks", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample duration")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms in the background."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload: str):
+    """DRAM bytes per sweep launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / f"k_sweep_{workload}.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(w, seconds: float):
+    """Oracle preorder replay over the first states of the workload, timed alone."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    S = len(w.parent)
+    probe = max(1, min(S, 2000))
+    _, done, secs = oracle.ev_sweep_prefix(w.parent, w.n_keys, w.events, w.queries, probe)
+    rate_steps = probe / max(secs, 1e-9)
+    limit = int(min(2 * S, max(probe, rate_steps * seconds)))
+    _, done, secs = oracle.ev_sweep_prefix(w.parent, w.n_keys, w.events, w.queries, limit)
+    return {"value": done / max(secs, 1e-9), "unit": "answers/s", "cores": 1, "kind": "port",
+            "sample": f"preorder replay of the first {limit} of {S} states ({done} answers, {secs:.1f} s)"}
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    w = load_pkg().workloads.make(args.workload, args.seed, args.scale)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(w, min(3.0, args.cpu_seconds / 4))
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(w, max(1.0, args.cpu_seconds / max(1, args.steps))))
+    v = statistics.median([x["value"] for x in vals])
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "answers/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+            "config": dict(w.describe(), l2="inputs larger than L2"),
+            "cpu_baseline": {"value": v, "unit": "answers/s", "cores": 1, "kind": "port",
+                             "sample": vals[-1]["sample"]},
+            "e2e": {"value": v, "unit": "answers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def load_pkg():
+    import __graft_entry__ as g
+    return g.package()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    bw = load_pkg()
+    bw.build()
+    w = bw.workloads.make(args.workload, args.seed, args.scale)
+    S, E, Q = len(w.parent), len(w.events), len(w.queries)
+
+    h_parent = torch.from_numpy(w.parent).pin_memory()
+    h_events = torch.from_numpy(w.events.view(np.int64).reshape(-1, 2)).pin_memory()
+    h_queries = torch.from_numpy(w.queries.view(np.int32).reshape(-1, 3)).pin_memory()
+    h_answers = torch.empty(Q, dtype=torch.int64).pin_memory()
+    d_parent = h_parent.to(dev)
+    d_events = h_events.to(dev)
+    d_queries = h_queries.to(dev)
+    d_answers = torch.empty(Q, dtype=torch.int64, device=dev)
+    plan = bw.Replay(d_parent, w.n_keys, E, Q, blocks=args.blocks, chain=w.chain, timing=True)
+    stream = torch.cuda.current_stream(dev)
+
+    # warm-up + correctness spot check (oracle ancestor walk on a query sample)
+    for i in range(args.warmup):
+        plan.launch(d_parent, d_events, d_queries, d_answers)
+        if i == 0:
+            st = plan.status()
+            if st:
+                raise SystemExit(f"device rejected the workload: {bw.STATUS_NAMES.get(st, st)}")
+    torch.cuda.synchronize()
+    ans0 = d_answers.cpu().numpy()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    rng = np.random.default_rng(123)
+    sample = np.sort(rng.choice(Q, size=min(Q, 20000), replace=False))
+    want = oracle.ev_bruteforce(w.parent, w.events, w.queries[sample])
+    if not np.array_equal(ans0[sample], want):
+        raise SystemExit("GPU answers differ from the oracle on the spot-check sample")
+    digest = oracle.sha256_hex(ans0.tobytes())
+
+    # ---- timed region (device-resident inputs)
+    clocks = ClockSampler(local)
+    kernels, blocks = plan.info()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    plan.timing_reset()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(args.steps):
+        plan.launch(d_parent, d_events, d_queries, d_answers)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    ms = t0.elapsed_time(t1) / args.steps
+    stage_ms, n_timed = plan.stage_times()
+    stage_mean = {k: v / max(1, n_timed) for k, v in stage_ms.items()}
+    if ws > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    if not np.array_equal(d_answers.cpu().numpy(), ans0):
+        raise SystemExit("answers changed between steps")
+    value = ws * Q / (ms / 1e3)
+
+    # ---- e2e through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            d_parent.copy_(h_parent, non_blocking=True)
+            d_events.copy_(h_events, non_blocking=True)
+            d_queries.copy_(h_queries, non_blocking=True)
+            plan.launch(d_parent, d_events, d_queries, d_answers)
+            h_answers.copy_(d_answers, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = e0.elapsed_time(e1) / args.steps
+        if ws > 1:
+            t = torch.tensor([ems], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ems = float(t.item())
+        if not np.array_equal(h_answers.numpy(), ans0):
+            raise SystemExit("e2e answers differ")
+        e2e = {"value": ws * Q / (ems / 1e3), "unit": "answers/s",
+               "h2d_bytes_per_step": 4 * S + 16 * E + 12 * Q, "d2h_bytes_per_step": 8 * Q,
+               "ms_per_step": ems}
+
+    peak, peak_kind = measured_peaks()
+    sweep_bytes = 16 * E + 20 * Q
+    sweep_ms = stage_mean["sweep"]
+    achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9
+    traffic = profiled_traffic(w.name)
+    line = {
+        "metric": METRIC, "value": value, "unit": "answers/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": dict(w.describe(), blocks=blocks, l2="inputs larger than L2 (no flush needed)",
+                       answers_sha256=digest, parallelism=f"replicas{ws}" if ws > 1 else "single"),
+        "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": sweep_bytes,
+                     "mean_launch_ms": sweep_ms},
+        "pipeline": {"stages_ms": stage_mean,
+                     "whole_step_gbs": w.algorithmic_bytes / (ms / 1e3) / 1e9,
+                     "whole_step_frac": w.algorithmic_bytes / (ms / 1e3) / 1e9 / peak},
+        "gpu_launches": kernels * args.steps,
+        "clocks": clk,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

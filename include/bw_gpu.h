@@ -1,0 +1,174 @@
+/*
+ * bw_gpu.h -- C ABI of the GB300 (sm_103a) version-tree range-sum executor.
+ *
+ * Plain C types only (no CUDA or torch types), so the header is includable from
+ * gcc, g++ and nvcc, like the reference's gpu_v7.h:1-2.  Every pointer named
+ * "device" is device memory owned by the caller.  Every entry returns 0 on
+ * success or the cudaError_t value of the failing CUDA call (as the reference's
+ * *_launch functions do, gpu_v7.cu:98-121), after printing a one-line
+ * diagnostic to stderr; argument errors return BW_EINVAL.  Launches are
+ * asynchronous on the given stream (NULL = legacy default stream, as the
+ * reference launches).
+ *
+ * Two families of entry points:
+ *
+ *  1. Drop-in replacements for the reference's GPU v7 interface
+ *     (gpu_v7.h:7-50): same struct layouts, same argument meaning, same
+ *     outputs (local endpoint prefixes `lvals`, dense block leaf deltas `dV`,
+ *     answers of the combine), so the reference worker panel_batch_gpu.cpp can
+ *     link this library unchanged.
+ *
+ *  2. The event-model replay (bw_replay_*): a version tree (parent array),
+ *     int64 delta events (state, key, delta) grouped by state and range-sum
+ *     queries (state, lo, hi) grouped by state.  The answer of query j is the
+ *     wrapping int64 sum of the deltas of every event whose state lies on the
+ *     root path of queries[j].state (inclusive) and whose key lies in [lo, hi);
+ *     0 when hi <= lo.  This is the reference's per-state answer
+ *     (oracle.cpp:357-422) restated over endpoint classes: a row edit or factor
+ *     edit becomes class-delta events (batch_engine_v7.hpp:884-929), a query
+ *     becomes the class interval [qlb, qhb) (batch_engine_v7.hpp:666-698).
+ */
+#ifndef BW_GPU_H
+#define BW_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BW_EINVAL 1001
+
+/* ===================================================================== v7 drop-in
+ * Layouts identical to the reference (gpu_v7.h:7-47). */
+struct GpuV7Node {  /* one edited state (node 0 is unused) */
+  int32_t kind;     /* 1 row, 2 factor */
+  int32_t g_old, c_old, ti_old;
+  int32_t g_new, c_new, ti_new;
+  int64_t amt_old, amt_new, fac_val, fac_prev;
+  uint8_t ex_old, ex_new;
+  uint8_t pad[6];
+};
+
+struct GpuV7Args {
+  int B, G, Cpfx, ncls, q;
+  const struct GpuV7Node* nodes; /* device, kStates entries */
+  const int32_t* block_v0;       /* device, B */
+  const int32_t* block_v1;       /* device, B */
+  const int64_t* fac_start;      /* device, B*G factor vector at each block start */
+  const int32_t* g2row;          /* device, G (-1: group never factor-edited) */
+  const int32_t* ms_off;         /* device, n_active+1 merged-support offsets */
+  const int64_t* ms_cls;         /* device, support classes */
+  const int64_t* ms_base;        /* device, base mass at support classes */
+  const int32_t* ms_dev;         /* device, deviation index or -1 */
+  int64_t* devbuf;               /* device in/out, block-start deviation snapshots */
+  const int64_t* need_off;       /* device, B*G offsets into devbuf, -1 when not needed */
+  const int32_t* qlb;            /* device, kStates*q lower endpoint classes */
+  const int32_t* qhb;            /* device, kStates*q upper endpoint classes */
+  int64_t* lvals;                /* device out, (kStates-1)*2q local endpoint prefixes */
+  int64_t* dV;                   /* device out, B*Cpfx dense block leaf deltas */
+  int threads;                   /* hint only; the GB300 kernel picks its own width */
+  int shared_bytes;              /* hint only */
+};
+
+struct GpuV7CombineArgs {
+  int nstates;               /* kStates-1 */
+  int q;
+  int Cpfx;
+  const int32_t* qlb;        /* device */
+  const int32_t* qhb;        /* device */
+  const int64_t* carrypref;  /* device, B*Cpfx */
+  const int32_t* bidx;       /* device, kStates state -> block */
+  const int64_t* lvals;      /* device */
+  int64_t* answers;          /* device out, nstates*q */
+};
+
+/* Replaces gpu_v7_launch (gpu_v7.h:49, gpu_v7.cu:98-113): per state block, replay
+ * the block's nodes from a zero local prefix, record the local prefix at both
+ * declared endpoints of every query, and emit the block's dense leaf delta.
+ * Updates devbuf exactly as the reference kernel does (gpu_v7.cu:29-37). */
+int gpu_v7_launch(const struct GpuV7Args* a);
+/* Replaces gpu_combine_launch (gpu_v7.h:50, gpu_v7.cu:115-121):
+ * answers = carry prefix difference + local prefix difference. */
+int gpu_combine_launch(const struct GpuV7CombineArgs* a);
+/* Device-side replacement of the worker's host carry pass
+ * (panel_batch_gpu.cpp:191-202): carrypref[b][k] = sum_{c<k} vstart_b[c],
+ * vstart_0 = vbase, vstart_{b+1} = vstart_b + dV[b].  Same stream semantics. */
+int bw_v7_carry_launch(int B, int Cpfx, const int64_t* vbase, const int64_t* dV,
+                       int64_t* carrypref, void* stream);
+
+/* ===================================================================== event model */
+typedef struct { uint32_t state, key; int64_t delta; } BwEvent;   /* 16 bytes */
+typedef struct { uint32_t state, lo, hi; } BwQuery;               /* 12 bytes */
+
+typedef struct {
+  int32_t n_states;          /* states 0..n_states-1; state 0 is the root */
+  const int32_t* parent;     /* device, n_states; parent[0] = -1, parent[v] < v */
+  uint32_t n_keys;           /* key domain [0, n_keys); query bounds lie in [0, n_keys] */
+  int64_t n_events;
+  const BwEvent* events;     /* device, grouped by state (non-decreasing state) */
+  int64_t n_queries;
+  const BwQuery* queries;    /* device, grouped by state (non-decreasing state) */
+  int64_t* answers;          /* device out, n_queries */
+  void* workspace;           /* device, >= bw_replay_workspace_size(); 256-byte aligned */
+  size_t workspace_bytes;
+  void* stream;              /* cudaStream_t or NULL */
+  int32_t blocks;            /* state blocks; 0 = pick from the device and the workload */
+  int32_t flags;             /* BW_REPLAY_* */
+} BwReplayArgs;
+
+#define BW_REPLAY_CHAIN_HINT 1  /* caller asserts parent[v] == v-1 (skips tree linearisation) */
+#define BW_REPLAY_TIMING 2      /* record CUDA events between pipeline stages (see below) */
+
+/* Pipeline stages timed under BW_REPLAY_TIMING, in order. */
+enum {
+  BW_STAGE_INGEST = 0,     /* per-state offsets + validation */
+  BW_STAGE_LINEARISE = 1,  /* Euler tour / chain layout */
+  BW_STAGE_BLOCKS = 2,     /* work prefix + block cut */
+  BW_STAGE_PREPARE = 3,    /* block rank tables, slices, net key-prefix rows */
+  BW_STAGE_CARRY = 4,      /* carry scan over blocks */
+  BW_STAGE_SWEEP = 5,      /* block sweep and answers */
+  BW_STAGE_COUNT = 6
+};
+
+/* Input errors found on the device are reported through bw_replay_status(). */
+enum {
+  BW_STATUS_OK = 0,
+  BW_STATUS_EVENTS_UNSORTED = 1,
+  BW_STATUS_EVENT_KEY_RANGE = 2,
+  BW_STATUS_QUERIES_UNSORTED = 3,
+  BW_STATUS_QUERY_RANGE = 4,
+  BW_STATUS_BAD_PARENT = 5,
+  BW_STATUS_TOO_MANY_SLICES = 6,
+  BW_STATUS_STATE_RANGE = 7
+};
+
+/* Bytes of device workspace needed for these arguments (pointers unused). */
+int bw_replay_workspace_size(const BwReplayArgs* a, size_t* bytes);
+/* Enqueue the whole replay (ingest offsets, tree linearisation, block plan, carry
+ * scan, block sweep) on a->stream.  Reads only the inputs, writes answers and the
+ * workspace. */
+int bw_replay_launch(const BwReplayArgs* a);
+/* Synchronise a->stream and read the device status word written by the last
+ * bw_replay_launch with this workspace; *status receives a BW_STATUS_* code. */
+int bw_replay_status(const BwReplayArgs* a, int32_t* status);
+/* Number of kernels the last bw_replay_launch on this workspace enqueued and the
+ * state-block count it used (host-side bookkeeping, no synchronisation). */
+int bw_replay_last_info(const BwReplayArgs* a, int32_t* kernels, int32_t* blocks);
+
+/* Stage timing over a run of launches made with BW_REPLAY_TIMING (CUDA events
+ * recorded on each launch's stream).  bw_replay_timing_reset() starts a new run;
+ * bw_replay_stage_times() synchronises on the last recorded event and writes the
+ * per-stage milliseconds summed over the run's launches (ms[BW_STAGE_COUNT]) and
+ * the number of launches.  Process-wide, for one host thread at a time. */
+int bw_replay_timing_reset(void);
+int bw_replay_stage_times(float* ms, int32_t* launches);
+
+/* Library/device information: SM count of the current device and the library's
+ * compile-time architecture tag (e.g. 1030 for sm_103a). */
+int bw_device_info(int32_t* sm_count, int32_t* arch_tag);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,188 @@
+"""ctypes wrapper around liboracle.so -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import
+this module.  It exposes the CPU restatements in bw_oracle.c:
+
+* ``fixture_*`` / ``workload_*`` / ``direct_scan``: the reference-native semantics
+  (common.hpp:112-155 loader, common.hpp:279-374 make_workload, oracle.cpp:213-451
+  direct-scan oracle);
+* ``ev_bruteforce`` / ``ev_sweep`` / ``ev_blocks``: the event-model checkers
+  (ancestor walk, batch_engine_v7.hpp:1021-1059 preorder replay,
+  batch_engine_v7.hpp:832-968 block-parallel chain executor).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liboracle.so"
+
+EVENT_DTYPE = np.dtype([("state", "<u4"), ("key", "<u4"), ("delta", "<i8")])
+QUERY_DTYPE = np.dtype([("state", "<u4"), ("lo", "<u4"), ("hi", "<u4")])
+
+
+def build(force: bool = False) -> Path:
+    """Compile liboracle.so in place (gcc, a few seconds)."""
+    src = HERE / "bw_oracle.c"
+    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
+    return LIB_PATH
+
+
+class _Fixture(C.Structure):
+    _fields_ = [("n", C.c_int64), ("groups", C.c_int32), ("unit", C.c_int32),
+                ("t_min", C.c_int64), ("t_max", C.c_int64), ("row_t", C.c_void_p),
+                ("rows", C.c_void_p), ("factor", C.c_void_p), ("labels", C.c_void_p)]
+
+
+class _Workload(C.Structure):
+    _fields_ = [("n_states", C.c_int32), ("topology", C.c_int32), ("seed", C.c_int32),
+                ("factor_period", C.c_int32), ("q", C.c_int32), ("per_state", C.c_int32),
+                ("factor_pct", C.c_int32), ("n_base", C.c_int64), ("groups", C.c_int32),
+                ("n_inserted", C.c_int32), ("t_min", C.c_int64), ("t_max", C.c_int64),
+                ("parent", C.c_void_p), ("op", C.c_void_p), ("eg", C.c_void_p),
+                ("eid", C.c_void_p), ("eval", C.c_void_p), ("et", C.c_void_p),
+                ("qlo", C.c_void_p), ("qhi", C.c_void_p), ("ins_t", C.c_void_p),
+                ("ins_g", C.c_void_p), ("endpoints", C.c_void_p), ("n_endpoints", C.c_int64)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB_PATH))
+        L.bwo_sha256_hex.argtypes = [C.c_void_p, C.c_size_t, C.c_char_p]
+        L.bwo_fnv1a.argtypes = [C.c_void_p, C.c_size_t]
+        L.bwo_fnv1a.restype = C.c_uint64
+        L.bwo_fixture_parse.argtypes = [C.c_void_p, C.c_size_t, C.POINTER(_Fixture)]
+        L.bwo_workload_make.argtypes = [C.POINTER(_Fixture)] + [C.c_int32] * 7 + [C.POINTER(_Workload)]
+        L.bwo_workload_free.argtypes = [C.POINTER(_Workload)]
+        L.bwo_direct_scan.argtypes = [C.POINTER(_Fixture), C.POINTER(_Workload), C.c_void_p]
+        ev_args = [C.c_int32, C.c_void_p, C.c_uint32, C.c_int64, C.c_void_p, C.c_int64,
+                   C.c_void_p, C.c_void_p]
+        L.bwo_ev_bruteforce.argtypes = [C.c_int32, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64,
+                                        C.c_void_p, C.c_void_p]
+        L.bwo_ev_sweep.argtypes = ev_args
+        L.bwo_ev_sweep_prefix.argtypes = ev_args + [C.c_int64, C.POINTER(C.c_int64),
+                                                    C.POINTER(C.c_double)]
+        L.bwo_ev_blocks.argtypes = ev_args + [C.c_int32, C.c_int32]
+        L.bwo_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def sha256_hex(buf) -> str:
+    a = np.ascontiguousarray(np.frombuffer(memoryview(buf).cast("B"), dtype=np.uint8))
+    out = C.create_string_buffer(65)
+    lib().bwo_sha256_hex(_ptr(a) if a.size else None, a.size, out)
+    return out.value.decode()
+
+
+def fnv1a(buf) -> int:
+    a = np.ascontiguousarray(np.frombuffer(memoryview(buf).cast("B"), dtype=np.uint8))
+    return int(lib().bwo_fnv1a(_ptr(a) if a.size else None, a.size))
+
+
+class Fixture:
+    """A parsed BWBASE02 image (keeps the bytes alive)."""
+
+    def __init__(self, image: bytes):
+        self.image = np.frombuffer(image, dtype=np.uint8).copy()
+        self.s = _Fixture()
+        rc = lib().bwo_fixture_parse(_ptr(self.image), self.image.size, C.byref(self.s))
+        if rc:
+            raise ValueError(f"malformed BWBASE02 fixture (rc={rc})")
+
+
+def direct_scan(fx: Fixture, n_states: int, topology: int, seed: int, factor_period: int,
+                q: int, per_state: bool = True, factor_pct: int = -1) -> np.ndarray:
+    """Answers of the independent direct-scan oracle, order v=1..S-1, k=0..q-1."""
+    w = _Workload()
+    rc = lib().bwo_workload_make(C.byref(fx.s), n_states, topology, seed, factor_period, q,
+                                 int(per_state), factor_pct, C.byref(w))
+    if rc:
+        raise ValueError(f"workload rejected (rc={rc})")
+    try:
+        ans = np.zeros((n_states - 1) * q, dtype=np.int64)
+        rc = lib().bwo_direct_scan(C.byref(fx.s), C.byref(w), _ptr(ans))
+        if rc == 6:
+            raise OverflowError("an exact answer does not fit int64")
+        if rc:
+            raise RuntimeError(f"direct scan failed rc={rc}")
+        return ans
+    finally:
+        lib().bwo_workload_free(C.byref(w))
+
+
+def _ev_arrays(parent, events, queries):
+    parent = np.ascontiguousarray(parent, dtype=np.int32)
+    events = np.ascontiguousarray(events, dtype=EVENT_DTYPE)
+    queries = np.ascontiguousarray(queries, dtype=QUERY_DTYPE)
+    return parent, events, queries
+
+
+def ev_bruteforce(parent, events, queries) -> np.ndarray:
+    parent, events, queries = _ev_arrays(parent, events, queries)
+    ans = np.zeros(len(queries), dtype=np.int64)
+    rc = lib().bwo_ev_bruteforce(len(parent), _ptr(parent), len(events), _ptr(events),
+                                 len(queries), _ptr(queries), _ptr(ans))
+    if rc not in (0, 6):
+        raise ValueError(f"bad event-model input (rc={rc})")
+    return ans
+
+
+def ev_sweep(parent, n_keys: int, events, queries) -> np.ndarray:
+    parent, events, queries = _ev_arrays(parent, events, queries)
+    ans = np.zeros(len(queries), dtype=np.int64)
+    rc = lib().bwo_ev_sweep(len(parent), _ptr(parent), n_keys, len(events), _ptr(events),
+                            len(queries), _ptr(queries), _ptr(ans))
+    if rc:
+        raise ValueError(f"bad event-model input (rc={rc})")
+    return ans
+
+
+def ev_sweep_prefix(parent, n_keys: int, events, queries, limit_steps: int):
+    """Preorder replay of the first `limit_steps` states; returns (answers,
+    answered, seconds of the replay loop)."""
+    parent, events, queries = _ev_arrays(parent, events, queries)
+    ans = np.zeros(len(queries), dtype=np.int64)
+    done = C.c_int64(0)
+    secs = C.c_double(0.0)
+    rc = lib().bwo_ev_sweep_prefix(len(parent), _ptr(parent), n_keys, len(events), _ptr(events),
+                                   len(queries), _ptr(queries), _ptr(ans), limit_steps,
+                                   C.byref(done), C.byref(secs))
+    if rc:
+        raise ValueError(f"bad event-model input (rc={rc})")
+    return ans, int(done.value), float(secs.value)
+
+
+def ev_blocks(parent, n_keys: int, events, queries, blocks: int = 0, threads: int = 0) -> np.ndarray:
+    parent, events, queries = _ev_arrays(parent, events, queries)
+    ans = np.zeros(len(queries), dtype=np.int64)
+    rc = lib().bwo_ev_blocks(len(parent), _ptr(parent), n_keys, len(events), _ptr(events),
+                             len(queries), _ptr(queries), _ptr(ans), blocks, threads)
+    if rc:
+        raise ValueError(f"block executor needs a chain and valid input (rc={rc})")
+    return ans
+
+
+def max_threads() -> int:
+    return int(lib().bwo_max_threads())
+
+
+def ref_binary(name: str, states: int) -> Path | None:
+    """Path of a reference binary built by oracle/ref.mk, when present."""
+    p = HERE / "_ref" / f"{name}_{states}"
+    return p if p.exists() and os.access(p, os.X_OK) else None

@@ -1,0 +1,28 @@
+# Builds the reference's own CPU path from the read-only mounted sources into
+# oracle/_ref/ (git-ignored).  Used only to pin the oracle and as a CPU
+# reference where the sources exist.  No cmake: g++ on the reference's worker
+# sources directly, with a local stand-in for the absent OpenSSL header.
+#   make -f oracle/ref.mk REF=/root/reference STATES=2049
+REF ?= /root/reference
+STATES ?= 2049
+MAXQ ?= 32
+OUT ?= oracle/_ref
+CXX ?= g++
+CC ?= gcc
+
+all: $(OUT)/oracle_$(STATES) $(OUT)/compiled_$(STATES)
+
+$(OUT)/sha_shim.o: oracle/ref_shim/sha256_shim.c oracle/bw_oracle.c
+	mkdir -p $(OUT)
+	$(CC) -O2 -c -o $(OUT)/sha_shim.o oracle/ref_shim/sha256_shim.c
+	$(CC) -O2 -c -o $(OUT)/bwo.o oracle/bw_oracle.c
+
+$(OUT)/oracle_$(STATES):
+	mkdir -p $(OUT)
+	$(CXX) -std=c++17 -O2 -DBWH_STATES=$(STATES) -DBWH_MAXQ=$(MAXQ) -I$(REF)/src $(REF)/src/oracle.cpp -o $@
+
+$(OUT)/compiled_$(STATES): $(OUT)/sha_shim.o
+	$(CXX) -std=c++17 -O3 -fopenmp -DBWH_STATES=$(STATES) -DBWH_MAXQ=$(MAXQ) -Ioracle/ref_shim -I$(REF)/src \
+	  $(REF)/src/panel_batch_v7fix.cpp $(OUT)/sha_shim.o $(OUT)/bwo.o -o $@
+
+.PHONY: all
