@@ -175,3 +175,200 @@ def device_info():
     sms, tag = C.c_int32(0), C.c_int32(0)
     _check(gpu_lib().bw_device_info(C.byref(sms), C.byref(tag)), "bw_device_info")
     return int(sms.value), int(tag.value)
+
+
+# ---------------------------------------------------------------------------- host side
+class BwNativeSpec(C.Structure):
+    _fields_ = [("n_states", C.c_int32), ("topology", C.c_int32), ("seed", C.c_int32),
+                ("factor_period", C.c_int32), ("q", C.c_int32), ("per_state", C.c_int32),
+                ("factor_pct", C.c_int32)]
+
+
+class BwNativeWorkload(C.Structure):
+    _fields_ = [("n_states", C.c_int32), ("n_keys", C.c_uint32), ("n_events", C.c_int64),
+                ("n_queries", C.c_int64), ("parent", C.c_void_p), ("events", C.c_void_p),
+                ("queries", C.c_void_p), ("n_factor_events", C.c_int64)]
+
+
+HOST_SYMBOLS = ["bw_fixture_open", "bw_fixture_from_memory", "bw_fixture_close", "bw_fixture_rows",
+                "bw_native_build", "bw_native_free", "bw_sha256_hex", "bw_fnv1a"]
+
+_host = None
+
+
+def host_lib(build_if_missing: bool = True):
+    """The host C++ library (fixtures, declared workloads, digests)."""
+    global _host
+    if _host is None:
+        if build_if_missing:
+            _build.build()
+        L = C.CDLL(str(_build.HOST_LIB))
+        L.bw_fixture_from_memory.argtypes = [C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)]
+        L.bw_fixture_open.argtypes = [C.c_char_p, C.POINTER(C.c_void_p)]
+        L.bw_fixture_close.argtypes = [C.c_void_p]
+        L.bw_fixture_rows.argtypes = [C.c_void_p]
+        L.bw_fixture_rows.restype = C.c_int64
+        L.bw_native_build.argtypes = [C.c_void_p, C.POINTER(BwNativeSpec),
+                                      C.POINTER(C.POINTER(BwNativeWorkload))]
+        L.bw_native_free.argtypes = [C.POINTER(BwNativeWorkload)]
+        L.bw_sha256_hex.argtypes = [C.c_void_p, C.c_size_t, C.c_char_p]
+        L.bw_fnv1a.argtypes = [C.c_void_p, C.c_size_t]
+        L.bw_fnv1a.restype = C.c_uint64
+        _host = L
+    return _host
+
+
+def sha256_hex(buf) -> str:
+    import numpy as np
+    a = np.ascontiguousarray(np.frombuffer(memoryview(buf).cast("B"), dtype=np.uint8))
+    out = C.create_string_buffer(65)
+    host_lib().bw_sha256_hex(a.ctypes.data if a.size else None, a.size, out)
+    return out.value.decode()
+
+
+def fnv1a(buf) -> int:
+    import numpy as np
+    a = np.ascontiguousarray(np.frombuffer(memoryview(buf).cast("B"), dtype=np.uint8))
+    return int(host_lib().bw_fnv1a(a.ctypes.data if a.size else None, a.size))
+
+
+def native_workload(fixture: bytes, n_states: int, topology: int, seed: int, factor_period: int,
+                    q: int, per_state: bool = True, factor_pct: int = -1) -> "workloads.Workload":
+    """Compile a reference-native case (BWBASE02 image + declared edits) into the
+    event model: class-delta events by state and class-interval queries in the
+    reference's answer order (v = 1..S-1, k = 0..q-1)."""
+    import numpy as np
+    L = host_lib()
+    img = np.frombuffer(fixture, dtype=np.uint8)
+    fx = C.c_void_p()
+    rc = L.bw_fixture_from_memory(img.ctypes.data, img.size, C.byref(fx))
+    if rc:
+        raise ValueError(f"malformed BWBASE02 fixture (rc={rc})")
+    try:
+        spec = BwNativeSpec(n_states, topology, seed, factor_period, q, int(per_state), factor_pct)
+        out = C.POINTER(BwNativeWorkload)()
+        rc = L.bw_native_build(fx, C.byref(spec), C.byref(out))
+        if rc:
+            raise ValueError(f"native workload rejected (rc={rc})")
+        try:
+            w = out.contents
+            S, E, Q = w.n_states, w.n_events, w.n_queries
+            parent = np.ctypeslib.as_array(C.cast(w.parent, C.POINTER(C.c_int32)), (S,)).copy()
+            ev = np.frombuffer(C.string_at(w.events, 16 * E), dtype=workloads.EVENT_DTYPE).copy() \
+                if E else np.empty(0, dtype=workloads.EVENT_DTYPE)
+            qs = np.frombuffer(C.string_at(w.queries, 12 * Q), dtype=workloads.QUERY_DTYPE).copy() \
+                if Q else np.empty(0, dtype=workloads.QUERY_DTYPE)
+            name = f"native_S{n_states}_t{topology}_s{seed}_f{factor_period}_q{q}"
+            return workloads.Workload(name, parent, int(w.n_keys), ev, qs, topology == 0)
+        finally:
+            L.bw_native_free(out)
+    finally:
+        L.bw_fixture_close(fx)
+
+
+class BwV7Plan(C.Structure):
+    _fields_ = [("B", C.c_int32), ("G", C.c_int32), ("Cpfx", C.c_int32), ("ncls", C.c_int32),
+                ("q", C.c_int32), ("n_states", C.c_int32), ("n_active", C.c_int32),
+                ("nodes", C.c_void_p), ("block_v0", C.c_void_p), ("block_v1", C.c_void_p),
+                ("fac_start", C.c_void_p), ("g2row", C.c_void_p), ("ms_off", C.c_void_p),
+                ("ms_cls", C.c_void_p), ("ms_base", C.c_void_p), ("ms_dev", C.c_void_p),
+                ("devbuf", C.c_void_p), ("n_devbuf", C.c_int64), ("need_off", C.c_void_p),
+                ("qlb", C.c_void_p), ("qhb", C.c_void_p), ("bidx", C.c_void_p), ("vbase", C.c_void_p)]
+
+
+def _node_dtype():
+    import numpy as np
+    return np.dtype([("kind", "<i4"), ("g_old", "<i4"), ("c_old", "<i4"), ("ti_old", "<i4"),
+                     ("g_new", "<i4"), ("c_new", "<i4"), ("ti_new", "<i4"), ("pad0", "<i4"),
+                     ("amt_old", "<i8"), ("amt_new", "<i8"), ("fac_val", "<i8"), ("fac_prev", "<i8"),
+                     ("ex_old", "u1"), ("ex_new", "u1"), ("pad", "u1", (6,))])
+
+
+def v7_plan(fixture: bytes, n_states: int, seed: int, factor_period: int, q: int, blocks: int,
+            per_state: bool = True, factor_pct: int = -1) -> dict:
+    """The reference's v7 chain plan for gpu_v7_launch, as numpy arrays."""
+    import numpy as np
+    L = host_lib()
+    L.bw_v7_plan_build.argtypes = [C.c_void_p, C.POINTER(BwNativeSpec), C.c_int32,
+                                   C.POINTER(C.POINTER(BwV7Plan))]
+    L.bw_v7_plan_free.argtypes = [C.POINTER(BwV7Plan)]
+    img = np.frombuffer(fixture, dtype=np.uint8)
+    fx = C.c_void_p()
+    rc = L.bw_fixture_from_memory(img.ctypes.data, img.size, C.byref(fx))
+    if rc:
+        raise ValueError(f"malformed BWBASE02 fixture (rc={rc})")
+    try:
+        spec = BwNativeSpec(n_states, 0, seed, factor_period, q, int(per_state), factor_pct)
+        out = C.POINTER(BwV7Plan)()
+        rc = L.bw_v7_plan_build(fx, C.byref(spec), blocks, C.byref(out))
+        if rc:
+            raise ValueError(f"v7 plan rejected (rc={rc})")
+        try:
+            p = out.contents
+            B, G, Cp, S, na = p.B, p.G, p.Cpfx, p.n_states, p.n_active
+            nms = None
+
+            def arr(ptr, dtype, n):
+                dt = np.dtype(dtype)
+                return np.frombuffer(C.string_at(ptr, dt.itemsize * n), dtype=dt).copy() if n else np.zeros(0, dt)
+            ms_off = arr(p.ms_off, "<i4", na + 1)
+            nms = int(ms_off[-1])
+            return {"B": B, "G": G, "Cpfx": Cp, "ncls": p.ncls, "q": p.q, "n_states": S,
+                    "nodes": arr(p.nodes, _node_dtype(), S), "block_v0": arr(p.block_v0, "<i4", B),
+                    "block_v1": arr(p.block_v1, "<i4", B), "fac_start": arr(p.fac_start, "<i8", B * G),
+                    "g2row": arr(p.g2row, "<i4", G), "ms_off": ms_off, "ms_cls": arr(p.ms_cls, "<i8", nms),
+                    "ms_base": arr(p.ms_base, "<i8", nms), "ms_dev": arr(p.ms_dev, "<i4", nms),
+                    "devbuf": arr(p.devbuf, "<i8", max(1, p.n_devbuf)), "need_off": arr(p.need_off, "<i8", B * G),
+                    "qlb": arr(p.qlb, "<i4", S * p.q), "qhb": arr(p.qhb, "<i4", S * p.q),
+                    "bidx": arr(p.bidx, "<i4", S), "vbase": arr(p.vbase, "<i8", Cp)}
+        finally:
+            L.bw_v7_plan_free(out)
+    finally:
+        L.bw_fixture_close(fx)
+
+
+class GpuV7Args(C.Structure):
+    _fields_ = [("B", C.c_int), ("G", C.c_int), ("Cpfx", C.c_int), ("ncls", C.c_int), ("q", C.c_int),
+                ("nodes", C.c_void_p), ("block_v0", C.c_void_p), ("block_v1", C.c_void_p),
+                ("fac_start", C.c_void_p), ("g2row", C.c_void_p), ("ms_off", C.c_void_p),
+                ("ms_cls", C.c_void_p), ("ms_base", C.c_void_p), ("ms_dev", C.c_void_p),
+                ("devbuf", C.c_void_p), ("need_off", C.c_void_p), ("qlb", C.c_void_p), ("qhb", C.c_void_p),
+                ("lvals", C.c_void_p), ("dV", C.c_void_p), ("threads", C.c_int), ("shared_bytes", C.c_int)]
+
+
+class GpuV7CombineArgs(C.Structure):
+    _fields_ = [("nstates", C.c_int), ("q", C.c_int), ("Cpfx", C.c_int), ("qlb", C.c_void_p),
+                ("qhb", C.c_void_p), ("carrypref", C.c_void_p), ("bidx", C.c_void_p),
+                ("lvals", C.c_void_p), ("answers", C.c_void_p)]
+
+
+def run_v7_plan(plan: dict):
+    """Drive the drop-in gpu_v7 ABI exactly as the reference worker does
+    (panel_batch_gpu.cpp:171-224): block kernel, carry, combine.  The carry runs
+    on the device (bw_v7_carry_launch) instead of the host.  Returns answers."""
+    import numpy as np
+    torch = _torch()
+    L = gpu_lib()
+    dev = torch.device("cuda")
+
+    def up(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8)).to(dev)
+    d = {k: up(plan[k]) for k in ("nodes", "block_v0", "block_v1", "fac_start", "g2row", "ms_off", "ms_cls",
+                                  "ms_base", "ms_dev", "devbuf", "need_off", "qlb", "qhb", "bidx", "vbase")}
+    B, Cp, q, S = plan["B"], plan["Cpfx"], plan["q"], plan["n_states"]
+    lvals = torch.empty((S - 1) * 2 * q, dtype=torch.int64, device=dev)
+    dV = torch.empty(B * Cp, dtype=torch.int64, device=dev)
+    carry = torch.empty(B * Cp, dtype=torch.int64, device=dev)
+    answers = torch.empty((S - 1) * q, dtype=torch.int64, device=dev)
+    a = GpuV7Args(B, plan["G"], Cp, plan["ncls"], q, *(d[k].data_ptr() for k in (
+        "nodes", "block_v0", "block_v1", "fac_start", "g2row", "ms_off", "ms_cls", "ms_base", "ms_dev",
+        "devbuf", "need_off", "qlb", "qhb")), lvals.data_ptr(), dV.data_ptr(), 256, 0)
+    torch.cuda.synchronize()
+    _check(L.gpu_v7_launch(C.byref(a)), "gpu_v7_launch")
+    _check(L.bw_v7_carry_launch(B, Cp, d["vbase"].data_ptr(), dV.data_ptr(), carry.data_ptr(), None),
+           "bw_v7_carry_launch")
+    ca = GpuV7CombineArgs(S - 1, q, Cp, d["qlb"].data_ptr(), d["qhb"].data_ptr(), carry.data_ptr(),
+                          d["bidx"].data_ptr(), lvals.data_ptr(), answers.data_ptr())
+    _check(L.gpu_combine_launch(C.byref(ca)), "gpu_combine_launch")
+    torch.cuda.synchronize()
+    return answers.cpu().numpy(), dV.cpu().numpy(), lvals.cpu().numpy()

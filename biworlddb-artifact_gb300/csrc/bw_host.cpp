@@ -1,0 +1,663 @@
+// bw_host.cpp -- host front end of the GB300 executor (include/bw_host.h).
+//
+// Compiles a reference-native workload (BWBASE02 fixture + declared edits and
+// per-state nested ranges) into the event model of bw_replay_launch: class-delta
+// events grouped by state and class-interval queries in the reference's answer
+// order.  One preorder pass over the version tree with apply/undo keeps each
+// row's current image, each group's factor and each group's per-class alive mass,
+// so factor edits expand to exactly the deltas the reference's executor adds.
+#include "bw_host.h"
+
+#include <fcntl.h>
+#include <sys/mman.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+struct BwFixture {
+  std::vector<uint8_t> copy;
+  void* map = nullptr;
+  size_t len = 0;
+  const uint8_t* base = nullptr;
+  int64_t n = 0;
+  int32_t G = 0;
+  int64_t t_min = 0, t_max = 0;
+
+  int64_t ld64(size_t off) const { int64_t x; std::memcpy(&x, base + off, 8); return x; }
+  int32_t ld32(size_t off) const { int32_t x; std::memcpy(&x, base + off, 4); return x; }
+  int64_t row_t(int64_t i) const { return ld64(64 + 24 * (size_t)i); }
+  int64_t row_amt(int64_t i) const { return ld64(64 + 24 * (size_t)i + 8); }
+  int32_t row_g(int64_t i) const { return ld32(64 + 24 * (size_t)i + 16); }
+  int64_t factor(int32_t g) const { return ld64(64 + 24 * (size_t)n + 8 * (size_t)g); }
+  ~BwFixture() { if (map) ::munmap(map, len); }
+};
+
+namespace {
+
+// Header checks of common.hpp:125-132 and 152-153.
+int parse_fixture(BwFixture* f) {
+  if (f->len < 64 || std::memcmp(f->base, "BWBASE02", 8) != 0) return 3;
+  f->n = f->ld64(8);
+  f->G = f->ld32(16);
+  if (f->n <= 0 || f->G <= 0 || f->n > ((int64_t)1 << 40) || f->G > (1 << 20)) return 3;
+  const size_t need = 64 + 24 * (size_t)f->n + 12 * (size_t)f->G;
+  if (need > f->len) return 3;
+  f->t_min = f->ld64(40);
+  f->t_max = f->ld64(48);
+  for (int32_t g = 0; g < f->G; ++g)
+    if (f->factor(g) <= 0) return 3;
+  return 0;
+}
+
+// SplitMix64 generator with the reference's seeding and draws (common.hpp:40-54):
+// identical numbers are required to reproduce the declared workload.
+struct Rng {
+  uint64_t s;
+  explicit Rng(uint64_t seed) : s(seed ? seed : 0x9E3779B97F4A7C15ULL) {}
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+  }
+  uint32_t bounded(uint32_t n) { return n ? (uint32_t)(next() % n) : 0u; }
+  int64_t range(int64_t lo, int64_t hi) { return hi <= lo ? lo : lo + (int64_t)(next() % (uint64_t)(hi - lo)); }
+};
+
+enum : uint8_t { OP_REPLACE = 0, OP_INSERT = 1, OP_DELETE = 2, OP_MOVE = 3, OP_FACTOR = 4 };
+
+struct Edit {
+  uint8_t op = 0;
+  int32_t g = 0;
+  int64_t id = 0, val = 0, t = 0;
+};
+
+struct Declared {
+  std::vector<int32_t> parent;
+  std::vector<Edit> edit;
+  std::vector<int64_t> qlo, qhi;  // per state (v*q+k) or shared (k)
+  std::vector<int64_t> ins_t;
+  std::vector<int32_t> ins_g;
+  std::vector<int64_t> endpoints;
+};
+
+int32_t version_parent(int32_t topology, int32_t v) {
+  if (v <= 0) return -1;
+  return topology == 0 ? v - 1 : topology == 1 ? (v - 1) / 2 : 0;
+}
+
+// Nested ranges of one state (common.hpp:229-246), first q levels.
+void nested(Rng& r, int64_t tmin, int64_t tmax, int32_t q, int64_t* lo_out, int64_t* hi_out) {
+  int64_t lo = tmin, hi = tmax + 1;
+  const int64_t span0 = hi - lo;
+  for (int32_t k = 0; k < q; ++k) {
+    int64_t span = hi - lo;
+    if (span <= 4096) {
+      lo = tmin + span0 / 2;
+      hi = lo + 2048;
+      span = hi - lo;
+    }
+    const int64_t a = span * (int64_t)(3 + r.bounded(16)) / 100;
+    const int64_t b = span * (int64_t)(3 + r.bounded(16)) / 100;
+    lo += a;
+    hi -= b;
+    if (hi - lo < 1024) hi = lo + 1024;
+    lo_out[k] = lo;
+    hi_out[k] = hi;
+  }
+}
+
+// Declared workload of common.hpp:279-374 for a runtime state count.
+void declare(const BwFixture& f, const BwNativeSpec& sp, Declared& w) {
+  const int32_t S = sp.n_states, q = sp.q, G = f.G;
+  const int64_t N = f.n, tmin = f.t_min, tmax = f.t_max;
+  const uint64_t seed = (uint64_t)(int64_t)sp.seed, topo = (uint64_t)(int64_t)sp.topology,
+                 fp = (uint64_t)(int64_t)sp.factor_period;
+  if (sp.per_state) {
+    w.qlo.assign((size_t)S * q, 0);
+    w.qhi.assign((size_t)S * q, 0);
+    for (int32_t v = 1; v < S; ++v) {
+      Rng r(seed * 1000000007ULL + topo * 65537ULL + fp * 131ULL + (uint64_t)v * 2654435761ULL + 17ULL);
+      nested(r, tmin, tmax, q, &w.qlo[(size_t)v * q], &w.qhi[(size_t)v * q]);
+    }
+  } else {
+    w.qlo.assign(q, 0);
+    w.qhi.assign(q, 0);
+    Rng r(seed * 1000000007ULL + topo * 65537ULL + fp * 131ULL + 17ULL);
+    nested(r, tmin, tmax, q, w.qlo.data(), w.qhi.data());
+  }
+  Rng rng(seed * 1000003ULL + topo * 7919ULL + fp * 104729ULL + 20261025ULL);
+  w.parent.resize(S);
+  for (int32_t v = 0; v < S; ++v) w.parent[v] = version_parent(sp.topology, v);
+  w.edit.assign(S, Edit{});
+  std::vector<int64_t> gfactor(G, 1000);
+  int32_t next_group = 0;
+  for (int32_t v = 1; v < S; ++v) {
+    Edit& e = w.edit[v];
+    const bool factor_step = sp.factor_pct >= 0 ? rng.bounded(100) < (uint32_t)sp.factor_pct
+                                                : (sp.factor_period > 0 && v % sp.factor_period == 0);
+    if (factor_step) {
+      const int32_t g = next_group++ % G;
+      const int64_t cur = gfactor[g];
+      const int64_t nf = cur == 950 ? 1000 : (cur == 1000 ? 1050 : 950);
+      gfactor[g] = nf;
+      e.op = OP_FACTOR; e.g = g; e.val = nf;
+      continue;
+    }
+    const uint32_t roll = rng.bounded(100);
+    if (roll < 55) {
+      e.op = OP_REPLACE;
+      e.id = rng.range(0, N);
+      e.val = f.row_amt(e.id) + rng.range(-100000, 100000);
+    } else if (roll < 75) {
+      e.op = OP_INSERT;
+      e.id = N + (int64_t)w.ins_t.size();
+      e.t = rng.range(tmin, tmax + 1);
+      e.g = (int32_t)rng.bounded((uint32_t)G);
+      const int64_t base_amt = f.row_amt(rng.bounded((uint32_t)N));
+      e.val = base_amt + rng.range(-100000, 100000);
+      w.ins_t.push_back(e.t);
+      w.ins_g.push_back(e.g);
+    } else if (roll < 90) {
+      e.op = OP_DELETE;
+      e.id = rng.range(0, N);
+    } else {
+      e.op = OP_MOVE;
+      e.id = rng.range(0, N);
+      e.t = rng.range(tmin, tmax + 1);
+      e.g = (int32_t)rng.bounded((uint32_t)G);
+      e.val = f.row_amt(e.id) + rng.range(-100000, 100000);
+    }
+  }
+  w.endpoints.reserve((size_t)(S - 1) * q * 2);
+  for (int32_t v = 1; v < S; ++v)
+    for (int32_t k = 0; k < q; ++k) {
+      const size_t qi = sp.per_state ? (size_t)v * q + k : (size_t)k;
+      w.endpoints.push_back(w.qlo[qi]);
+      w.endpoints.push_back(w.qhi[qi]);
+    }
+  std::sort(w.endpoints.begin(), w.endpoints.end());
+  w.endpoints.erase(std::unique(w.endpoints.begin(), w.endpoints.end()), w.endpoints.end());
+}
+
+// Per-group support: every class a row of the group can occupy (base rows of the
+// group, inserted/moved rows landing in it); holds the group's alive mass per class.
+struct GroupMass {
+  std::vector<int32_t> cls;
+  std::vector<uint64_t> mass;
+  size_t index(int32_t c) const {
+    return (size_t)(std::lower_bound(cls.begin(), cls.end(), c) - cls.begin());
+  }
+};
+
+struct RowImage {
+  uint8_t ex;
+  int32_t g, c;
+  int64_t amt;
+};
+
+}  // namespace
+
+extern "C" int bw_fixture_open(const char* path, BwFixture** out) {
+  if (!path || !out) return 2;
+  const int fd = ::open(path, O_RDONLY);
+  if (fd < 0) return 3;
+  struct stat st {};
+  if (::fstat(fd, &st) != 0 || st.st_size < 64) { ::close(fd); return 3; }
+  void* m = ::mmap(nullptr, (size_t)st.st_size, PROT_READ, MAP_PRIVATE, fd, 0);
+  ::close(fd);
+  if (m == MAP_FAILED) return 3;
+  BwFixture* f = new (std::nothrow) BwFixture();
+  if (!f) { ::munmap(m, (size_t)st.st_size); return 3; }
+  f->map = m;
+  f->len = (size_t)st.st_size;
+  f->base = static_cast<const uint8_t*>(m);
+  const int rc = parse_fixture(f);
+  if (rc) { delete f; return rc; }
+  *out = f;
+  return 0;
+}
+
+extern "C" int bw_fixture_from_memory(const void* image, size_t len, BwFixture** out) {
+  if (!image || !out) return 2;
+  BwFixture* f = new (std::nothrow) BwFixture();
+  if (!f) return 3;
+  f->copy.assign(static_cast<const uint8_t*>(image), static_cast<const uint8_t*>(image) + len);
+  f->len = len;
+  f->base = f->copy.data();
+  const int rc = parse_fixture(f);
+  if (rc) { delete f; return rc; }
+  *out = f;
+  return 0;
+}
+
+extern "C" void bw_fixture_close(BwFixture* f) { delete f; }
+extern "C" int64_t bw_fixture_rows(const BwFixture* f) { return f ? f->n : 0; }
+
+extern "C" int bw_native_build(const BwFixture* fx, const BwNativeSpec* sp, BwNativeWorkload** out) {
+  if (!fx || !sp || !out || sp->n_states < 2 || sp->q < 1 || sp->topology < 0 || sp->topology > 2)
+    return 2;
+  const BwFixture& f = *fx;
+  Declared w;
+  declare(f, *sp, w);
+  const int32_t S = sp->n_states, q = sp->q, G = f.G;
+  const int64_t N = f.n, M = N + (int64_t)w.ins_t.size();
+  const std::vector<int64_t>& ep = w.endpoints;
+  auto class_of = [&](int64_t t) {
+    return (int32_t)(std::upper_bound(ep.begin(), ep.end(), t) - ep.begin());
+  };
+
+  // row images and group supports
+  std::vector<RowImage> row((size_t)M);
+  std::vector<std::vector<int32_t>> sup(G);
+  for (int64_t i = 0; i < N; ++i) {
+    row[i] = {1, f.row_g(i), class_of(f.row_t(i)), f.row_amt(i)};
+    if (row[i].g < 0 || row[i].g >= G) return 3;
+    sup[row[i].g].push_back(row[i].c);
+  }
+  for (size_t k = 0; k < w.ins_t.size(); ++k) row[N + k] = {0, w.ins_g[k], class_of(w.ins_t[k]), 0};
+  for (int32_t v = 1; v < S; ++v) {
+    const Edit& e = w.edit[v];
+    if (e.op == OP_INSERT || e.op == OP_MOVE) sup[e.g].push_back(class_of(e.t));
+  }
+  std::vector<GroupMass> gm(G);
+  for (int32_t g = 0; g < G; ++g) {
+    std::sort(sup[g].begin(), sup[g].end());
+    sup[g].erase(std::unique(sup[g].begin(), sup[g].end()), sup[g].end());
+    gm[g].cls.swap(sup[g]);
+    gm[g].mass.assign(gm[g].cls.size(), 0);
+  }
+  std::vector<int64_t> fac(G);
+  for (int32_t g = 0; g < G; ++g) fac[g] = f.factor(g);
+
+  std::vector<BwEvent> ev;
+  ev.reserve((size_t)N + 2 * (size_t)S);
+  int64_t n_factor = 0;
+  // state 0: the base relation weighted by the fixture factors
+  for (int64_t i = 0; i < N; ++i) {
+    const RowImage& r = row[i];
+    GroupMass& m = gm[r.g];
+    m.mass[m.index(r.c)] += (uint64_t)r.amt;
+    const uint64_t d = (uint64_t)r.amt * (uint64_t)fac[r.g];
+    if (d) ev.push_back({0u, (uint32_t)r.c, (int64_t)d});
+  }
+
+  // preorder apply/undo over the version tree, children ascending
+  std::vector<int32_t> cnt((size_t)S + 1, 0);
+  for (int32_t v = 1; v < S; ++v) {
+    const int32_t p = w.parent[v];
+    if (p < 0 || p >= v) return 2;
+    ++cnt[p + 1];
+  }
+  for (int32_t v = 0; v < S; ++v) cnt[v + 1] += cnt[v];
+  std::vector<int32_t> kids((size_t)S), cur(cnt.begin(), cnt.end() - 1);
+  for (int32_t v = 1; v < S; ++v) kids[cur[w.parent[v]]++] = v;
+  std::vector<RowImage> undo_row((size_t)S);
+  std::vector<int64_t> undo_fac((size_t)S);
+  std::vector<std::pair<int32_t, int32_t>> st;
+  st.reserve((size_t)S);
+  st.push_back({0, cnt[0]});
+  auto add_mass = [&](const RowImage& r, uint64_t sign_amt) {
+    GroupMass& m = gm[r.g];
+    m.mass[m.index(r.c)] += sign_amt;
+  };
+  while (!st.empty()) {
+    auto& top = st.back();
+    const int32_t v = top.first;
+    if (top.second < cnt[v + 1]) {
+      const int32_t c = kids[top.second++];
+      const Edit& e = w.edit[c];
+      if (e.op == OP_FACTOR) {
+        const uint64_t ds = (uint64_t)e.val - (uint64_t)fac[e.g];
+        const GroupMass& m = gm[e.g];
+        if (ds)
+          for (size_t i = 0; i < m.cls.size(); ++i) {
+            const uint64_t d = ds * m.mass[i];
+            if (d) { ev.push_back({(uint32_t)c, (uint32_t)m.cls[i], (int64_t)d}); ++n_factor; }
+          }
+        undo_fac[c] = fac[e.g];
+        fac[e.g] = e.val;
+      } else {
+        RowImage& r = row[(size_t)e.id];
+        const RowImage old = r;
+        RowImage nw = old;
+        switch (e.op) {
+          case OP_REPLACE: nw.ex = 1; nw.amt = e.val; break;
+          case OP_DELETE: nw.ex = 0; break;
+          default: nw.ex = 1; nw.g = e.g; nw.c = class_of(e.t); nw.amt = e.val; break;  // insert, move
+        }
+        if (old.ex && old.amt != 0)
+          ev.push_back({(uint32_t)c, (uint32_t)old.c,
+                        (int64_t)((uint64_t)0 - (uint64_t)fac[old.g] * (uint64_t)old.amt)});
+        if (nw.ex && nw.amt != 0)
+          ev.push_back({(uint32_t)c, (uint32_t)nw.c, (int64_t)((uint64_t)fac[nw.g] * (uint64_t)nw.amt)});
+        if (old.ex) add_mass(old, (uint64_t)0 - (uint64_t)old.amt);
+        if (nw.ex) add_mass(nw, (uint64_t)nw.amt);
+        undo_row[c] = old;
+        r = nw;
+      }
+      st.push_back({c, cnt[c]});
+    } else {
+      if (v > 0) {
+        const Edit& e = w.edit[v];
+        if (e.op == OP_FACTOR) {
+          fac[e.g] = undo_fac[v];
+        } else {
+          RowImage& r = row[(size_t)e.id];
+          if (r.ex) add_mass(r, (uint64_t)0 - (uint64_t)r.amt);
+          r = undo_row[v];
+          if (r.ex) add_mass(r, (uint64_t)r.amt);
+        }
+      }
+      st.pop_back();
+    }
+  }
+
+  // group events by state (stable counting sort; chains are already in order)
+  BwNativeWorkload* o = new (std::nothrow) BwNativeWorkload();
+  if (!o) return 3;
+  o->n_states = S;
+  o->n_keys = (uint32_t)ep.size() + 1u;
+  o->n_events = (int64_t)ev.size();
+  o->n_queries = (int64_t)(S - 1) * q;
+  o->n_factor_events = n_factor;
+  o->parent = new int32_t[S];
+  std::memcpy(o->parent, w.parent.data(), sizeof(int32_t) * S);
+  o->events = new BwEvent[ev.empty() ? 1 : ev.size()];
+  {
+    std::vector<int64_t> off((size_t)S + 1, 0);
+    for (const BwEvent& x : ev) ++off[x.state + 1];
+    for (int32_t v = 0; v < S; ++v) off[v + 1] += off[v];
+    for (const BwEvent& x : ev) o->events[off[x.state]++] = x;
+  }
+  o->queries = new BwQuery[o->n_queries ? o->n_queries : 1];
+  for (int32_t v = 1; v < S; ++v)
+    for (int32_t k = 0; k < q; ++k) {
+      const size_t qi = sp->per_state ? (size_t)v * q + k : (size_t)k;
+      o->queries[(size_t)(v - 1) * q + k] = {(uint32_t)v, (uint32_t)class_of(w.qlo[qi]),
+                                             (uint32_t)class_of(w.qhi[qi])};
+    }
+  *out = o;
+  return 0;
+}
+
+extern "C" void bw_native_free(BwNativeWorkload* w) {
+  if (!w) return;
+  delete[] w->parent;
+  delete[] w->events;
+  delete[] w->queries;
+  delete w;
+}
+
+// ------------------------------------------------------------------ digests
+namespace {
+// FIPS 180-4 SHA-256; round constants and initial hash derived from the cube and
+// square roots of the first primes with exact integer arithmetic.
+struct Sha256Consts {
+  uint32_t k[64], h0[8];
+  static uint64_t iroot(unsigned __int128 x, int n) {
+    uint64_t lo = 0, hi = (uint64_t)1 << 40;
+    while (lo < hi) {
+      const uint64_t mid = lo + (hi - lo + 1) / 2;
+      unsigned __int128 p = (unsigned __int128)mid * mid;
+      if (n == 3) p *= mid;
+      if (p <= x) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+  }
+  Sha256Consts() {
+    uint32_t primes[64];
+    int np = 0;
+    for (uint32_t c = 2; np < 64; ++c) {
+      bool prime = true;
+      for (int i = 0; i < np && primes[i] * primes[i] <= c; ++i)
+        if (c % primes[i] == 0) { prime = false; break; }
+      if (prime) primes[np++] = c;
+    }
+    for (int i = 0; i < 64; ++i) k[i] = (uint32_t)iroot((unsigned __int128)primes[i] << 96, 3);
+    for (int i = 0; i < 8; ++i) h0[i] = (uint32_t)iroot((unsigned __int128)primes[i] << 64, 2);
+  }
+};
+const Sha256Consts& sha_consts() {
+  static const Sha256Consts c;
+  return c;
+}
+inline uint32_t rotr(uint32_t x, int n) { return (x >> n) | (x << (32 - n)); }
+void sha_compress(uint32_t h[8], const uint8_t* p, const uint32_t* K) {
+  uint32_t w[64];
+  for (int i = 0; i < 16; ++i)
+    w[i] = ((uint32_t)p[4 * i] << 24) | ((uint32_t)p[4 * i + 1] << 16) | ((uint32_t)p[4 * i + 2] << 8) | p[4 * i + 3];
+  for (int i = 16; i < 64; ++i)
+    w[i] = w[i - 16] + (rotr(w[i - 15], 7) ^ rotr(w[i - 15], 18) ^ (w[i - 15] >> 3)) + w[i - 7] +
+           (rotr(w[i - 2], 17) ^ rotr(w[i - 2], 19) ^ (w[i - 2] >> 10));
+  uint32_t a = h[0], b = h[1], c = h[2], d = h[3], e = h[4], f = h[5], g = h[6], hh = h[7];
+  for (int i = 0; i < 64; ++i) {
+    const uint32_t t1 = hh + (rotr(e, 6) ^ rotr(e, 11) ^ rotr(e, 25)) + ((e & f) ^ (~e & g)) + K[i] + w[i];
+    const uint32_t t2 = (rotr(a, 2) ^ rotr(a, 13) ^ rotr(a, 22)) + ((a & b) ^ (a & c) ^ (b & c));
+    hh = g; g = f; f = e; e = d + t1; d = c; c = b; b = a; a = t1 + t2;
+  }
+  h[0] += a; h[1] += b; h[2] += c; h[3] += d; h[4] += e; h[5] += f; h[6] += g; h[7] += hh;
+}
+}  // namespace
+
+extern "C" void bw_sha256_hex(const void* data, size_t n, char out_hex[65]) {
+  const Sha256Consts& C = sha_consts();
+  uint32_t h[8];
+  std::memcpy(h, C.h0, sizeof(h));
+  const uint8_t* p = static_cast<const uint8_t*>(data);
+  const size_t full = n / 64;
+  for (size_t i = 0; i < full; ++i) sha_compress(h, p + 64 * i, C.k);
+  uint8_t tail[128] = {0};
+  const size_t rem = n - full * 64;
+  if (rem) std::memcpy(tail, p + full * 64, rem);
+  tail[rem] = 0x80;
+  const size_t tl = rem < 56 ? 64 : 128;
+  const uint64_t bits = (uint64_t)n * 8u;
+  for (int i = 0; i < 8; ++i) tail[tl - 1 - i] = (uint8_t)(bits >> (8 * i));
+  sha_compress(h, tail, C.k);
+  if (tl == 128) sha_compress(h, tail + 64, C.k);
+  static const char* hx = "0123456789abcdef";
+  for (int i = 0; i < 8; ++i)
+    for (int j = 0; j < 8; ++j) out_hex[8 * i + j] = hx[(h[i] >> (28 - 4 * j)) & 15];
+  out_hex[64] = 0;
+}
+
+// FNV-1a with the reference's offset basis 1469598103934665603 (common.hpp:396-400).
+extern "C" uint64_t bw_fnv1a(const void* data, size_t n) {
+  const uint8_t* p = static_cast<const uint8_t*>(data);
+  uint64_t h = 1469598103934665603ULL;
+  for (size_t i = 0; i < n; ++i) h = (h ^ p[i]) * 1099511628211ULL;
+  return h;
+}
+
+// ------------------------------------------------------------------ v7 chain plan
+// Host-side restatement of the reference's v7 setup for chains in the argument
+// layout of gpu_v7_launch: row-edit previous images (batch_engine_v7.hpp:1123-1230),
+// touched-class coordinates per group (1234-1308), factor plan (1311-1340), base
+// leaf and base mass (1350-1415), merged support (1578-1629), equal state blocks,
+// block-start factors and deviation snapshots (707-830).
+extern "C" int bw_v7_plan_build(const BwFixture* fx, const BwNativeSpec* sp, int32_t blocks, BwV7Plan** out) {
+  if (!fx || !sp || !out || sp->n_states < 3 || sp->q < 1 || sp->topology != 0) return 2;
+  const BwFixture& f = *fx;
+  Declared w;
+  declare(f, *sp, w);
+  const int32_t S = sp->n_states, q = sp->q, G = f.G, VS = S - 1;
+  const int64_t N = f.n;
+  const std::vector<int64_t>& ep = w.endpoints;
+  auto class_of = [&](int64_t t) {
+    return (int32_t)(std::upper_bound(ep.begin(), ep.end(), t) - ep.begin());
+  };
+  const int32_t ncls = (int32_t)ep.size() + 1, Cpfx = ncls + 1;
+  std::vector<int64_t> s0(G);
+  for (int32_t g = 0; g < G; ++g) s0[g] = f.factor(g);
+
+  // node plans: previous image of each edited row = its last image along the chain
+  std::vector<GpuV7Node> nodes((size_t)S);
+  std::memset(nodes.data(), 0, sizeof(GpuV7Node) * (size_t)S);
+  {
+    std::vector<RowImage> img((size_t)(N + (int64_t)w.ins_t.size()));
+    for (int64_t i = 0; i < N; ++i) img[i] = {1, f.row_g(i), class_of(f.row_t(i)), f.row_amt(i)};
+    for (size_t k = 0; k < w.ins_t.size(); ++k) img[N + k] = {0, w.ins_g[k], class_of(w.ins_t[k]), 0};
+    std::vector<int64_t> fcur = s0;
+    for (int32_t v = 1; v < S; ++v) {
+      const Edit& e = w.edit[v];
+      GpuV7Node& p = nodes[v];
+      if (e.op == OP_FACTOR) {
+        p.kind = 2; p.g_old = e.g; p.fac_prev = fcur[e.g]; p.fac_val = e.val;
+        fcur[e.g] = e.val;
+        continue;
+      }
+      RowImage& r = img[(size_t)e.id];
+      p.kind = 1;
+      p.ex_old = r.ex; p.g_old = r.g; p.c_old = r.c; p.amt_old = r.amt;
+      switch (e.op) {
+        case OP_REPLACE: r.ex = 1; r.amt = e.val; break;
+        case OP_DELETE: r.ex = 0; break;
+        default: r.ex = 1; r.g = e.g; r.c = class_of(e.t); r.amt = e.val; break;
+      }
+      p.ex_new = r.ex; p.g_new = r.g; p.c_new = r.c; p.amt_new = r.amt;
+    }
+  }
+  // touched classes per group and the row deviation coordinates
+  std::vector<std::vector<int32_t>> tcoord(G);
+  for (int32_t v = 1; v < S; ++v) {
+    const GpuV7Node& p = nodes[v];
+    if (p.kind != 1) continue;
+    if (p.ex_old && p.amt_old != 0) tcoord[p.g_old].push_back(p.c_old);
+    if (p.ex_new && p.amt_new != 0) tcoord[p.g_new].push_back(p.c_new);
+  }
+  for (auto& t : tcoord) { std::sort(t.begin(), t.end()); t.erase(std::unique(t.begin(), t.end()), t.end()); }
+  auto ti_of = [&](int32_t g, int32_t c) {
+    return (int32_t)(std::lower_bound(tcoord[g].begin(), tcoord[g].end(), c) - tcoord[g].begin());
+  };
+  for (int32_t v = 1; v < S; ++v) {
+    GpuV7Node& p = nodes[v];
+    if (p.kind != 1) continue;
+    if (p.ex_old && p.amt_old != 0) p.ti_old = ti_of(p.g_old, p.c_old);
+    if (p.ex_new && p.amt_new != 0) p.ti_new = ti_of(p.g_new, p.c_new);
+  }
+  // factor-edited groups -> rows
+  std::vector<int32_t> g2row(G, -1);
+  int32_t n_active = 0;
+  {
+    std::vector<uint8_t> touched(G, 0);
+    for (int32_t v = 1; v < S; ++v) if (nodes[v].kind == 2) touched[nodes[v].g_old] = 1;
+    for (int32_t g = 0; g < G; ++g) if (touched[g]) g2row[g] = n_active++;
+  }
+  // root leaf and base mass per (active group, class)
+  std::vector<int64_t> vbase((size_t)Cpfx, 0);
+  std::vector<std::vector<std::pair<int32_t, int64_t>>> gb(n_active);
+  for (int64_t i = 0; i < N; ++i) {
+    const int32_t c = class_of(f.row_t(i)), g = f.row_g(i);
+    vbase[(size_t)c + 1] = (int64_t)((uint64_t)vbase[(size_t)c + 1] + (uint64_t)f.row_amt(i) * (uint64_t)s0[g]);
+    if (g2row[g] >= 0) gb[g2row[g]].push_back({c, f.row_amt(i)});
+  }
+  // merged support: union of nonzero base classes and touched classes, class order
+  std::vector<int32_t> ms_off((size_t)n_active + 1, 0);
+  std::vector<int64_t> ms_cls, ms_base;
+  std::vector<int32_t> ms_dev;
+  for (int32_t g = 0; g < G; ++g) {
+    const int32_t r = g2row[g];
+    if (r < 0) continue;
+    auto& lst = gb[r];
+    std::sort(lst.begin(), lst.end());
+    std::vector<std::pair<int32_t, int64_t>> base;  // (class, mass != 0)
+    for (size_t i = 0; i < lst.size();) {
+      size_t j = i;
+      uint64_t m = 0;
+      while (j < lst.size() && lst[j].first == lst[i].first) m += (uint64_t)lst[j++].second;
+      if (m) base.push_back({lst[i].first, (int64_t)m});
+      i = j;
+    }
+    const auto& tc = tcoord[g];
+    size_t bi = 0, di = 0;
+    while (bi < base.size() || di < tc.size()) {
+      if (di >= tc.size() || (bi < base.size() && base[bi].first < tc[di])) {
+        ms_cls.push_back(base[bi].first); ms_base.push_back(base[bi].second); ms_dev.push_back(-1); ++bi;
+      } else if (bi >= base.size() || tc[di] < base[bi].first) {
+        ms_cls.push_back(tc[di]); ms_base.push_back(0); ms_dev.push_back((int32_t)di); ++di;
+      } else {
+        ms_cls.push_back(base[bi].first); ms_base.push_back(base[bi].second); ms_dev.push_back((int32_t)di);
+        ++bi; ++di;
+      }
+    }
+    ms_off[r + 1] = (int32_t)ms_cls.size();
+  }
+  // blocks, block-start factors, deviation snapshots of the groups each block edits
+  int32_t B = blocks > 0 ? blocks : 1;
+  if (B > VS) B = VS;
+  std::vector<int32_t> v0(B), v1(B), bidx((size_t)S, 0);
+  for (int32_t b = 0; b < B; ++b) {
+    v0[b] = 1 + (int32_t)(((int64_t)VS * b) / B);
+    v1[b] = 1 + (int32_t)(((int64_t)VS * (b + 1)) / B);
+    for (int32_t v = v0[b]; v < v1[b]; ++v) bidx[v] = b;
+  }
+  std::vector<int64_t> fac_start((size_t)B * G), need_off((size_t)B * G, -1);
+  std::vector<std::vector<int32_t>> bgroups(B);
+  for (int32_t v = 1; v < S; ++v) if (nodes[v].kind == 2) bgroups[bidx[v]].push_back(nodes[v].g_old);
+  int64_t ndev = 0;
+  for (int32_t b = 0; b < B; ++b) {
+    auto& gs = bgroups[b];
+    std::sort(gs.begin(), gs.end());
+    gs.erase(std::unique(gs.begin(), gs.end()), gs.end());
+    for (int32_t g : gs) { need_off[(size_t)b * G + g] = ndev; ndev += (int64_t)tcoord[g].size(); }
+  }
+  std::vector<int64_t> devbuf((size_t)(ndev ? ndev : 1), 0);
+  {
+    std::vector<int64_t> fcur = s0;
+    std::vector<std::vector<uint64_t>> dv(G);
+    for (int32_t g = 0; g < G; ++g) dv[g].assign(tcoord[g].size(), 0);
+    int32_t b = 0;
+    for (int32_t v = 1; v < S; ++v) {
+      if (v == v0[b]) {
+        for (int32_t g = 0; g < G; ++g) fac_start[(size_t)b * G + g] = fcur[g];
+        for (int32_t g : bgroups[b])
+          for (size_t k = 0; k < tcoord[g].size(); ++k)
+            devbuf[(size_t)need_off[(size_t)b * G + g] + k] = (int64_t)dv[g][k];
+      }
+      const GpuV7Node& p = nodes[v];
+      if (p.kind == 2) fcur[p.g_old] = p.fac_val;
+      if (p.kind == 1) {
+        if (p.ex_old && p.amt_old != 0) dv[p.g_old][p.ti_old] -= (uint64_t)p.amt_old;
+        if (p.ex_new && p.amt_new != 0) dv[p.g_new][p.ti_new] += (uint64_t)p.amt_new;
+      }
+      if (b + 1 < B && v + 1 == v1[b]) ++b;
+    }
+  }
+  std::vector<int32_t> qlb((size_t)S * q, 0), qhb((size_t)S * q, 0);
+  for (int32_t v = 1; v < S; ++v)
+    for (int32_t k = 0; k < q; ++k) {
+      const size_t qi = sp->per_state ? (size_t)v * q + k : (size_t)k;
+      qlb[(size_t)v * q + k] = class_of(w.qlo[qi]);
+      qhb[(size_t)v * q + k] = class_of(w.qhi[qi]);
+    }
+
+  BwV7Plan* o = new (std::nothrow) BwV7Plan();
+  if (!o) return 3;
+  auto dup = [](const auto& v) {
+    using T = typename std::decay_t<decltype(v)>::value_type;
+    T* p = new T[v.empty() ? 1 : v.size()];
+    if (!v.empty()) std::memcpy(p, v.data(), sizeof(T) * v.size());
+    return p;
+  };
+  o->B = B; o->G = G; o->Cpfx = Cpfx; o->ncls = ncls; o->q = q; o->n_states = S; o->n_active = n_active;
+  o->nodes = dup(nodes); o->block_v0 = dup(v0); o->block_v1 = dup(v1); o->fac_start = dup(fac_start);
+  o->g2row = dup(g2row); o->ms_off = dup(ms_off); o->ms_cls = dup(ms_cls); o->ms_base = dup(ms_base);
+  o->ms_dev = dup(ms_dev); o->devbuf = dup(devbuf); o->n_devbuf = ndev; o->need_off = dup(need_off);
+  o->qlb = dup(qlb); o->qhb = dup(qhb); o->bidx = dup(bidx); o->vbase = dup(vbase);
+  *out = o;
+  return 0;
+}
+
+extern "C" void bw_v7_plan_free(BwV7Plan* p) {
+  if (!p) return;
+  delete[] p->nodes; delete[] p->block_v0; delete[] p->block_v1; delete[] p->fac_start; delete[] p->g2row;
+  delete[] p->ms_off; delete[] p->ms_cls; delete[] p->ms_base; delete[] p->ms_dev; delete[] p->devbuf;
+  delete[] p->need_off; delete[] p->qlb; delete[] p->qhb; delete[] p->bidx; delete[] p->vbase;
+  delete p;
+}

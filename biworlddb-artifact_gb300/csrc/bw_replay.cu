@@ -65,6 +65,8 @@ struct Plan {            // device pointers carved from the workspace
   uint64_t* rank_a;      // 2S  (next:int32 | dist:int32)
   uint64_t* rank_b;      // 2S
   int32_t* steps;        // 2S  (v: enter v, ~v: exit v)
+  int32_t* tin;          // S   step index of enter(v)
+  int32_t* tout;         // S   step index of exit(v) (INT32_MAX when not swept)
   StepDesc* desc;        // 2S
   int64_t* work;         // 2S  inclusive work prefix
   int64_t* scan_tmp;     // scan partials
@@ -178,7 +180,8 @@ __global__ void k_rank_round(const uint64_t* __restrict__ src, uint64_t* __restr
 // Step sequence and per-step descriptors; records the last step that answers
 // queries (steps after it cannot change any answer and are trimmed).
 __global__ void k_steps(const uint64_t* r, int32_t S, const int64_t* eoff, const int64_t* qoff,
-                        int32_t* steps, StepDesc* desc, int32_t* last_q, const int32_t* status) {
+                        int32_t* steps, StepDesc* desc, int32_t* last_q, int32_t* tin, int32_t* tout,
+                        const int32_t* status) {
   if (*status) return;  // offsets or ranks may be incomplete after an input error
   const int64_t n = 2 * (int64_t)S;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
@@ -186,6 +189,7 @@ __global__ void k_steps(const uint64_t* r, int32_t S, const int64_t* eoff, const
     const int32_t v = (int32_t)(x >> 1);
     const bool enter = (x & 1) == 0;
     steps[pos] = enter ? v : ~v;
+    (enter ? tin : tout)[v] = (int32_t)pos;
     StepDesc d;
     d.e0 = eoff[v];
     d.ne = (int32_t)(eoff[v + 1] - eoff[v]);
@@ -202,10 +206,13 @@ __global__ void k_check_chain(const int32_t* parent, int32_t S, int32_t* status)
 }
 // Chain layout without list ranking: step v enters state v.
 __global__ void k_steps_chain(int32_t S, const int64_t* eoff, const int64_t* qoff, int32_t* steps,
-                              StepDesc* desc, int32_t* last_q, const int32_t* status) {
+                              StepDesc* desc, int32_t* last_q, int32_t* tin, int32_t* tout,
+                              const int32_t* status) {
   if (*status) return;
   for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < S; v += gridDim.x * blockDim.x) {
     steps[v] = v;
+    tin[v] = v;
+    tout[v] = 0x7FFFFFFF;  // a chain never leaves a state before the last query
     StepDesc d;
     d.e0 = eoff[v];
     d.ne = (int32_t)(eoff[v + 1] - eoff[v]);
@@ -249,6 +256,9 @@ __global__ void k_bounds(const int64_t* work, int64_t T, int32_t B, int32_t* bou
 struct PrepParams {
   const BwEvent* ev;
   const StepDesc* desc;
+  const int32_t* steps;
+  const int32_t* tin;
+  const int32_t* tout;
   const int32_t* bounds;
   int32_t nwords;
   uint32_t C;
@@ -261,16 +271,25 @@ struct PrepParams {
   int32_t* status;
 };
 
-// Visit every (key, signed delta) of the block's steps; warps take steps round
-// robin, lanes take events.  No ordering is needed for sets and sums.  Loop
+// Visit the (key, signed delta) of the block's steps that matter: mode 0 (key
+// set) skips exits of nodes entered in the block (their keys come with the
+// enter); mode 1 (net deltas) also skips enters of nodes that exit in the block,
+// since the two cancel.  Warps take steps round robin, lanes take events; loop
 // bounds are warp-uniform and f is called by all 32 lanes (valid marks real
 // events), so f may use warp-collective operations.
 template <typename F>
-__device__ __forceinline__ void for_block_events(const PrepParams& p, int32_t t0, int32_t t1, F&& f) {
+__device__ __forceinline__ void for_block_events(const PrepParams& p, int32_t t0, int32_t t1, int mode, F&& f) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int32_t t = t0 + warp; t < t1; t += nw) {
     const StepDesc d = p.desc[t];
     const bool neg = d.nq < 0;
+    const int32_t x = p.steps[t];
+    const int32_t u = x >= 0 ? x : ~x;
+    if (neg) {
+      if (p.tin[u] >= t0) continue;         // entered in this block: keys known, deltas cancel
+    } else if (mode == 1 && p.tout[u] < t1) {
+      continue;                             // leaves within this block: net zero
+    }
     for (int32_t i0 = 0; i0 < d.ne; i0 += 32) {
       const int32_t i = i0 + lane;
       const bool valid = i < d.ne;
@@ -310,7 +329,7 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
     __syncthreads();
     const uint32_t klo = (uint32_t)w0 << 6;
     const uint32_t khi = (uint32_t)imin64((int64_t)(w0 + ww) << 6, (int64_t)p.C);
-    for_block_events(p, t0, t1, [&](uint32_t k, uint64_t, bool valid) {
+    for_block_events(p, t0, t1, 0, [&](uint32_t k, uint64_t, bool valid) {
       if (valid && k >= klo && k < khi) atomicOr(reinterpret_cast<unsigned long long*>(&sbits[(k >> 6) - w0]), 1ull << (k & 63));
     });
     __syncthreads();
@@ -363,10 +382,8 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
     const uint32_t klo = (uint32_t)s.word_lo << 6;
     const uint32_t khi = (uint32_t)imin64((int64_t)s.word_hi << 6, (int64_t)p.C);
     if (s.n) {
-      for_block_events(p, t0, t1, [&](uint32_t k, uint64_t d, bool valid) {
-        const bool in = valid && k >= klo && k < khi;
-        const uint32_t r = in ? local_rank(sbits, srl, k - klo) : 0u;
-        warp_add_aggregated(hist, r, d, in);
+      for_block_events(p, t0, t1, 1, [&](uint32_t k, uint64_t d, bool valid) {
+        if (valid && k >= klo && k < khi) atomicAdd(hist + local_rank(sbits, srl, k - klo), (unsigned long long)d);
       });
     }
     __syncthreads();
@@ -414,36 +431,114 @@ struct SweepParams {
   const int32_t* status;
 };
 
-// Register-staged step data: each thread holds at most one event and one query of
-// a step; steps wider than the CTA fall back to a strided loop.
-struct StepRegs {
-  StepDesc d;
-  uint32_t key;
-  uint64_t delta;
-  uint32_t lo, hi;
-};
+// The sweep keeps the block-local prefix structure in shared memory as 64-rank
+// chunks: a Fenwick tree inside every chunk (levels below the chunk top), the
+// chunk totals T[h], and the exclusive prefix of the chunk totals P[h], rebuilt
+// by one warp before every probe phase.  An update touches only its own chunk
+// (<= 6 shared atomics, no cross-key hot spots); a probe reads P[h] plus <= 6
+// nodes of one chunk.
+constexpr int kSweepThreads = 256;
+constexpr int kChunk = 64;
+constexpr int kStages = 5;                 // shared-memory ring of staged steps
+constexpr int kAhead = kStages - 1;        // steps staged ahead of the one processed
+constexpr int kStageEv = 224;              // events staged per step (more: read from global)
+constexpr int kStageQ = kSweepThreads;     // queries staged per step (thread j owns query j)
+constexpr int kStageBytes = kStageEv * 16 + kStageQ * 12;
 
-__device__ __forceinline__ void load_step(const SweepParams& p, int32_t t, int32_t t1, StepRegs& r) {
-  if (t >= t1) { r.d.ne = 0; r.d.nq = -1; return; }
-  r.d = p.desc[t];
-  const int i = threadIdx.x;
-  if (i < r.d.ne) {
-    const BwEvent e = p.ev[r.d.e0 + i];
-    r.key = e.key;
-    r.delta = (uint64_t)e.delta;
-  }
-  if (i < r.d.nq) {
-    const BwQuery q = p.qs[r.d.q0 + i];
-    r.lo = q.lo;
-    r.hi = q.hi;
-  }
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Shared-memory layout of the sweep for a rank-table window of `ww` words.
+struct SweepLayout {
+  int32_t ww;        // rank-table words reserved
+  int32_t nch;       // chunk capacity
+  uint32_t cap;      // rank capacity = nch * kChunk
+  size_t off_rl, off_fine, off_T, off_P, off_desc, off_stage, bytes;
+};
+__host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budget) {
+  SweepLayout L;
+  L.ww = nwords < kWinWords ? nwords : kWinWords;
+  auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
+  const size_t fixed = al((size_t)L.ww * 8) + al(((size_t)L.ww + 2) * 4) + al(sizeof(StepDesc) * kStages) +
+                       (size_t)kStages * kStageBytes + 16;
+  const size_t per_chunk = kChunk * 8 + 16;  // fine nodes + T + P
+  L.nch = (int32_t)((budget - fixed) / per_chunk);
+  L.cap = (uint32_t)L.nch * kChunk;
+  size_t o = al((size_t)L.ww * 8);
+  L.off_rl = o;   o = al(o + ((size_t)L.ww + 2) * 4);
+  L.off_fine = o; o = al(o + (size_t)L.nch * kChunk * 8);
+  L.off_T = o;    o = al(o + (size_t)L.nch * 8);
+  L.off_P = o;    o = al(o + ((size_t)L.nch + 1) * 8);
+  L.off_desc = o; o = al(o + sizeof(StepDesc) * kStages);
+  L.off_stage = o; o += (size_t)kStages * kStageBytes;
+  L.bytes = o;
+  return L;
 }
 
-__global__ void __launch_bounds__(kThreads) k_sweep(SweepParams p, uint32_t cap) {
+// Stage one step (events, queries) into a ring slot with cp.async; every thread
+// commits one group per call so group counting stays uniform.
+__device__ __forceinline__ void stage_step(const SweepParams& p, const StepDesc& d, bool valid,
+                                           unsigned char* slot, StepDesc* sdesc) {
+  if (threadIdx.x == 0) {
+    StepDesc e = d;
+    if (!valid) { e.ne = 0; e.nq = -1; e.e0 = 0; e.q0 = 0; }
+    *sdesc = e;
+  }
+  if (valid) {
+    const int ne = min(d.ne, kStageEv);
+    for (int i = threadIdx.x; i < ne; i += kSweepThreads) cp_async16(slot + 16 * i, p.ev + d.e0 + i);
+    if (d.nq > 0) {
+      const int words = 3 * min(d.nq, kStageQ);
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + d.q0);
+      unsigned char* dq = slot + kStageEv * 16;
+      for (int w = threadIdx.x; w < words; w += kSweepThreads) cp_async4(dq + 4 * w, src + w);
+    }
+  }
+  cp_async_commit();
+}
+
+__device__ __forceinline__ uint64_t chunk_prefix(const unsigned long long* fine, const unsigned long long* P,
+                                                 uint32_t r) {
+  const uint32_t h = r >> 6;
+  uint64_t v = P[h];
+  const unsigned long long* f = fine + (size_t)h * kChunk;
+#pragma unroll
+  for (int it = 0; it < 6; ++it) {
+    const uint32_t x = (r & 63u);
+    if (x == 0) break;
+    v += f[x];
+    r &= r - 1;
+  }
+  return v;
+}
+
+// Prefix (keys < k) of the slice's contribution.
+__device__ __forceinline__ uint64_t slice_prefix2(const unsigned long long* fine, const unsigned long long* P,
+                                                  uint32_t n, const uint64_t* bits, const uint32_t* rl,
+                                                  uint32_t klo, uint32_t khi, uint32_t k) {
+  if (k <= klo) return 0;
+  const uint32_t r = k >= khi ? n : local_rank(bits, rl, k - klo);
+  return chunk_prefix(fine, P, r);
+}
+
+__global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
   uint64_t* sbits = reinterpret_cast<uint64_t*>(smem);
-  uint32_t* srl = reinterpret_cast<uint32_t*>(sbits + kWinWords);
-  unsigned long long* fen = reinterpret_cast<unsigned long long*>(srl + kWinWords + 2);  // cap + 1
+  uint32_t* srl = reinterpret_cast<uint32_t*>(smem + L.off_rl);
+  unsigned long long* fine = reinterpret_cast<unsigned long long*>(smem + L.off_fine);
+  unsigned long long* T = reinterpret_cast<unsigned long long*>(smem + L.off_T);
+  unsigned long long* P = reinterpret_cast<unsigned long long*>(smem + L.off_P);
+  StepDesc* sdesc = reinterpret_cast<StepDesc*>(smem + L.off_desc);
+  unsigned char* stage = smem + L.off_stage;
 
   if (*p.status) return;  // never index with descriptors of rejected input
   const int b = blockIdx.x;
@@ -460,58 +555,138 @@ __global__ void __launch_bounds__(kThreads) k_sweep(SweepParams p, uint32_t cap)
     const int32_t nwd = s.word_hi - s.word_lo;
     const uint32_t klo = (uint32_t)s.word_lo << 6;
     const uint32_t khi = (uint32_t)imin64((int64_t)s.word_hi << 6, (int64_t)p.C);
+    const uint32_t nch = (s.n + kChunk - 1) / kChunk;
     const bool first = si == 0;
-    for (int i = tid; i < nwd; i += blockDim.x) {
+    for (int i = tid; i < nwd; i += kSweepThreads) {
       sbits[i] = gbits[s.word_lo + i];
       srl[i] = grl[s.word_lo + i] - s.rank_lo;
     }
-    for (uint32_t i = tid; i <= s.n; i += blockDim.x) fen[i] = 0;
+    for (uint32_t i = tid; i < nch * kChunk; i += kSweepThreads) fine[i] = 0;
+    for (uint32_t i = tid; i <= nch; i += kSweepThreads) { T[i < nch ? i : 0] = 0; P[i] = 0; }
     __syncthreads();
 
-    StepRegs cur, nxt;
-    load_step(p, t0, t1, cur);
+    // prologue: stage the first kAhead steps, prefetch the next descriptor
+    for (int u = 0; u < kAhead; ++u) {
+      const int32_t t = t0 + u;
+      StepDesc d{};
+      if (t < t1) d = p.desc[t];
+      stage_step(p, d, t < t1, stage + (size_t)(t % kStages) * kStageBytes, sdesc + (t % kStages));
+    }
+    StepDesc dn{};
+    if (t0 + kAhead < t1) dn = p.desc[t0 + kAhead];
+    cp_async_wait<kAhead - 2>();
+    __syncthreads();
+    // carries of the first step's queries
+    uint64_t c_lo = 0, c_hi = 0, n_lo = 0, n_hi = 0;
+    if (first) {
+      const StepDesc d = sdesc[t0 % kStages];
+      const uint32_t* q = reinterpret_cast<const uint32_t*>(stage + (size_t)(t0 % kStages) * kStageBytes + kStageEv * 16);
+      if (tid < min(d.nq, kStageQ) && q[3 * tid + 2] > q[3 * tid + 1]) {
+        c_lo = (uint64_t)__ldg(crow + q[3 * tid + 1]);
+        c_hi = (uint64_t)__ldg(crow + q[3 * tid + 2]);
+      }
+    }
+    bool dirty = true;  // chunk totals changed since the last coarse rebuild
+
     for (int32_t t = t0; t < t1; ++t) {
-      load_step(p, t + 1, t1, nxt);   // in flight while step t is processed
-      const bool neg = cur.d.nq < 0;
-      // ---- updates of step t
-      if (s.n) {
-        for (int32_t i0 = 0; i0 < cur.d.ne; i0 += blockDim.x) {
-          const int i = i0 + tid;
-          uint32_t k = 0;
-          uint64_t d = 0;
-          if (i < cur.d.ne) {
-            if (i0 == 0) { k = cur.key; d = cur.delta; }
-            else { const BwEvent e = p.ev[cur.d.e0 + i]; k = e.key; d = (uint64_t)e.delta; }
-          }
-          const bool in = i < cur.d.ne && k >= klo && k < khi;
-          const uint32_t r = in ? local_rank(sbits, srl, k - klo) + 1u : 0u;
-          fenwick_add_warp(fen, s.n, r, neg ? (uint64_t)0 - d : d, in);
+      const int slot = t % kStages;
+      // 1. stage step t + kAhead (its slot held step t - 1, finished before the last barrier)
+      {
+        const int32_t ta = t + kAhead;
+        stage_step(p, dn, ta < t1, stage + (size_t)(ta % kStages) * kStageBytes, sdesc + (ta % kStages));
+        if (ta + 1 < t1) dn = p.desc[ta + 1];
+      }
+      // 2. carries of step t + 1's queries (its data landed before the last barrier)
+      if (first && t + 1 < t1) {
+        const int s1 = (t + 1) % kStages;
+        const StepDesc d1 = sdesc[s1];
+        const uint32_t* q = reinterpret_cast<const uint32_t*>(stage + (size_t)s1 * kStageBytes + kStageEv * 16);
+        if (tid < min(d1.nq, kStageQ) && q[3 * tid + 2] > q[3 * tid + 1]) {
+          n_lo = (uint64_t)__ldg(crow + q[3 * tid + 1]);
+          n_hi = (uint64_t)__ldg(crow + q[3 * tid + 2]);
         }
       }
-      __syncthreads();
-      // ---- queries of step t
-      for (int32_t j0 = 0; j0 < cur.d.nq; j0 += blockDim.x) {
-        const int j = j0 + tid;
-        if (j < cur.d.nq) {
+      const StepDesc d = sdesc[slot];
+      const unsigned char* sl = stage + (size_t)slot * kStageBytes;
+      // 3. updates of step t (exit steps remove the node's events)
+      if (s.n && d.ne > 0) {
+        const bool neg = d.nq < 0;
+        for (int i = tid; i < d.ne; i += kSweepThreads) {
+          uint32_t k;
+          uint64_t v;
+          if (i < kStageEv) {
+            const BwEvent* e = reinterpret_cast<const BwEvent*>(sl) + i;
+            k = e->key;
+            v = (uint64_t)e->delta;
+          } else {
+            const BwEvent e = p.ev[d.e0 + i];
+            k = e.key;
+            v = (uint64_t)e.delta;
+          }
+          if (k >= klo && k < khi) {
+            if (neg) v = (uint64_t)0 - v;
+            const uint32_t r = local_rank(sbits, srl, k - klo);
+            const uint32_t h = r >> 6;
+            unsigned long long* f = fine + (size_t)h * kChunk;
+            for (uint32_t x = (r & 63u) + 1u; x < (uint32_t)kChunk; x += x & (0u - x)) atomicAdd(f + x, v);
+            atomicAdd(T + h, v);
+          }
+        }
+        dirty = true;
+      }
+      // 4. queries of step t
+      if (d.nq > 0) {
+        __syncthreads();
+        if (dirty && tid < 32) {
+          // P = exclusive prefix of the chunk totals (one warp)
+          const uint32_t per = (nch + 31) / 32;
+          const uint32_t lo = tid * per, hi = min(nch, lo + per);
+          uint64_t sum = 0;
+          for (uint32_t i = lo; i < hi; ++i) sum += T[i];
+          uint64_t x = sum;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (tid >= o) x += y;
+          }
+          uint64_t run = x - sum;
+          for (uint32_t i = lo; i < hi; ++i) { P[i] = run; run += T[i]; }
+          if (tid == 31) P[nch] = x;
+        }
+        dirty = false;
+        __syncthreads();
+        const uint32_t* q = reinterpret_cast<const uint32_t*>(sl + kStageEv * 16);
+        for (int j = tid; j < d.nq; j += kSweepThreads) {
           uint32_t lo, hi;
-          if (j0 == 0) { lo = cur.lo; hi = cur.hi; }
-          else { const BwQuery q = p.qs[cur.d.q0 + j]; lo = q.lo; hi = q.hi; }
-          int64_t* out = p.answers + cur.d.q0 + j;
+          uint64_t acc = 0;
+          if (j < kStageQ) {
+            lo = q[3 * j + 1];
+            hi = q[3 * j + 2];
+            if (first) acc = c_hi - c_lo;
+          } else {
+            const BwQuery qq = p.qs[d.q0 + j];
+            lo = qq.lo;
+            hi = qq.hi;
+            if (first && hi > lo) acc = (uint64_t)__ldg(crow + hi) - (uint64_t)__ldg(crow + lo);
+          }
+          int64_t* out = p.answers + d.q0 + j;
           if (hi <= lo) {
             if (first) *out = 0;
-          } else {
-            uint64_t acc = 0;
-            if (first) acc = (uint64_t)__ldg(crow + hi) - (uint64_t)__ldg(crow + lo);
-            acc += slice_prefix(fen, s.n, sbits, srl, klo, khi, hi);
-            acc -= slice_prefix(fen, s.n, sbits, srl, klo, khi, lo);
-            if (first) *out = (int64_t)acc;
-            else *out = (int64_t)((uint64_t)*out + acc);
+            continue;
           }
+          acc += slice_prefix2(fine, P, s.n, sbits, srl, klo, khi, hi);
+          acc -= slice_prefix2(fine, P, s.n, sbits, srl, klo, khi, lo);
+          *out = first ? (int64_t)acc : (int64_t)((uint64_t)*out + acc);
         }
       }
+      // 5. step t + 2 staged and visible; slot of step t free
+      cp_async_wait<kAhead - 2>();
       __syncthreads();
-      cur = nxt;
+      c_lo = n_lo; c_hi = n_hi;
+      n_lo = 0; n_hi = 0;
     }
+    cp_async_wait<0>();
+    __syncthreads();
   }
 }
 
@@ -560,18 +735,14 @@ static void layout(const BwReplayArgs* a, int32_t B, Layout& L) {
   take(14, (size_t)B * kMaxSlices * sizeof(Slice));
   take(15, (size_t)B * 4);         // nslices
   take(16, (size_t)B * ((size_t)a->n_keys + 1) * 8);  // carry rows
+  take(17, S * 4);                 // tin
+  take(18, S * 4);                 // tout
   L.total = o;
 }
 
-static uint32_t smem_cap(int32_t nwords, size_t& smem_bytes) {
-  // window bitmap + rank table + Fenwick/histogram of cap+1 int64
-  const int32_t ww = nwords < kWinWords ? nwords : kWinWords;
-  const size_t fixed = (size_t)kWinWords * 8 + ((size_t)kWinWords + 2) * 4;
-  (void)ww;
-  const size_t budget = kSmemLimit - 2048;  // leave room for static shared memory
-  const uint32_t cap = (uint32_t)((budget - fixed) / 8) - 1;
-  smem_bytes = fixed + ((size_t)cap + 1) * 8;
-  return cap;
+// Prepare smem: window bitmap + rank table + histogram of cap+1 int64.
+static size_t prepare_smem(uint32_t cap) {
+  return (size_t)kWinWords * 8 + ((size_t)kWinWords + 2) * 4 + ((size_t)cap + 1) * 8;
 }
 
 struct LastInfo { int32_t kernels = 0, blocks = 0; };
@@ -647,6 +818,8 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
   P.slices = reinterpret_cast<Slice*>(ws + L.off[14]);
   P.nslices = reinterpret_cast<int32_t*>(ws + L.off[15]);
   P.carry = reinterpret_cast<int64_t*>(ws + L.off[16]);
+  P.tin = reinterpret_cast<int32_t*>(ws + L.off[17]);
+  P.tout = reinterpret_cast<int32_t*>(ws + L.off[18]);
 
   const int32_t S = a->n_states;
   const int64_t S2 = 2 * (int64_t)S;
@@ -697,7 +870,7 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
   if (a->flags & BW_REPLAY_CHAIN_HINT) {
     k_check_chain<<<grid, 256, 0, st>>>(a->parent, S, P.misc);
     if ((rc = chk("k_check_chain"))) return rc;
-    k_steps_chain<<<grid, 256, 0, st>>>(S, P.eoff, P.qoff, P.steps, P.desc, P.misc + 1, P.misc);
+    k_steps_chain<<<grid, 256, 0, st>>>(S, P.eoff, P.qoff, P.steps, P.desc, P.misc + 1, P.tin, P.tout, P.misc);
     if ((rc = chk("k_steps_chain"))) return rc;
     T = S;
   } else {
@@ -713,7 +886,7 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
       if ((rc = chk("k_rank_round"))) return rc;
       uint64_t* t = src; src = dst; dst = t;
     }
-    k_steps<<<grid, 256, 0, st>>>(src, S, P.eoff, P.qoff, P.steps, P.desc, P.misc + 1, P.misc);
+    k_steps<<<grid, 256, 0, st>>>(src, S, P.eoff, P.qoff, P.steps, P.desc, P.misc + 1, P.tin, P.tout, P.misc);
     if ((rc = chk("k_steps"))) return rc;
     T = S2;
   }
@@ -730,17 +903,19 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
   if ((rc = chk("k_trim_bounds"))) return rc;
 
   if ((rc = mark(3))) return rc;
-  // ---- 4. prepare
-  size_t smem = 0;
-  const uint32_t cap = smem_cap(nwords, smem);
+  // ---- 4. prepare (slices are sized for the sweep's shared-memory chunk capacity)
+  const SweepLayout SL = sweep_layout(nwords, (size_t)kSmemLimit - 3072);
+  uint32_t cap = SL.cap;
+  while (cap > 64 && prepare_smem(cap) > (size_t)kSmemLimit - 2048) cap -= 64;
+  const size_t smem = prepare_smem(cap);
   static bool attr_done = false;
   if (!attr_done) {
-    if ((rc = report(cudaFuncSetAttribute(k_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr"))) return rc;
-    if ((rc = report(cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr"))) return rc;
+    if ((rc = report(cudaFuncSetAttribute(k_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit - 1024), "smem attr"))) return rc;
+    if ((rc = report(cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit - 1024), "smem attr"))) return rc;
     attr_done = true;
   }
   PrepParams pp;
-  pp.ev = a->events; pp.desc = P.desc; pp.bounds = P.bounds; pp.nwords = nwords; pp.C = C; pp.cap = cap;
+  pp.ev = a->events; pp.desc = P.desc; pp.steps = P.steps; pp.tin = P.tin; pp.tout = P.tout; pp.bounds = P.bounds; pp.nwords = nwords; pp.C = C; pp.cap = cap;
   pp.bits = P.bits; pp.rlut = P.rlut; pp.slices = P.slices; pp.nslices = P.nslices; pp.carry = P.carry;
   pp.status = P.misc;
   k_prepare<<<B, kThreads, smem, st>>>(pp);
@@ -758,7 +933,7 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
     sp.ev = a->events; sp.qs = a->queries; sp.desc = P.desc; sp.bounds = P.bounds; sp.bits = P.bits;
     sp.rlut = P.rlut; sp.slices = P.slices; sp.nslices = P.nslices; sp.carry = P.carry;
     sp.answers = a->answers; sp.nwords = nwords; sp.C = C; sp.status = P.misc;
-    k_sweep<<<B, kThreads, smem, st>>>(sp, cap);
+    k_sweep<<<B, kSweepThreads, SL.bytes, st>>>(sp, SL);
     if ((rc = chk("k_sweep"))) return rc;
   }
   if ((rc = mark(6))) return rc;

@@ -1,0 +1,113 @@
+"""Reference-native parity: BWBASE02 fixtures + declared workloads compiled by the
+host front end (libbwhost.so) must reproduce the reference's answer hashes.
+
+CPU tests check the host front end through the oracle's event-model replay and the
+v7 plan through a Python port of the reference's block executor; GPU tests run the
+same cases through the CUDA replay and through the gpu_v7.h drop-in entry points."""
+from __future__ import annotations
+
+import json
+import zlib
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import v7_emul
+
+GOLD = Path(__file__).resolve().parent / "golden"
+GOLDEN = json.loads((GOLD / "golden.json").read_text())
+CASES = GOLDEN["cases"]
+LARGE = GOLDEN["large_cases"]
+
+
+def fixture(name: str) -> bytes:
+    return zlib.decompress((GOLD / f"{name}.bin.z").read_bytes())
+
+
+def cid(c):
+    return f"{c['fixture']}-S{c['states']}-t{c['topology']}-s{c['seed']}-f{c['factor_period']}-q{c['q']}"
+
+
+def expected(c):
+    return c.get("published") or c.get("reference") or c["oracle"]
+
+
+@pytest.mark.parametrize("case", CASES, ids=cid)
+def test_front_end_events_reproduce_golden(bw, oracle_mod, case):
+    w = bw.native_workload(fixture(case["fixture"]), case["states"], case["topology"], case["seed"],
+                           case["factor_period"], case["q"], case["per_state"])
+    assert len(w.queries) == case["n_answers"]
+    ans = oracle_mod.ev_sweep(w.parent, w.n_keys, w.events, w.queries)
+    assert bw.sha256_hex(ans.tobytes()) == expected(case)
+    assert f"{bw.fnv1a(ans.tobytes()):016x}" == case["fnv1a"]
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c["topology"] == 0 and c["q"] == 2], ids=cid)
+def test_v7_plan_reproduces_golden(bw, case):
+    plan = bw.v7_plan(fixture(case["fixture"]), case["states"], case["seed"], case["factor_period"],
+                      case["q"], blocks=7)
+    ans, _, _ = v7_emul.run(plan)
+    assert bw.sha256_hex(ans.tobytes()) == expected(case)
+
+
+def test_host_sha_matches_oracle(bw, oracle_mod):
+    data = np.arange(1000, dtype=np.int64).tobytes()
+    for n in (0, 3, 55, 64, 100, 8000):
+        assert bw.sha256_hex(data[:n]) == oracle_mod.sha256_hex(data[:n])
+        assert bw.fnv1a(data[:n]) == oracle_mod.fnv1a(data[:n])
+
+
+def test_front_end_rejects_bad_fixture(bw):
+    img = bytearray(fixture("check"))
+    img[0:8] = b"BWBASE99"
+    with pytest.raises(ValueError):
+        bw.native_workload(bytes(img), 33, 0, 1, 4, 2)
+
+
+# ------------------------------------------------------------------------------ GPU
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", CASES, ids=cid)
+def test_gpu_replay_reproduces_golden(bw, torch_cuda, case):
+    import evgen
+    w = bw.native_workload(fixture(case["fixture"]), case["states"], case["topology"], case["seed"],
+                           case["factor_period"], case["q"], case["per_state"])
+    p, e, q = evgen.to_device(torch_cuda, w.parent, w.events, w.queries)
+    ans = bw.replay(p, w.n_keys, e, q, chain=w.chain).cpu().numpy()
+    assert bw.sha256_hex(ans.tobytes()) == expected(case)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", LARGE, ids=cid)
+def test_gpu_replay_large_reference_case(bw, torch_cuda, case):
+    import evgen
+    w = bw.native_workload(fixture(case["fixture"]), case["states"], case["topology"], case["seed"],
+                           case["factor_period"], case["q"], case["per_state"])
+    p, e, q = evgen.to_device(torch_cuda, w.parent, w.events, w.queries)
+    for chain in (True, False):
+        ans = bw.replay(p, w.n_keys, e, q, chain=chain).cpu().numpy()
+        assert bw.sha256_hex(ans.tobytes()) == case["reference"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [c for c in CASES if c["topology"] == 0], ids=cid)
+@pytest.mark.parametrize("blocks", [1, 9, 64])
+def test_gpu_v7_dropin_reproduces_golden(bw, torch_cuda, case, blocks):
+    plan = bw.v7_plan(fixture(case["fixture"]), case["states"], case["seed"], case["factor_period"],
+                      case["q"], blocks=blocks)
+    ans, dV, lvals = bw.run_v7_plan(plan)
+    assert bw.sha256_hex(ans.tobytes()) == expected(case)
+    if case["q"] == 2 and blocks == 9:
+        # intermediate outputs of gpu_v7_launch equal the reference block executor's
+        e_ans, e_dV, e_lvals = v7_emul.run(plan)
+        np.testing.assert_array_equal(dV.reshape(e_dV.shape), e_dV)
+        np.testing.assert_array_equal(lvals, e_lvals)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", LARGE, ids=cid)
+def test_gpu_v7_dropin_large_reference_case(bw, torch_cuda, case):
+    plan = bw.v7_plan(fixture(case["fixture"]), case["states"], case["seed"], case["factor_period"],
+                      case["q"], blocks=128)
+    ans, _, _ = bw.run_v7_plan(plan)
+    assert bw.sha256_hex(ans.tobytes()) == case["reference"]
