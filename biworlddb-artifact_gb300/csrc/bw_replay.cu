@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
     const uint32_t klo = (uint32_t)w0 << 6;
     const uint32_t khi = (uint32_t)imin64((int64_t)(w0 + ww) << 6, (int64_t)p.C);
     for_block_events(p, t0, t1, 0, [&](uint32_t k, uint64_t, bool valid) {
-      if (valid && k >= klo && k < khi) atomicOr(reinterpret_cast<unsigned long long*>(&sbits[(k >> 6) - w0]), 1ull << (k & 63));
+      if (valid && k >= klo && k < khi) shared_set_bit(sbits, k - klo);
     });
     __syncthreads();
     const uint32_t wtot = block_exclusive_scan_popc(sbits, srl, ww);   // srl[0..ww]
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
     const uint32_t khi = (uint32_t)imin64((int64_t)s.word_hi << 6, (int64_t)p.C);
     if (s.n) {
       for_block_events(p, t0, t1, 1, [&](uint32_t k, uint64_t d, bool valid) {
-        if (valid && k >= klo && k < khi) atomicAdd(hist + local_rank(sbits, srl, k - klo), (unsigned long long)d);
+        if (valid && k >= klo && k < khi) shared_add_u64(hist + local_rank(sbits, srl, k - klo), d);
       });
     }
     __syncthreads();
@@ -628,8 +628,8 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLay
             const uint32_t r = local_rank(sbits, srl, k - klo);
             const uint32_t h = r >> 6;
             unsigned long long* f = fine + (size_t)h * kChunk;
-            for (uint32_t x = (r & 63u) + 1u; x < (uint32_t)kChunk; x += x & (0u - x)) atomicAdd(f + x, v);
-            atomicAdd(T + h, v);
+            for (uint32_t x = (r & 63u) + 1u; x < (uint32_t)kChunk; x += x & (0u - x)) shared_add_u64(f + x, v);
+            shared_add_u64(T + h, v);
           }
         }
         dirty = true;

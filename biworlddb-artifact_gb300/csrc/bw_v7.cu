@@ -4,8 +4,8 @@
 // Kernel design (not the reference's): one CTA of 512 threads per state block.
 //  * Row edits touch at most two classes; one warp applies them.
 //  * A factor edit's merged support (batch_engine_v7.hpp:1578-1629) is spread over
-//    all threads; each support class gets one Fenwick point update through the
-//    warp-aggregated update of bw_common.cuh, instead of writing the dense leaf and
+//    all threads; each support class gets one Fenwick point update (32-bit-pair
+//    shared atomics, bw_common.cuh), instead of writing the dense leaf and
 //    rebuilding the whole Fenwick tree in O(C) as gpu_v7.cu:41-71 does.
 //  * The dense block leaf delta lives directly in the caller's dV row (global
 //    memory), so shared memory holds only the Fenwick tree and the factor vector
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(kV7Threads) k_v7_block(GpuV7Args a) {
           if (off >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(a.devbuf + off + p.ti_new),
                                   (unsigned long long)p.amt_new);
         }
-        fenwick_add_warp(fen, (uint32_t)ncls, c1, w, act);
+        if (act) fenwick_add(fen, (uint32_t)ncls, c1, w);
       }
       __syncthreads();
     } else if (p.kind == 2) {
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kV7Threads) k_v7_block(GpuV7Args a) {
               leaf[c1] = (int64_t)((uint64_t)leaf[c1] + d);  // support classes are distinct
             }
           }
-          fenwick_add_warp(fen, (uint32_t)ncls, c1, d, act);
+          if (act) fenwick_add(fen, (uint32_t)ncls, c1, d);
         }
       }
       __syncthreads();
