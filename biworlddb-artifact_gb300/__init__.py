@@ -372,3 +372,32 @@ def run_v7_plan(plan: dict):
     _check(L.gpu_combine_launch(C.byref(ca)), "gpu_combine_launch")
     torch.cuda.synchronize()
     return answers.cpu().numpy(), dV.cpu().numpy(), lvals.cpu().numpy()
+
+
+def replay_noalloc(parent, n_keys: int, events, queries, *, blocks: int = 0, chain: bool = False):
+    """The replay through bw_replay_launch_noalloc: for callers that cannot allocate
+    device memory when they run it, the scratch comes from the library's fixed
+    region instead of a workspace.  Only the answer buffer is created here (by the
+    caller's side, as any output); the native call allocates nothing.  Workloads
+    whose scratch exceeds the region raise ValueError."""
+    torch = _torch()
+    L = gpu_lib()
+    L.bw_replay_launch_noalloc.argtypes = [C.POINTER(BwReplayArgs), C.POINTER(C.c_int32)]
+    a = BwReplayArgs()
+    a.n_states, a.n_keys = int(parent.numel()), int(n_keys)
+    a.n_events, a.n_queries = int(events.shape[0]), int(queries.shape[0])
+    a.blocks, a.flags = int(blocks), BW_REPLAY_CHAIN_HINT if chain else 0
+    answers = torch.empty(a.n_queries, dtype=torch.int64, device=parent.device)
+    a.parent = parent.data_ptr()
+    a.events = events.data_ptr() if a.n_events else None
+    a.queries = queries.data_ptr() if a.n_queries else None
+    a.answers = answers.data_ptr() if a.n_queries else None
+    a.stream = torch.cuda.current_stream(parent.device).cuda_stream
+    st = C.c_int32(0)
+    rc = L.bw_replay_launch_noalloc(C.byref(a), C.byref(st))
+    if rc == BW_EINVAL:
+        raise ValueError("bw_replay_launch_noalloc rejected the call (see stderr)")
+    _check(rc, "bw_replay_launch_noalloc")
+    if st.value:
+        raise ValueError(f"replay input rejected on the device: {STATUS_NAMES.get(st.value, st.value)}")
+    return answers

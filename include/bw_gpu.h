@@ -164,6 +164,19 @@ int bw_replay_last_info(const BwReplayArgs* a, int32_t* kernels, int32_t* blocks
 int bw_replay_timing_reset(void);
 int bw_replay_stage_times(float* ms, int32_t* launches);
 
+/* The replay for callers that cannot allocate device memory when they run it (a
+ * plugin inside a host engine with a fixed memory budget, a loop that must not
+ * block in the allocator).  No counterpart in the reference.  Same arguments and
+ * results as bw_replay_launch, except that a->workspace must be NULL and
+ * a->workspace_bytes 0: the scratch comes from a fixed 32 MiB region compiled into
+ * the library (held by every GPU that loads it until exit); workloads needing more
+ * (bw_replay_workspace_size) are rejected with BW_EINVAL.  Nothing is allocated or
+ * freed.  The first call on a device looks the region up and should come before
+ * any stream capture.  Calls share the region, so calls overlapping on the GPU
+ * race.  A non-NULL host `status` makes the call wait for its stream and receive
+ * the BW_STATUS_* code; NULL returns once the work is enqueued. */
+int bw_replay_launch_noalloc(const BwReplayArgs* a, int32_t* status);
+
 /* Library/device information: SM count of the current device and the library's
  * compile-time architecture tag (e.g. 1030 for sm_103a). */
 int bw_device_info(int32_t* sm_count, int32_t* arch_tag);
