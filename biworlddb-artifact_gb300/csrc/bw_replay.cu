@@ -43,6 +43,7 @@ constexpr int kWinBits = 18;                  // rank window: 2^18 keys per smem
 constexpr int kWinWords = 1 << (kWinBits - 6);
 constexpr int kMaxSlices = 64;                // key slices per block
 constexpr int kSmemLimit = 232448;            // 227 KiB dynamic smem per CTA on sm_100/103
+constexpr int kSmemPerSM = 233472;            // 228 KiB shared memory per SM
 
 struct StepDesc {        // one Euler step, 24 bytes
   int64_t e0;            // first event of the node
@@ -67,6 +68,7 @@ struct Plan {            // device pointers carved from the workspace
   int32_t* steps;        // 2S  (v: enter v, ~v: exit v)
   int32_t* tin;          // S   step index of enter(v)
   int32_t* tout;         // S   step index of exit(v) (INT32_MAX when not swept)
+  int32_t* bmode;        // B   1 = the block's applied |delta| sum is < 2^31
   StepDesc* desc;        // 2S
   int64_t* work;         // 2S  inclusive work prefix
   int64_t* scan_tmp;     // scan partials
@@ -262,19 +264,20 @@ struct PrepParams {
   const int32_t* bounds;
   int32_t nwords;
   uint32_t C;
-  uint32_t cap;
+  uint32_t cap32, cap64;   // slice rank capacity with int32 / int64 sweep nodes
   uint64_t* bits;
   uint32_t* rlut;
   Slice* slices;
   int32_t* nslices;
   int64_t* carry;
   int32_t* status;
+  int32_t* bmode;
 };
 
 // Visit the (key, signed delta) of the block's steps that matter: mode 0 (key
 // set) skips exits of nodes entered in the block (their keys come with the
-// enter); mode 1 (net deltas) also skips enters of nodes that exit in the block,
-// since the two cancel.  Warps take steps round robin, lanes take events; loop
+// enter, flagged by `twice` since the sweep applies them twice); mode 1 (net
+// deltas) also skips enters of nodes that exit in the block, since the two cancel.  Warps take steps round robin, lanes take events; loop
 // bounds are warp-uniform and f is called by all 32 lanes (valid marks real
 // events), so f may use warp-collective operations.
 template <typename F>
@@ -285,9 +288,10 @@ __device__ __forceinline__ void for_block_events(const PrepParams& p, int32_t t0
     const bool neg = d.nq < 0;
     const int32_t x = p.steps[t];
     const int32_t u = x >= 0 ? x : ~x;
+    const bool exits_here = !neg && p.tout[u] < t1;
     if (neg) {
       if (p.tin[u] >= t0) continue;         // entered in this block: keys known, deltas cancel
-    } else if (mode == 1 && p.tout[u] < t1) {
+    } else if (mode == 1 && exits_here) {
       continue;                             // leaves within this block: net zero
     }
     for (int32_t i0 = 0; i0 < d.ne; i0 += 32) {
@@ -300,7 +304,7 @@ __device__ __forceinline__ void for_block_events(const PrepParams& p, int32_t t0
         k = e.key;
         v = neg ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
       }
-      f(k, v, valid);
+      f(k, v, valid, exits_here);
     }
   }
 }
@@ -312,6 +316,7 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
   uint32_t* srl = reinterpret_cast<uint32_t*>(sbits + kWinWords);         // kWinWords + 1
   unsigned long long* hist = reinterpret_cast<unsigned long long*>(srl + kWinWords + 2);  // cap + 1
   __shared__ int32_t s_nsl;
+  __shared__ int32_t s_mode;
   __shared__ uint64_t s_base;
 
   const int b = blockIdx.x;
@@ -321,6 +326,7 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
   Slice* gsl = p.slices + (size_t)b * kMaxSlices;
   if (threadIdx.x == 0) s_nsl = 0;
   uint32_t rank_base = 0;
+  uint64_t mass = 0;  // per-thread partial of the block's applied |delta| sum
 
   // ---- pass A: per window, key bitmap -> rank table -> slices
   for (int32_t w0 = 0; w0 < p.nwords; w0 += kWinWords) {
@@ -329,10 +335,22 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
     __syncthreads();
     const uint32_t klo = (uint32_t)w0 << 6;
     const uint32_t khi = (uint32_t)imin64((int64_t)(w0 + ww) << 6, (int64_t)p.C);
-    for_block_events(p, t0, t1, 0, [&](uint32_t k, uint64_t, bool valid) {
+    for_block_events(p, t0, t1, 0, [&](uint32_t k, uint64_t v, bool valid, bool twice) {
       if (valid && k >= klo && k < khi) shared_set_bit(sbits, k - klo);
+      if (valid && w0 == 0) {
+        // |delta| summed over every application the sweep makes (saturating)
+        const uint64_t a = (v >> 63) ? (uint64_t)0 - v : v;
+        const uint64_t m = (a > (1ull << 33) ? (1ull << 33) : a) << (twice ? 1 : 0);
+        mass = mass + m > (1ull << 40) ? (1ull << 40) : mass + m;   // 512 partials stay < 2^49
+      }
     });
+    if (w0 == 0) {
+      uint64_t tot = 0;
+      block_exclusive_scan<uint64_t>(mass, &tot);   // block total
+      if (threadIdx.x == 0) s_mode = tot < (1ull << 31) ? 1 : 0;
+    }
     __syncthreads();
+    const uint32_t cap = s_mode ? p.cap32 : p.cap64;
     const uint32_t wtot = block_exclusive_scan_popc(sbits, srl, ww);   // srl[0..ww]
     for (int i = threadIdx.x; i < ww; i += blockDim.x) {
       gbits[w0 + i] = sbits[i];
@@ -344,7 +362,7 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
       int32_t lo = 0;
       while (lo < ww) {
         int32_t hi = lo + 1;
-        while (hi < ww && srl[hi + 1] - srl[lo] <= p.cap) ++hi;
+        while (hi < ww && srl[hi + 1] - srl[lo] <= cap) ++hi;
         if (ns < kMaxSlices) {
           Slice s;
           s.word_lo = w0 + lo; s.word_hi = w0 + hi;
@@ -363,6 +381,7 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
     grl[p.nwords] = rank_base;
     if (s_nsl > kMaxSlices) set_status(p.status, BW_STATUS_TOO_MANY_SLICES);
     p.nslices[b] = min(s_nsl, kMaxSlices);
+    p.bmode[b] = s_mode;
   }
   __syncthreads();
   const int32_t nsl = min(s_nsl, kMaxSlices);
@@ -382,7 +401,7 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
     const uint32_t klo = (uint32_t)s.word_lo << 6;
     const uint32_t khi = (uint32_t)imin64((int64_t)s.word_hi << 6, (int64_t)p.C);
     if (s.n) {
-      for_block_events(p, t0, t1, 1, [&](uint32_t k, uint64_t d, bool valid) {
+      for_block_events(p, t0, t1, 1, [&](uint32_t k, uint64_t d, bool valid, bool) {
         if (valid && k >= klo && k < khi) shared_add_u64(hist + local_rank(sbits, srl, k - klo), d);
       });
     }
@@ -403,13 +422,19 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
 // key-prefix rows, i.e. the key prefix of the state vector at block b's start.
 __global__ void k_carry(int64_t* carry, int32_t B, int64_t width, const int32_t* status) {
   if (*status) return;
+  constexpr int kRows = 8;  // row loads kept in flight per column
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < width; k += (int64_t)gridDim.x * blockDim.x) {
     uint64_t run = 0;
     int64_t* p = carry + k;
-    for (int32_t b = 0; b < B; ++b) {
-      const uint64_t v = (uint64_t)p[(size_t)b * width];
-      p[(size_t)b * width] = (int64_t)run;
-      run += v;
+    for (int32_t b0 = 0; b0 < B; b0 += kRows) {
+      uint64_t v[kRows];
+#pragma unroll
+      for (int i = 0; i < kRows; ++i) v[i] = b0 + i < B ? (uint64_t)p[(size_t)(b0 + i) * width] : 0;
+#pragma unroll
+      for (int i = 0; i < kRows; ++i) {
+        if (b0 + i < B) p[(size_t)(b0 + i) * width] = (int64_t)run;
+        run += v[i];
+      }
     }
   }
 }
@@ -429,6 +454,7 @@ struct SweepParams {
   int32_t nwords;
   uint32_t C;
   const int32_t* status;
+  const int32_t* bmode;   // per block: 1 = int32 Fenwick nodes are exact, 0 = int64
 };
 
 // The sweep keeps the block-local prefix structure in shared memory as 64-rank
@@ -438,12 +464,17 @@ struct SweepParams {
 // (<= 6 shared atomics, no cross-key hot spots); a probe reads P[h] plus <= 6
 // nodes of one chunk.
 constexpr int kSweepThreads = 256;
-constexpr int kChunk = 64;
-constexpr int kStages = 5;                 // shared-memory ring of staged steps
+constexpr int kChunk = 256;
+constexpr int kChunkBits = 8;
+constexpr int kChunkLevels = 8;            // Fenwick levels inside a chunk (below its top)
+constexpr int kChunkStride = 257;          // words per chunk: odd stride spreads node x of
+                                           // different chunks over different banks
+constexpr int kStages = 4;                 // shared-memory ring of staged steps
 constexpr int kAhead = kStages - 1;        // steps staged ahead of the one processed
 constexpr int kStageEv = 224;              // events staged per step (more: read from global)
 constexpr int kStageQ = kSweepThreads;     // queries staged per step (thread j owns query j)
 constexpr int kStageBytes = kStageEv * 16 + kStageQ * 12;
+constexpr int kRebuildPer = 5;             // chunk totals per lane in the coarse rebuild (nch <= 128)
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
@@ -457,11 +488,16 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// Shared-memory layout of the sweep for a rank-table window of `ww` words.
+// Shared-memory layout of the sweep for a rank-table window of `ww` words.  The
+// Fenwick nodes of a block are int32 when the block's applied |delta| sum is below
+// 2^31 (every node value is a sum of a subset of those deltas, so it cannot
+// overflow) and int64 otherwise; the same byte budget then holds twice as many
+// int32 chunks.  Chunk totals and their prefix are always int64.
 struct SweepLayout {
-  int32_t ww;        // rank-table words reserved
-  int32_t nch;       // chunk capacity
-  uint32_t cap;      // rank capacity = nch * kChunk
+  int32_t ww;          // rank-table words reserved
+  int32_t nch32;       // chunk capacity with int32 nodes
+  int32_t nch64;       // chunk capacity with int64 nodes
+  uint32_t cap32, cap64;  // rank capacities
   size_t off_rl, off_fine, off_T, off_P, off_desc, off_stage, bytes;
 };
 __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budget) {
@@ -469,15 +505,19 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   L.ww = nwords < kWinWords ? nwords : kWinWords;
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const size_t fixed = al((size_t)L.ww * 8) + al(((size_t)L.ww + 2) * 4) + al(sizeof(StepDesc) * kStages) +
-                       (size_t)kStages * kStageBytes + 16;
-  const size_t per_chunk = kChunk * 8 + 16;  // fine nodes + T + P
-  L.nch = (int32_t)((budget - fixed) / per_chunk);
-  L.cap = (uint32_t)L.nch * kChunk;
+                       (size_t)kStages * kStageBytes + 64;
+  const size_t per32 = (size_t)kChunkStride * 4 + 16;   // int32 nodes + T + P per chunk
+  int32_t n32 = (int32_t)((budget - fixed) / per32);
+  if (n32 > 128) n32 = 128;
+  L.nch32 = n32;
+  L.nch64 = (int32_t)(((size_t)n32 * kChunkStride * 4) / ((size_t)kChunkStride * 8));
+  L.cap32 = (uint32_t)L.nch32 * kChunk;
+  L.cap64 = (uint32_t)L.nch64 * kChunk;
   size_t o = al((size_t)L.ww * 8);
   L.off_rl = o;   o = al(o + ((size_t)L.ww + 2) * 4);
-  L.off_fine = o; o = al(o + (size_t)L.nch * kChunk * 8);
-  L.off_T = o;    o = al(o + (size_t)L.nch * 8);
-  L.off_P = o;    o = al(o + ((size_t)L.nch + 1) * 8);
+  L.off_fine = o; o = al(o + (size_t)n32 * kChunkStride * 4);
+  L.off_T = o;    o = al(o + (size_t)n32 * 8);
+  L.off_P = o;    o = al(o + ((size_t)n32 + 1) * 8);
   L.off_desc = o; o = al(o + sizeof(StepDesc) * kStages);
   L.off_stage = o; o += (size_t)kStages * kStageBytes;
   L.bytes = o;
@@ -493,54 +533,106 @@ __device__ __forceinline__ void stage_step(const SweepParams& p, const StepDesc&
     if (!valid) { e.ne = 0; e.nq = -1; e.e0 = 0; e.q0 = 0; }
     *sdesc = e;
   }
-  if (valid) {
-    const int ne = min(d.ne, kStageEv);
-    for (int i = threadIdx.x; i < ne; i += kSweepThreads) cp_async16(slot + 16 * i, p.ev + d.e0 + i);
-    if (d.nq > 0) {
+  if (valid && threadIdx.x < 64) {
+    // warp 0 copies the events, warp 1 the queries; the other warps skip staging
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) {
+      const int ne = min(d.ne, kStageEv);
+      for (int i = lane; i < ne; i += 32) cp_async16(slot + 16 * i, p.ev + d.e0 + i);
+    } else if (d.nq > 0) {
       const int words = 3 * min(d.nq, kStageQ);
       const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + d.q0);
       unsigned char* dq = slot + kStageEv * 16;
-      for (int w = threadIdx.x; w < words; w += kSweepThreads) cp_async4(dq + 4 * w, src + w);
+      for (int w = lane; w < words; w += 32) cp_async4(dq + 4 * w, src + w);
     }
   }
   cp_async_commit();
 }
 
-__device__ __forceinline__ uint64_t chunk_prefix(const unsigned long long* fine, const unsigned long long* P,
-                                                 uint32_t r) {
-  const uint32_t h = r >> 6;
-  uint64_t v = P[h];
-  const unsigned long long* f = fine + (size_t)h * kChunk;
+// Point update of one chunk: the Fenwick nodes above local index l (l in
+// 1..kChunk, stopping below the chunk top, at most kChunkLevels nodes) and the
+// chunk total.  int64 nodes
+// use exact 32-bit-pair atomics with all low-word atomics issued before any
+// high-word one (one shared-atomic round trip, not six); int32 nodes take plain
+// 32-bit atomics with no return value.
+template <typename Node>
+__device__ __forceinline__ void chunk_add(Node* f, unsigned long long* tot, uint32_t l, uint64_t v) {
+  const unsigned lo = (unsigned)v, hi = (unsigned)(v >> 32);
+  unsigned* tw = reinterpret_cast<unsigned*>(tot);
+  if constexpr (sizeof(Node) == 4) {
+    uint32_t x = l;
 #pragma unroll
-  for (int it = 0; it < 6; ++it) {
-    const uint32_t x = (r & 63u);
-    if (x == 0) break;
-    v += f[x];
-    r &= r - 1;
+    for (int lv = 0; lv < kChunkLevels; ++lv) {
+      if (x < (uint32_t)kChunk) atomicAdd(reinterpret_cast<unsigned*>(f) + x, lo);
+      x += x & (0u - x);
+    }
+    shared_add_u64(tot, v);
+  } else {
+    unsigned* fw = reinterpret_cast<unsigned*>(f);
+    unsigned old[kChunkLevels];
+    uint32_t x = l;
+#pragma unroll
+    for (int lv = 0; lv < kChunkLevels; ++lv) {
+      if (x < (uint32_t)kChunk) old[lv] = atomicAdd(fw + 2 * x, lo);
+      x += x & (0u - x);
+    }
+    const unsigned oldt = atomicAdd(tw, lo);
+    x = l;
+#pragma unroll
+    for (int lv = 0; lv < kChunkLevels; ++lv) {
+      if (x < (uint32_t)kChunk) {
+        const unsigned h = hi + ((old[lv] + lo) < old[lv] ? 1u : 0u);
+        if (h) atomicAdd(fw + 2 * x + 1, h);
+      }
+      x += x & (0u - x);
+    }
+    const unsigned ht = hi + ((oldt + lo) < oldt ? 1u : 0u);
+    if (ht) atomicAdd(tw + 1, ht);
+  }
+}
+
+template <typename Node>
+__device__ __forceinline__ uint64_t node_value(Node x) {
+  if constexpr (sizeof(Node) == 4) return (uint64_t)(int64_t)(int32_t)x;
+  else return (uint64_t)x;
+}
+
+// Prefix of ranks < r: coarse prefix of the chunk plus the in-chunk Fenwick nodes
+// (<= kChunkLevels, indices known up front so the loads issue together).
+template <typename Node>
+__device__ __forceinline__ uint64_t chunk_prefix(const Node* fine, const unsigned long long* P, uint32_t r) {
+  const uint32_t h = r >> kChunkBits;
+  const Node* f = fine + (size_t)h * kChunkStride;
+  uint64_t v = P[h];
+  uint32_t x = r & (kChunk - 1u);
+#pragma unroll
+  for (int it = 0; it < kChunkLevels; ++it) {
+    if (x) v += node_value(f[x]);
+    x &= x - 1;
   }
   return v;
 }
 
 // Prefix (keys < k) of the slice's contribution.
-__device__ __forceinline__ uint64_t slice_prefix2(const unsigned long long* fine, const unsigned long long* P,
-                                                  uint32_t n, const uint64_t* bits, const uint32_t* rl,
-                                                  uint32_t klo, uint32_t khi, uint32_t k) {
+template <typename Node>
+__device__ __forceinline__ uint64_t slice_prefix2(const Node* fine, const unsigned long long* P, uint32_t n,
+                                                  const uint64_t* bits, const uint32_t* rl, uint32_t klo,
+                                                  uint32_t khi, uint32_t k) {
   if (k <= klo) return 0;
   const uint32_t r = k >= khi ? n : local_rank(bits, rl, k - klo);
   return chunk_prefix(fine, P, r);
 }
 
-__global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLayout L) {
-  extern __shared__ __align__(16) unsigned char smem[];
+template <typename Node>
+__device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLayout& L, unsigned char* smem) {
   uint64_t* sbits = reinterpret_cast<uint64_t*>(smem);
   uint32_t* srl = reinterpret_cast<uint32_t*>(smem + L.off_rl);
-  unsigned long long* fine = reinterpret_cast<unsigned long long*>(smem + L.off_fine);
+  Node* fine = reinterpret_cast<Node*>(smem + L.off_fine);
   unsigned long long* T = reinterpret_cast<unsigned long long*>(smem + L.off_T);
   unsigned long long* P = reinterpret_cast<unsigned long long*>(smem + L.off_P);
   StepDesc* sdesc = reinterpret_cast<StepDesc*>(smem + L.off_desc);
   unsigned char* stage = smem + L.off_stage;
 
-  if (*p.status) return;  // never index with descriptors of rejected input
   const int b = blockIdx.x;
   const int32_t t0 = p.bounds[b], t1 = p.bounds[b + 1];
   if (t0 >= t1) return;
@@ -561,7 +653,7 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLay
       sbits[i] = gbits[s.word_lo + i];
       srl[i] = grl[s.word_lo + i] - s.rank_lo;
     }
-    for (uint32_t i = tid; i < nch * kChunk; i += kSweepThreads) fine[i] = 0;
+    for (uint32_t i = tid; i < nch * kChunkStride; i += kSweepThreads) fine[i] = 0;
     for (uint32_t i = tid; i <= nch; i += kSweepThreads) { T[i < nch ? i : 0] = 0; P[i] = 0; }
     __syncthreads();
 
@@ -577,18 +669,21 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLay
     cp_async_wait<kAhead - 2>();
     __syncthreads();
     // carries of the first step's queries
-    uint64_t c_lo = 0, c_hi = 0, n_lo = 0, n_hi = 0;
+    uint64_t ca_lo = 0, ca_hi = 0, cb_lo = 0, cb_hi = 0;
     if (first) {
       const StepDesc d = sdesc[t0 % kStages];
       const uint32_t* q = reinterpret_cast<const uint32_t*>(stage + (size_t)(t0 % kStages) * kStageBytes + kStageEv * 16);
       if (tid < min(d.nq, kStageQ) && q[3 * tid + 2] > q[3 * tid + 1]) {
-        c_lo = (uint64_t)__ldg(crow + q[3 * tid + 1]);
-        c_hi = (uint64_t)__ldg(crow + q[3 * tid + 2]);
+        ca_lo = (uint64_t)__ldg(crow + q[3 * tid + 1]);
+        ca_hi = (uint64_t)__ldg(crow + q[3 * tid + 2]);
       }
     }
     bool dirty = true;  // chunk totals changed since the last coarse rebuild
 
-    for (int32_t t = t0; t < t1; ++t) {
+    // One step.  The carries of step t arrive in (c_lo, c_hi); the carries of step
+    // t + 1 are loaded into (n_lo, n_hi).  The loop below alternates the two
+    // register pairs statically, so no register copy waits on a pending load.
+    auto step = [&](int32_t t, uint64_t& c_lo, uint64_t& c_hi, uint64_t& n_lo, uint64_t& n_hi) {
       const int slot = t % kStages;
       // 1. stage step t + kAhead (its slot held step t - 1, finished before the last barrier)
       {
@@ -626,10 +721,8 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLay
           if (k >= klo && k < khi) {
             if (neg) v = (uint64_t)0 - v;
             const uint32_t r = local_rank(sbits, srl, k - klo);
-            const uint32_t h = r >> 6;
-            unsigned long long* f = fine + (size_t)h * kChunk;
-            for (uint32_t x = (r & 63u) + 1u; x < (uint32_t)kChunk; x += x & (0u - x)) shared_add_u64(f + x, v);
-            shared_add_u64(T + h, v);
+            chunk_add<Node>(fine + (size_t)(r >> kChunkBits) * kChunkStride, T + (r >> kChunkBits),
+                            (r & (kChunk - 1u)) + 1u, v);
           }
         }
         dirty = true;
@@ -638,11 +731,17 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLay
       if (d.nq > 0) {
         __syncthreads();
         if (dirty && tid < 32) {
-          // P = exclusive prefix of the chunk totals (one warp)
-          const uint32_t per = (nch + 31) / 32;
-          const uint32_t lo = tid * per, hi = min(nch, lo + per);
+          // P = exclusive prefix of the chunk totals (one warp, <= kRebuildPer
+          // contiguous chunks per lane, loads issued together)
+          const uint32_t per = ((nch + 31) / 32) | 1u;  // odd: lanes hit different banks
+          const uint32_t lo = tid * per;
+          uint64_t tv[kRebuildPer];
           uint64_t sum = 0;
-          for (uint32_t i = lo; i < hi; ++i) sum += T[i];
+#pragma unroll
+          for (int i = 0; i < kRebuildPer; ++i) {
+            tv[i] = ((uint32_t)i < per && lo + i < nch) ? T[lo + i] : 0;
+            sum += tv[i];
+          }
           uint64_t x = sum;
 #pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
@@ -650,7 +749,11 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLay
             if (tid >= o) x += y;
           }
           uint64_t run = x - sum;
-          for (uint32_t i = lo; i < hi; ++i) { P[i] = run; run += T[i]; }
+#pragma unroll
+          for (int i = 0; i < kRebuildPer; ++i) {
+            if ((uint32_t)i < per && lo + i < nch) P[lo + i] = run;
+            run += tv[i];
+          }
           if (tid == 31) P[nch] = x;
         }
         dirty = false;
@@ -682,26 +785,35 @@ __global__ void __launch_bounds__(kSweepThreads) k_sweep(SweepParams p, SweepLay
       // 5. step t + 2 staged and visible; slot of step t free
       cp_async_wait<kAhead - 2>();
       __syncthreads();
-      c_lo = n_lo; c_hi = n_hi;
-      n_lo = 0; n_hi = 0;
+    };
+    for (int32_t t = t0; t < t1; t += 2) {
+      step(t, ca_lo, ca_hi, cb_lo, cb_hi);
+      if (t + 1 < t1) step(t + 1, cb_lo, cb_hi, ca_lo, ca_hi);
     }
     cp_async_wait<0>();
     __syncthreads();
   }
 }
 
+__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(SweepParams p, SweepLayout L) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (*p.status) return;  // never index with descriptors of rejected input
+  if (p.bmode[blockIdx.x]) sweep_block<unsigned>(p, L, smem);
+  else sweep_block<unsigned long long>(p, L, smem);
+}
+
 // ------------------------------------------------------------------ host side
 static inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct Layout {
-  size_t off[20];
+  size_t off[24];
   size_t total;
 };
 
 static int32_t pick_blocks(const BwReplayArgs* a, int sms) {
   if (a->blocks > 0) return a->blocks;
   const int64_t work = a->n_events * 2 + a->n_queries * kQueryCost + (int64_t)a->n_states * 2 * kStepCost;
-  int64_t B = sms;
+  int64_t B = 2 * (int64_t)sms;                    // two sweep CTAs per SM hide each other's latency
   const int64_t min_work = 65536;                  // below this a block is launch-dominated
   if (work / min_work < B) B = work / min_work;
   const double carry_budget = 4.0e9;               // bytes of dense carry rows
@@ -737,6 +849,7 @@ static void layout(const BwReplayArgs* a, int32_t B, Layout& L) {
   take(16, (size_t)B * ((size_t)a->n_keys + 1) * 8);  // carry rows
   take(17, S * 4);                 // tin
   take(18, S * 4);                 // tout
+  take(19, (size_t)B * 4);         // bmode
   L.total = o;
 }
 
@@ -820,6 +933,7 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
   P.carry = reinterpret_cast<int64_t*>(ws + L.off[16]);
   P.tin = reinterpret_cast<int32_t*>(ws + L.off[17]);
   P.tout = reinterpret_cast<int32_t*>(ws + L.off[18]);
+  P.bmode = reinterpret_cast<int32_t*>(ws + L.off[19]);
 
   const int32_t S = a->n_states;
   const int64_t S2 = 2 * (int64_t)S;
@@ -903,11 +1017,15 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
   if ((rc = chk("k_trim_bounds"))) return rc;
 
   if ((rc = mark(3))) return rc;
-  // ---- 4. prepare (slices are sized for the sweep's shared-memory chunk capacity)
-  const SweepLayout SL = sweep_layout(nwords, (size_t)kSmemLimit - 3072);
-  uint32_t cap = SL.cap;
-  while (cap > 64 && prepare_smem(cap) > (size_t)kSmemLimit - 2048) cap -= 64;
-  const size_t smem = prepare_smem(cap);
+  // ---- 4. prepare (slices are sized for the sweep's shared-memory chunk capacity;
+  // two sweep CTAs share an SM when there are at least two blocks per SM)
+  const int ctas_per_sm = B >= 2 * sms ? 2 : 1;
+  const size_t sweep_budget = (size_t)(kSmemPerSM / ctas_per_sm) - 3072;
+  const SweepLayout SL = sweep_layout(nwords, sweep_budget);
+  uint32_t cap32 = SL.cap32, cap64 = SL.cap64;
+  while (cap32 > 64 && prepare_smem(cap32) > (size_t)kSmemLimit - 2048) cap32 -= 64;
+  if (cap64 > cap32) cap64 = cap32;
+  const size_t smem = prepare_smem(cap32);
   static bool attr_done = false;
   if (!attr_done) {
     if ((rc = report(cudaFuncSetAttribute(k_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit - 1024), "smem attr"))) return rc;
@@ -915,9 +1033,9 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
     attr_done = true;
   }
   PrepParams pp;
-  pp.ev = a->events; pp.desc = P.desc; pp.steps = P.steps; pp.tin = P.tin; pp.tout = P.tout; pp.bounds = P.bounds; pp.nwords = nwords; pp.C = C; pp.cap = cap;
+  pp.ev = a->events; pp.desc = P.desc; pp.steps = P.steps; pp.tin = P.tin; pp.tout = P.tout; pp.bounds = P.bounds; pp.nwords = nwords; pp.C = C; pp.cap32 = cap32; pp.cap64 = cap64;
   pp.bits = P.bits; pp.rlut = P.rlut; pp.slices = P.slices; pp.nslices = P.nslices; pp.carry = P.carry;
-  pp.status = P.misc;
+  pp.status = P.misc; pp.bmode = P.bmode;
   k_prepare<<<B, kThreads, smem, st>>>(pp);
   if ((rc = chk("k_prepare"))) return rc;
 
@@ -932,7 +1050,7 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
     SweepParams sp;
     sp.ev = a->events; sp.qs = a->queries; sp.desc = P.desc; sp.bounds = P.bounds; sp.bits = P.bits;
     sp.rlut = P.rlut; sp.slices = P.slices; sp.nslices = P.nslices; sp.carry = P.carry;
-    sp.answers = a->answers; sp.nwords = nwords; sp.C = C; sp.status = P.misc;
+    sp.answers = a->answers; sp.nwords = nwords; sp.C = C; sp.status = P.misc; sp.bmode = P.bmode;
     k_sweep<<<B, kSweepThreads, SL.bytes, st>>>(sp, SL);
     if ((rc = chk("k_sweep"))) return rc;
   }
