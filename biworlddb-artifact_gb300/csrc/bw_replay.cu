@@ -457,24 +457,32 @@ struct SweepParams {
   const int32_t* bmode;   // per block: 1 = int32 Fenwick nodes are exact, 0 = int64
 };
 
-// The sweep keeps the block-local prefix structure in shared memory as 64-rank
-// chunks: a Fenwick tree inside every chunk (levels below the chunk top), the
-// chunk totals T[h], and the exclusive prefix of the chunk totals P[h], rebuilt
-// by one warp before every probe phase.  An update touches only its own chunk
-// (<= 6 shared atomics, no cross-key hot spots); a probe reads P[h] plus <= 6
-// nodes of one chunk.
+// The sweep keeps the block-local prefix structure in shared memory as chunks of
+// kChunk ranks: a Fenwick tree inside every chunk (levels below the chunk top),
+// the chunk totals T[h], and per-warp copies of the exclusive prefix of the chunk
+// totals, rebuilt by each warp before every probe phase.  An update touches only
+// its own chunk; a probe reads the prefix copy plus <= kChunkLevels nodes.
+//
+// Staging is per thread: thread i prefetches, with cp.async, event i and query i
+// of the step kAhead ahead into its own slots and waits for them with its own
+// wait_group, so staging needs no barrier.  Barriers only order the Fenwick: after
+// the updates of a step that has queries (probes must see them) and after its
+// probes (the next updates must not run under them).  Steps without queries (the
+// exits of a tree walk, states without queries) run back to back with none.
+// Step descriptors come from a shared ring refilled every kDescRefill steps.
 constexpr int kSweepThreads = 256;
+constexpr int kSweepWarps = kSweepThreads / 32;
 constexpr int kChunk = 256;
 constexpr int kChunkBits = 8;
 constexpr int kChunkLevels = 8;            // Fenwick levels inside a chunk (below its top)
 constexpr int kChunkStride = 257;          // words per chunk: odd stride spreads node x of
                                            // different chunks over different banks
-constexpr int kStages = 4;                 // shared-memory ring of staged steps
-constexpr int kAhead = kStages - 1;        // steps staged ahead of the one processed
-constexpr int kStageEv = 224;              // events staged per step (more: read from global)
-constexpr int kStageQ = kSweepThreads;     // queries staged per step (thread j owns query j)
-constexpr int kStageBytes = kStageEv * 16 + kStageQ * 12;
-constexpr int kRebuildPer = 5;             // chunk totals per lane in the coarse rebuild (nch <= 128)
+constexpr int kMaxChunks = 128;
+constexpr int kAhead = 3;                  // steps prefetched ahead of the one processed
+constexpr int kSlots = kAhead + 1;         // per-thread prefetch slots
+constexpr int kDescRing = 64;              // step descriptors held in shared memory
+constexpr int kDescRefill = 32;            // ring refill period in steps
+constexpr int kRebuildPer = 5;             // chunk totals per lane in a prefix rebuild
 
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
@@ -492,23 +500,23 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // Fenwick nodes of a block are int32 when the block's applied |delta| sum is below
 // 2^31 (every node value is a sum of a subset of those deltas, so it cannot
 // overflow) and int64 otherwise; the same byte budget then holds twice as many
-// int32 chunks.  Chunk totals and their prefix are always int64.
+// int32 chunks.  Chunk totals and prefixes are always int64.
 struct SweepLayout {
-  int32_t ww;          // rank-table words reserved
-  int32_t nch32;       // chunk capacity with int32 nodes
-  int32_t nch64;       // chunk capacity with int64 nodes
+  int32_t ww;             // rank-table words reserved
+  int32_t nch32, nch64;   // chunk capacity with int32 / int64 nodes
   uint32_t cap32, cap64;  // rank capacities
-  size_t off_rl, off_fine, off_T, off_P, off_desc, off_stage, bytes;
+  size_t off_rl, off_fine, off_T, off_P, off_desc, off_ev, off_q, bytes;
 };
 __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budget) {
   SweepLayout L;
   L.ww = nwords < kWinWords ? nwords : kWinWords;
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
-  const size_t fixed = al((size_t)L.ww * 8) + al(((size_t)L.ww + 2) * 4) + al(sizeof(StepDesc) * kStages) +
-                       (size_t)kStages * kStageBytes + 64;
-  const size_t per32 = (size_t)kChunkStride * 4 + 16;   // int32 nodes + T + P per chunk
-  int32_t n32 = (int32_t)((budget - fixed) / per32);
-  if (n32 > 128) n32 = 128;
+  const size_t fixed = al((size_t)L.ww * 8) + al(((size_t)L.ww + 2) * 4) + al(sizeof(StepDesc) * kDescRing) +
+                       (size_t)kSlots * kSweepThreads * 16 + al((size_t)kSlots * kSweepThreads * 12) +
+                       (size_t)kSweepWarps * (kMaxChunks + 1) * 8 + 128;
+  const size_t per32 = (size_t)kChunkStride * 4 + 8;  // int32 nodes + chunk total
+  int32_t n32 = budget > fixed ? (int32_t)((budget - fixed) / per32) : 0;
+  if (n32 > kMaxChunks) n32 = kMaxChunks;
   L.nch32 = n32;
   L.nch64 = (int32_t)(((size_t)n32 * kChunkStride * 4) / ((size_t)kChunkStride * 8));
   L.cap32 = (uint32_t)L.nch32 * kChunk;
@@ -517,44 +525,19 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   L.off_rl = o;   o = al(o + ((size_t)L.ww + 2) * 4);
   L.off_fine = o; o = al(o + (size_t)n32 * kChunkStride * 4);
   L.off_T = o;    o = al(o + (size_t)n32 * 8);
-  L.off_P = o;    o = al(o + ((size_t)n32 + 1) * 8);
-  L.off_desc = o; o = al(o + sizeof(StepDesc) * kStages);
-  L.off_stage = o; o += (size_t)kStages * kStageBytes;
+  L.off_P = o;    o = al(o + (size_t)kSweepWarps * (kMaxChunks + 1) * 8);
+  L.off_desc = o; o = al(o + sizeof(StepDesc) * kDescRing);
+  L.off_ev = o;   o = al(o + (size_t)kSlots * kSweepThreads * 16);
+  L.off_q = o;    o = al(o + (size_t)kSlots * kSweepThreads * 12);
   L.bytes = o;
   return L;
 }
 
-// Stage one step (events, queries) into a ring slot with cp.async; every thread
-// commits one group per call so group counting stays uniform.
-__device__ __forceinline__ void stage_step(const SweepParams& p, const StepDesc& d, bool valid,
-                                           unsigned char* slot, StepDesc* sdesc) {
-  if (threadIdx.x == 0) {
-    StepDesc e = d;
-    if (!valid) { e.ne = 0; e.nq = -1; e.e0 = 0; e.q0 = 0; }
-    *sdesc = e;
-  }
-  if (valid && threadIdx.x < 64) {
-    // warp 0 copies the events, warp 1 the queries; the other warps skip staging
-    const int lane = threadIdx.x & 31;
-    if (threadIdx.x < 32) {
-      const int ne = min(d.ne, kStageEv);
-      for (int i = lane; i < ne; i += 32) cp_async16(slot + 16 * i, p.ev + d.e0 + i);
-    } else if (d.nq > 0) {
-      const int words = 3 * min(d.nq, kStageQ);
-      const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + d.q0);
-      unsigned char* dq = slot + kStageEv * 16;
-      for (int w = lane; w < words; w += 32) cp_async4(dq + 4 * w, src + w);
-    }
-  }
-  cp_async_commit();
-}
-
 // Point update of one chunk: the Fenwick nodes above local index l (l in
 // 1..kChunk, stopping below the chunk top, at most kChunkLevels nodes) and the
-// chunk total.  int64 nodes
-// use exact 32-bit-pair atomics with all low-word atomics issued before any
-// high-word one (one shared-atomic round trip, not six); int32 nodes take plain
-// 32-bit atomics with no return value.
+// chunk total.  int64 nodes use exact 32-bit-pair atomics with all low-word
+// atomics issued before any high-word one (one shared-atomic round trip);
+// int32 nodes take plain 32-bit atomics with no return value.
 template <typename Node>
 __device__ __forceinline__ void chunk_add(Node* f, unsigned long long* tot, uint32_t l, uint64_t v) {
   const unsigned lo = (unsigned)v, hi = (unsigned)(v >> 32);
@@ -629,9 +612,11 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
   uint32_t* srl = reinterpret_cast<uint32_t*>(smem + L.off_rl);
   Node* fine = reinterpret_cast<Node*>(smem + L.off_fine);
   unsigned long long* T = reinterpret_cast<unsigned long long*>(smem + L.off_T);
-  unsigned long long* P = reinterpret_cast<unsigned long long*>(smem + L.off_P);
-  StepDesc* sdesc = reinterpret_cast<StepDesc*>(smem + L.off_desc);
-  unsigned char* stage = smem + L.off_stage;
+  StepDesc* ring = reinterpret_cast<StepDesc*>(smem + L.off_desc);
+  unsigned char* evs = smem + L.off_ev;   // [slot][thread] 16 B
+  unsigned char* qss = smem + L.off_q;    // [slot][thread] 12 B
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  unsigned long long* Pw = reinterpret_cast<unsigned long long*>(smem + L.off_P) + (size_t)warp * (kMaxChunks + 1);
 
   const int b = blockIdx.x;
   const int32_t t0 = p.bounds[b], t1 = p.bounds[b + 1];
@@ -640,7 +625,29 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
   const uint64_t* gbits = p.bits + (size_t)b * p.nwords;
   const uint32_t* grl = p.rlut + (size_t)b * (p.nwords + 1);
   const int64_t* crow = p.carry + (size_t)b * ((size_t)p.C + 1);
-  const int tid = threadIdx.x;
+  unsigned char* my_ev = evs + 16 * tid;
+  unsigned char* my_q = qss + 12 * tid;
+
+  auto desc_at = [&](int32_t t) -> StepDesc {
+    StepDesc d;
+    if (t < t1) d = p.desc[t];
+    else { d.e0 = 0; d.q0 = 0; d.ne = 0; d.nq = -1; }
+    return d;
+  };
+  // Prefetch this thread's event and query of step t into slot t % kSlots.
+  auto stage_own = [&](int32_t t) {
+    const StepDesc d = ring[(t - t0) % kDescRing];
+    const int sl = (t - t0) % kSlots;
+    if (tid < d.ne) cp_async16(my_ev + (size_t)sl * kSweepThreads * 16, p.ev + d.e0 + tid);
+    if (tid < d.nq) {
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + d.q0 + tid);
+      unsigned char* dq = my_q + (size_t)sl * kSweepThreads * 12;
+      cp_async4(dq, src);
+      cp_async4(dq + 4, src + 1);
+      cp_async4(dq + 8, src + 2);
+    }
+    cp_async_commit();
+  };
 
   for (int32_t si = 0; si < nsl; ++si) {
     const Slice s = p.slices[(size_t)b * kMaxSlices + si];
@@ -654,63 +661,55 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       srl[i] = grl[s.word_lo + i] - s.rank_lo;
     }
     for (uint32_t i = tid; i < nch * kChunkStride; i += kSweepThreads) fine[i] = 0;
-    for (uint32_t i = tid; i <= nch; i += kSweepThreads) { T[i < nch ? i : 0] = 0; P[i] = 0; }
+    for (uint32_t i = tid; i < nch; i += kSweepThreads) T[i] = 0;
+    for (int i = tid; i < kDescRing; i += kSweepThreads) ring[i] = desc_at(t0 + i);
     __syncthreads();
 
-    // prologue: stage the first kAhead steps, prefetch the next descriptor
-    for (int u = 0; u < kAhead; ++u) {
-      const int32_t t = t0 + u;
-      StepDesc d{};
-      if (t < t1) d = p.desc[t];
-      stage_step(p, d, t < t1, stage + (size_t)(t % kStages) * kStageBytes, sdesc + (t % kStages));
-    }
-    StepDesc dn{};
-    if (t0 + kAhead < t1) dn = p.desc[t0 + kAhead];
-    cp_async_wait<kAhead - 2>();
-    __syncthreads();
-    // carries of the first step's queries
+    // prologue: own items of the first kAhead steps; step t0 landed before its carries
+    for (int u = 0; u < kAhead; ++u) stage_own(t0 + u);
+    cp_async_wait<kAhead - 1>();
     uint64_t ca_lo = 0, ca_hi = 0, cb_lo = 0, cb_hi = 0;
     if (first) {
-      const StepDesc d = sdesc[t0 % kStages];
-      const uint32_t* q = reinterpret_cast<const uint32_t*>(stage + (size_t)(t0 % kStages) * kStageBytes + kStageEv * 16);
-      if (tid < min(d.nq, kStageQ) && q[3 * tid + 2] > q[3 * tid + 1]) {
-        ca_lo = (uint64_t)__ldg(crow + q[3 * tid + 1]);
-        ca_hi = (uint64_t)__ldg(crow + q[3 * tid + 2]);
+      const StepDesc d = ring[0];
+      const uint32_t* q = reinterpret_cast<const uint32_t*>(my_q);
+      if (tid < d.nq && q[2] > q[1]) {
+        ca_lo = (uint64_t)__ldg(crow + q[1]);
+        ca_hi = (uint64_t)__ldg(crow + q[2]);
       }
     }
-    bool dirty = true;  // chunk totals changed since the last coarse rebuild
+    bool dirty = true;
 
-    // One step.  The carries of step t arrive in (c_lo, c_hi); the carries of step
-    // t + 1 are loaded into (n_lo, n_hi).  The loop below alternates the two
-    // register pairs statically, so no register copy waits on a pending load.
+    // One step.  The carries of step t arrive in (c_lo, c_hi); those of step t + 1
+    // are loaded into (n_lo, n_hi); the loop alternates the pairs statically.
     auto step = [&](int32_t t, uint64_t& c_lo, uint64_t& c_hi, uint64_t& n_lo, uint64_t& n_hi) {
-      const int slot = t % kStages;
-      // 1. stage step t + kAhead (its slot held step t - 1, finished before the last barrier)
-      {
-        const int32_t ta = t + kAhead;
-        stage_step(p, dn, ta < t1, stage + (size_t)(ta % kStages) * kStageBytes, sdesc + (ta % kStages));
-        if (ta + 1 < t1) dn = p.desc[ta + 1];
+      const int32_t rel = t - t0;
+      if (rel >= kDescRefill && rel % kDescRefill == 0) {
+        // ring entries of steps rel-32..rel-1 are done; refill them with rel+32..rel+63
+        __syncthreads();
+        for (int i = tid; i < kDescRefill; i += kSweepThreads)
+          ring[(rel + kDescRefill + i) % kDescRing] = desc_at(t + kDescRefill + i);
+        __syncthreads();
       }
-      // 2. carries of step t + 1's queries (its data landed before the last barrier)
+      const StepDesc d = ring[rel % kDescRing];
+      stage_own(t + kAhead);
+      cp_async_wait<kAhead - 1>();   // own items of steps t and t + 1 have landed
+      const int sl = rel % kSlots;
       if (first && t + 1 < t1) {
-        const int s1 = (t + 1) % kStages;
-        const StepDesc d1 = sdesc[s1];
-        const uint32_t* q = reinterpret_cast<const uint32_t*>(stage + (size_t)s1 * kStageBytes + kStageEv * 16);
-        if (tid < min(d1.nq, kStageQ) && q[3 * tid + 2] > q[3 * tid + 1]) {
-          n_lo = (uint64_t)__ldg(crow + q[3 * tid + 1]);
-          n_hi = (uint64_t)__ldg(crow + q[3 * tid + 2]);
+        const StepDesc d1 = ring[(rel + 1) % kDescRing];
+        const uint32_t* q = reinterpret_cast<const uint32_t*>(my_q + (size_t)((rel + 1) % kSlots) * kSweepThreads * 12);
+        if (tid < d1.nq && q[2] > q[1]) {
+          n_lo = (uint64_t)__ldg(crow + q[1]);
+          n_hi = (uint64_t)__ldg(crow + q[2]);
         }
       }
-      const StepDesc d = sdesc[slot];
-      const unsigned char* sl = stage + (size_t)slot * kStageBytes;
-      // 3. updates of step t (exit steps remove the node's events)
+      // updates of step t (exit steps remove the node's events)
       if (s.n && d.ne > 0) {
         const bool neg = d.nq < 0;
         for (int i = tid; i < d.ne; i += kSweepThreads) {
           uint32_t k;
           uint64_t v;
-          if (i < kStageEv) {
-            const BwEvent* e = reinterpret_cast<const BwEvent*>(sl) + i;
+          if (i < kSweepThreads) {
+            const BwEvent* e = reinterpret_cast<const BwEvent*>(my_ev + (size_t)sl * kSweepThreads * 16);
             k = e->key;
             v = (uint64_t)e->delta;
           } else {
@@ -727,64 +726,59 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         }
         dirty = true;
       }
-      // 4. queries of step t
-      if (d.nq > 0) {
-        __syncthreads();
-        if (dirty && tid < 32) {
-          // P = exclusive prefix of the chunk totals (one warp, <= kRebuildPer
-          // contiguous chunks per lane, loads issued together)
-          const uint32_t per = ((nch + 31) / 32) | 1u;  // odd: lanes hit different banks
-          const uint32_t lo = tid * per;
-          uint64_t tv[kRebuildPer];
-          uint64_t sum = 0;
+      if (d.nq <= 0) return;  // no probes: the next step's updates may follow at once
+      __syncthreads();         // every update of steps <= t is applied
+      if (dirty) {
+        // this warp's copy of the exclusive prefix of the chunk totals
+        const uint32_t per = ((nch + 31) / 32) | 1u;  // odd: lanes hit different banks
+        const uint32_t lo = lane * per;
+        uint64_t tv[kRebuildPer];
+        uint64_t sum = 0;
 #pragma unroll
-          for (int i = 0; i < kRebuildPer; ++i) {
-            tv[i] = ((uint32_t)i < per && lo + i < nch) ? T[lo + i] : 0;
-            sum += tv[i];
-          }
-          uint64_t x = sum;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (tid >= o) x += y;
-          }
-          uint64_t run = x - sum;
-#pragma unroll
-          for (int i = 0; i < kRebuildPer; ++i) {
-            if ((uint32_t)i < per && lo + i < nch) P[lo + i] = run;
-            run += tv[i];
-          }
-          if (tid == 31) P[nch] = x;
+        for (int i = 0; i < kRebuildPer; ++i) {
+          tv[i] = ((uint32_t)i < per && lo + i < nch) ? T[lo + i] : 0;
+          sum += tv[i];
         }
-        dirty = false;
-        __syncthreads();
-        const uint32_t* q = reinterpret_cast<const uint32_t*>(sl + kStageEv * 16);
-        for (int j = tid; j < d.nq; j += kSweepThreads) {
-          uint32_t lo, hi;
-          uint64_t acc = 0;
-          if (j < kStageQ) {
-            lo = q[3 * j + 1];
-            hi = q[3 * j + 2];
-            if (first) acc = c_hi - c_lo;
-          } else {
-            const BwQuery qq = p.qs[d.q0 + j];
-            lo = qq.lo;
-            hi = qq.hi;
-            if (first && hi > lo) acc = (uint64_t)__ldg(crow + hi) - (uint64_t)__ldg(crow + lo);
-          }
-          int64_t* out = p.answers + d.q0 + j;
-          if (hi <= lo) {
-            if (first) *out = 0;
-            continue;
-          }
-          acc += slice_prefix2(fine, P, s.n, sbits, srl, klo, khi, hi);
-          acc -= slice_prefix2(fine, P, s.n, sbits, srl, klo, khi, lo);
-          *out = first ? (int64_t)acc : (int64_t)((uint64_t)*out + acc);
+        uint64_t x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += y;
         }
+        uint64_t run = x - sum;
+#pragma unroll
+        for (int i = 0; i < kRebuildPer; ++i) {
+          if ((uint32_t)i < per && lo + i < nch) Pw[lo + i] = run;
+          run += tv[i];
+        }
+        if (lane == 31) Pw[nch] = x;
+        __syncwarp();
       }
-      // 5. step t + 2 staged and visible; slot of step t free
-      cp_async_wait<kAhead - 2>();
-      __syncthreads();
+      dirty = false;
+      const uint32_t* q = reinterpret_cast<const uint32_t*>(my_q + (size_t)sl * kSweepThreads * 12);
+      for (int j = tid; j < d.nq; j += kSweepThreads) {
+        uint32_t lo, hi;
+        uint64_t acc = 0;
+        if (j < kSweepThreads) {
+          lo = q[1];
+          hi = q[2];
+          if (first) acc = c_hi - c_lo;
+        } else {
+          const BwQuery qq = p.qs[d.q0 + j];
+          lo = qq.lo;
+          hi = qq.hi;
+          if (first && hi > lo) acc = (uint64_t)__ldg(crow + hi) - (uint64_t)__ldg(crow + lo);
+        }
+        int64_t* out = p.answers + d.q0 + j;
+        if (hi <= lo) {
+          if (first) *out = 0;
+          continue;
+        }
+        acc += slice_prefix2(fine, Pw, s.n, sbits, srl, klo, khi, hi);
+        acc -= slice_prefix2(fine, Pw, s.n, sbits, srl, klo, khi, lo);
+        *out = first ? (int64_t)acc : (int64_t)((uint64_t)*out + acc);
+      }
+      __syncthreads();  // probes done before the next step's updates
     };
     for (int32_t t = t0; t < t1; t += 2) {
       step(t, ca_lo, ca_hi, cb_lo, cb_hi);
