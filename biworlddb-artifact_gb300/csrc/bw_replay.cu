@@ -15,7 +15,8 @@
 //                                (the CSR rank-LUT of sparse_engine.hpp:70-102),
 //                                smem-sized key slices, and the block's net key
 //                                deltas as a dense key-prefix row
-//   5. carry     k_carry         column scan over blocks: carry prefix at every
+//   5. carry     k_carry_groups  column scan over blocks: carry prefix at every
+//                k_carry_apply
 //                                block start (batch_engine_v7.hpp:936-945, on the
 //                                device instead of the host)
 //   6. sweep     k_sweep         one CTA per block replays its steps from a zero
@@ -38,7 +39,7 @@
 namespace bw {
 
 // ------------------------------------------------------------------ constants
-constexpr int kThreads = 512;                 // CTA width of every per-block kernel
+constexpr int kPrepThreads = 512;             // CTA width of the prepare kernel (two per SM)
 constexpr int kWinBits = 18;                  // rank window: 2^18 keys per smem bitmap
 constexpr int kWinWords = 1 << (kWinBits - 6);
 constexpr int kMaxSlices = 64;                // key slices per block
@@ -69,6 +70,7 @@ struct Plan {            // device pointers carved from the workspace
   int32_t* tin;          // S   step index of enter(v)
   int32_t* tout;         // S   step index of exit(v) (INT32_MAX when not swept)
   int32_t* bmode;        // B   1 = the block's applied |delta| sum is < 2^31
+  int64_t* gsum;         // ceil(B/16) x (C+1) carry group sums
   StepDesc* desc;        // 2S
   int64_t* work;         // 2S  inclusive work prefix
   int64_t* scan_tmp;     // scan partials
@@ -263,6 +265,7 @@ struct PrepParams {
   const int32_t* tout;
   const int32_t* bounds;
   int32_t nwords;
+  int32_t ww;              // rank-table window in bitmap words (<= kWinWords)
   uint32_t C;
   uint32_t cap32, cap64;   // slice rank capacity with int32 / int64 sweep nodes
   uint64_t* bits;
@@ -309,15 +312,17 @@ __device__ __forceinline__ void for_block_events(const PrepParams& p, int32_t t0
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
+__global__ void __launch_bounds__(kPrepThreads, 2) k_prepare(PrepParams p) {
   if (*p.status) return;  // bounds/descriptors are not trustworthy after an input error
   extern __shared__ __align__(16) unsigned char smem[];
-  uint64_t* sbits = reinterpret_cast<uint64_t*>(smem);                    // kWinWords
-  uint32_t* srl = reinterpret_cast<uint32_t*>(sbits + kWinWords);         // kWinWords + 1
-  unsigned long long* hist = reinterpret_cast<unsigned long long*>(srl + kWinWords + 2);  // cap + 1
+  uint64_t* sbits = reinterpret_cast<uint64_t*>(smem);                    // ww words
+  uint32_t* srl = reinterpret_cast<uint32_t*>(sbits + p.ww);              // ww + 2
+  // histogram: int32 per rank when the block's nodes are int32 (exact, same
+  // bound), int64 otherwise; both fit the same bytes (cap32 ~ 2 * cap64)
+  unsigned char* hist_raw = reinterpret_cast<unsigned char*>(srl + p.ww + 2 + (p.ww & 1));  // 8-byte aligned
+  __shared__ uint64_t s_wsum[kPrepThreads / 32];
   __shared__ int32_t s_nsl;
   __shared__ int32_t s_mode;
-  __shared__ uint64_t s_base;
 
   const int b = blockIdx.x;
   const int32_t t0 = p.bounds[b], t1 = p.bounds[b + 1];
@@ -329,8 +334,8 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
   uint64_t mass = 0;  // per-thread partial of the block's applied |delta| sum
 
   // ---- pass A: per window, key bitmap -> rank table -> slices
-  for (int32_t w0 = 0; w0 < p.nwords; w0 += kWinWords) {
-    const int32_t ww = min(kWinWords, p.nwords - w0);
+  for (int32_t w0 = 0; w0 < p.nwords; w0 += p.ww) {
+    const int32_t ww = min(p.ww, p.nwords - w0);
     for (int i = threadIdx.x; i < ww; i += blockDim.x) sbits[i] = 0;
     __syncthreads();
     const uint32_t klo = (uint32_t)w0 << 6;
@@ -388,7 +393,11 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
 
   // ---- pass B: per slice, net key deltas of the block -> dense key-prefix row
   int64_t* row = p.carry + (size_t)b * ((size_t)p.C + 1);
-  if (threadIdx.x == 0) s_base = 0;
+  const bool h32 = s_mode != 0;
+  unsigned* hist32 = reinterpret_cast<unsigned*>(hist_raw);
+  unsigned long long* hist64 = reinterpret_cast<unsigned long long*>(hist_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  uint64_t base = 0;  // key prefix at the start of the slice (same in every thread)
   for (int32_t si = 0; si < nsl; ++si) {
     const Slice s = gsl[si];
     const int32_t nwd = s.word_hi - s.word_lo;
@@ -396,46 +405,108 @@ __global__ void __launch_bounds__(kThreads) k_prepare(PrepParams p) {
       sbits[i] = gbits[s.word_lo + i];
       srl[i] = grl[s.word_lo + i] - s.rank_lo;
     }
-    for (uint32_t i = threadIdx.x; i <= s.n; i += blockDim.x) hist[i] = 0;
+    for (uint32_t i = threadIdx.x; i <= s.n; i += blockDim.x) {
+      if (h32) hist32[i] = 0; else hist64[i] = 0;
+    }
     __syncthreads();
     const uint32_t klo = (uint32_t)s.word_lo << 6;
     const uint32_t khi = (uint32_t)imin64((int64_t)s.word_hi << 6, (int64_t)p.C);
     if (s.n) {
       for_block_events(p, t0, t1, 1, [&](uint32_t k, uint64_t d, bool valid, bool) {
-        if (valid && k >= klo && k < khi) shared_add_u64(hist + local_rank(sbits, srl, k - klo), d);
+        if (valid && k >= klo && k < khi) {
+          const uint32_t r = local_rank(sbits, srl, k - klo);
+          if (h32) atomicAdd(hist32 + r, (unsigned)d);
+          else shared_add_u64(hist64 + r, d);
+        }
       });
     }
     __syncthreads();
-    block_exclusive_scan_u64(hist, s.n + 1);   // hist[i] = sum of ranks < i
-    const uint64_t base = s_base;
-    for (uint32_t k = klo + threadIdx.x; k < khi; k += blockDim.x)
-      row[k] = (int64_t)(base + hist[local_rank(sbits, srl, k - klo)]);
+    auto hval = [&](uint32_t r) -> uint64_t {
+      return h32 ? (uint64_t)(int64_t)(int32_t)hist32[r] : (uint64_t)hist64[r];
+    };
+    // each warp writes a contiguous key range; its start value is the sum of the
+    // histogram over the ranks before the range (block scan of warp sums)
+    const uint32_t nk = khi - klo;
+    const uint32_t span = ((nk + nw - 1) / nw + 31) & ~31u;
+    const uint32_t ka = klo + imin64((int64_t)warp * span, nk), kb = klo + imin64((int64_t)(warp + 1) * span, nk);
+    const uint32_t ra = ka < khi ? local_rank(sbits, srl, ka - klo) : s.n;
+    const uint32_t rb = kb < khi ? local_rank(sbits, srl, kb - klo) : s.n;
+    uint64_t part = 0;
+    for (uint32_t r = ra + lane; r < rb; r += 32) part += hval(r);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) s_wsum[warp] = part;
     __syncthreads();
-    if (threadIdx.x == 0) s_base = base + hist[s.n];
+    uint64_t start = base, total = 0;
+    for (int w = 0; w < nw; ++w) {
+      const uint64_t x = s_wsum[w];
+      if (w < warp) start += x;
+      total += x;
+    }
+    for (uint32_t k0 = ka; k0 < kb; k0 += 32) {
+      const uint32_t k = k0 + lane;
+      uint64_t val = 0;
+      if (k < kb) {
+        const uint32_t x = k - klo;
+        if ((sbits[x >> 6] >> (x & 63)) & 1ull) val = hval(local_rank(sbits, srl, x));
+      }
+      uint64_t incl = val;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      if (k < kb) row[k] = (int64_t)(start + incl - val);
+      start += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    base += total;
     __syncthreads();
   }
-  if (threadIdx.x == 0) row[p.C] = (int64_t)s_base;
+  if (threadIdx.x == 0) row[p.C] = (int64_t)base;
 }
 
 // ------------------------------------------------------------------ 5. carry
 // In place: row b becomes the exclusive sum over blocks < b of the per-block
 // key-prefix rows, i.e. the key prefix of the state vector at block b's start.
-__global__ void k_carry(int64_t* carry, int32_t B, int64_t width, const int32_t* status) {
+// Two passes over groups of kCarryGroup rows, so that every (group, column) pair
+// is its own thread and all rows of a group are loaded at once: group sums, then
+// each group adds the sums of the groups before it and writes its rows.
+constexpr int kCarryGroup = 16;
+
+__global__ void k_carry_groups(const int64_t* carry, int32_t B, int64_t width, int64_t* gsum,
+                               const int32_t* status) {
   if (*status) return;
-  constexpr int kRows = 8;  // row loads kept in flight per column
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < width; k += (int64_t)gridDim.x * blockDim.x) {
-    uint64_t run = 0;
-    int64_t* p = carry + k;
-    for (int32_t b0 = 0; b0 < B; b0 += kRows) {
-      uint64_t v[kRows];
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t g = blockIdx.y, r0 = g * kCarryGroup;
+  if (k >= width) return;
+  const int64_t* p = carry + (size_t)r0 * width + k;
+  const int32_t n = min(kCarryGroup, B - r0);
+  uint64_t v[kCarryGroup];
 #pragma unroll
-      for (int i = 0; i < kRows; ++i) v[i] = b0 + i < B ? (uint64_t)p[(size_t)(b0 + i) * width] : 0;
+  for (int i = 0; i < kCarryGroup; ++i) v[i] = i < n ? (uint64_t)p[(size_t)i * width] : 0;
+  uint64_t sum = 0;
 #pragma unroll
-      for (int i = 0; i < kRows; ++i) {
-        if (b0 + i < B) p[(size_t)(b0 + i) * width] = (int64_t)run;
-        run += v[i];
-      }
-    }
+  for (int i = 0; i < kCarryGroup; ++i) sum += v[i];
+  gsum[(size_t)g * width + k] = (int64_t)sum;
+}
+
+__global__ void k_carry_apply(int64_t* carry, int32_t B, int64_t width, const int64_t* gsum,
+                              const int32_t* status) {
+  if (*status) return;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t g = blockIdx.y, r0 = g * kCarryGroup;
+  if (k >= width) return;
+  int64_t* p = carry + (size_t)r0 * width + k;
+  const int32_t n = min(kCarryGroup, B - r0);
+  uint64_t v[kCarryGroup];
+#pragma unroll
+  for (int i = 0; i < kCarryGroup; ++i) v[i] = i < n ? (uint64_t)p[(size_t)i * width] : 0;
+  uint64_t run = 0;
+  for (int32_t j = 0; j < g; ++j) run += (uint64_t)gsum[(size_t)j * width + k];
+#pragma unroll
+  for (int i = 0; i < kCarryGroup; ++i) {
+    if (i < n) p[(size_t)i * width] = (int64_t)run;
+    run += v[i];
   }
 }
 
@@ -844,12 +915,15 @@ static void layout(const BwReplayArgs* a, int32_t B, Layout& L) {
   take(17, S * 4);                 // tin
   take(18, S * 4);                 // tout
   take(19, (size_t)B * 4);         // bmode
+  take(20, (size_t)((B + kCarryGroup - 1) / kCarryGroup) * ((size_t)a->n_keys + 1) * 8);  // carry group sums
   L.total = o;
 }
 
-// Prepare smem: window bitmap + rank table + histogram of cap+1 int64.
-static size_t prepare_smem(uint32_t cap) {
-  return (size_t)kWinWords * 8 + ((size_t)kWinWords + 2) * 4 + ((size_t)cap + 1) * 8;
+// Prepare smem: window bitmap + rank table + histogram (int32 x cap32+1 or
+// int64 x cap64+1, whichever is larger).
+static size_t prepare_smem(int32_t ww, uint32_t cap32, uint32_t cap64) {
+  const size_t h32 = ((size_t)cap32 + 1) * 4, h64 = ((size_t)cap64 + 1) * 8;
+  return (size_t)ww * 8 + ((size_t)ww + 4) * 4 + (h32 > h64 ? h32 : h64) + 16;
 }
 
 struct LastInfo { int32_t kernels = 0, blocks = 0; };
@@ -928,6 +1002,7 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
   P.tin = reinterpret_cast<int32_t*>(ws + L.off[17]);
   P.tout = reinterpret_cast<int32_t*>(ws + L.off[18]);
   P.bmode = reinterpret_cast<int32_t*>(ws + L.off[19]);
+  P.gsum = reinterpret_cast<int64_t*>(ws + L.off[20]);
 
   const int32_t S = a->n_states;
   const int64_t S2 = 2 * (int64_t)S;
@@ -1016,10 +1091,8 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
   const int ctas_per_sm = B >= 2 * sms ? 2 : 1;
   const size_t sweep_budget = (size_t)(kSmemPerSM / ctas_per_sm) - 3072;
   const SweepLayout SL = sweep_layout(nwords, sweep_budget);
-  uint32_t cap32 = SL.cap32, cap64 = SL.cap64;
-  while (cap32 > 64 && prepare_smem(cap32) > (size_t)kSmemLimit - 2048) cap32 -= 64;
-  if (cap64 > cap32) cap64 = cap32;
-  const size_t smem = prepare_smem(cap32);
+  const uint32_t cap32 = SL.cap32, cap64 = SL.cap64;
+  const size_t smem = prepare_smem(SL.ww, cap32, cap64);
   static bool attr_done = false;
   if (!attr_done) {
     if ((rc = report(cudaFuncSetAttribute(k_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit - 1024), "smem attr"))) return rc;
@@ -1027,16 +1100,24 @@ extern "C" int bw_replay_launch(const BwReplayArgs* a) {
     attr_done = true;
   }
   PrepParams pp;
-  pp.ev = a->events; pp.desc = P.desc; pp.steps = P.steps; pp.tin = P.tin; pp.tout = P.tout; pp.bounds = P.bounds; pp.nwords = nwords; pp.C = C; pp.cap32 = cap32; pp.cap64 = cap64;
+  pp.ev = a->events; pp.desc = P.desc; pp.steps = P.steps; pp.tin = P.tin; pp.tout = P.tout; pp.bounds = P.bounds; pp.nwords = nwords; pp.ww = SL.ww; pp.C = C; pp.cap32 = cap32; pp.cap64 = cap64;
   pp.bits = P.bits; pp.rlut = P.rlut; pp.slices = P.slices; pp.nslices = P.nslices; pp.carry = P.carry;
   pp.status = P.misc; pp.bmode = P.bmode;
-  k_prepare<<<B, kThreads, smem, st>>>(pp);
+  k_prepare<<<B, kPrepThreads, smem, st>>>(pp);
   if ((rc = chk("k_prepare"))) return rc;
 
   if ((rc = mark(4))) return rc;
   // ---- 5. carry
-  k_carry<<<grid, 256, 0, st>>>(P.carry, B, (int64_t)C + 1, P.misc);
-  if ((rc = chk("k_carry"))) return rc;
+  {
+    const int64_t width = (int64_t)C + 1;
+    const dim3 cg((unsigned)((width + 255) / 256), (unsigned)((B + kCarryGroup - 1) / kCarryGroup));
+    if (cg.y > 1) {
+      k_carry_groups<<<cg, 256, 0, st>>>(P.carry, B, width, P.gsum, P.misc);
+      if ((rc = chk("k_carry_groups"))) return rc;
+    }
+    k_carry_apply<<<cg, 256, 0, st>>>(P.carry, B, width, P.gsum, P.misc);
+    if ((rc = chk("k_carry_apply"))) return rc;
+  }
 
   if ((rc = mark(5))) return rc;
   // ---- 6. sweep
