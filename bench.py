@@ -139,7 +139,7 @@ def profiled_traffic(workload: str):
 
 
 def cpu_baseline(w, seconds: float):
-    """Oracle preorder replay over the first states of the workload, timed alone."""
+    """Oracle preorder replay over the first Euler steps of the workload, timed alone."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
     S = len(w.parent)
@@ -149,7 +149,8 @@ def cpu_baseline(w, seconds: float):
     limit = int(min(2 * S, max(probe, rate_steps * seconds)))
     _, done, secs = oracle.ev_sweep_prefix(w.parent, w.n_keys, w.events, w.queries, limit)
     return {"value": done / max(secs, 1e-9), "unit": "answers/s", "cores": 1, "kind": "port",
-            "sample": f"preorder replay of the first {limit} of {S} states ({done} answers, {secs:.1f} s)"}
+            "sample": f"preorder replay of the first {limit} of {2 * S} Euler steps ({S} states; "
+                      f"{done} answers, {secs:.1f} s)"}
 
 
 def reference_arm(args):
