@@ -45,10 +45,17 @@ class BwReplayArgs(C.Structure):
                 ("flags", C.c_int32)]
 
 
+class BwCsr(C.Structure):
+    _fields_ = [("key_bits", C.c_int32), ("shift", C.c_int32), ("n_buckets", C.c_int64),
+                ("count", C.c_void_p), ("status", C.c_void_p), ("keys", C.c_void_p), ("pre", C.c_void_p), ("lut", C.c_void_p),
+                ("low", C.c_void_p)]
+
+
 GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch",
                "bw_replay_workspace_size", "bw_replay_launch", "bw_replay_status",
                "bw_replay_last_info", "bw_replay_timing_reset", "bw_replay_stage_times",
-               "bw_device_info"]
+               "bw_device_info", "bw_replay_launch_noalloc",
+               "bw_csr_workspace_size", "bw_csr_build", "bw_csr_point", "bw_csr_range", "bw_csr_status"]
 
 _gpu = None
 
@@ -78,6 +85,12 @@ def gpu_lib(build_if_missing: bool = True):
                                          C.c_void_p]
         L.gpu_v7_launch.argtypes = [C.c_void_p]
         L.gpu_combine_launch.argtypes = [C.c_void_p]
+        L.bw_csr_workspace_size.argtypes = [C.c_int64, C.c_int32, C.c_size_t, C.POINTER(C.c_size_t)]
+        L.bw_csr_build.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_size_t, C.c_void_p,
+                                   C.c_size_t, C.c_void_p, C.POINTER(BwCsr)]
+        L.bw_csr_point.argtypes = [C.POINTER(BwCsr), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        L.bw_csr_range.argtypes = [C.POINTER(BwCsr), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        L.bw_csr_status.argtypes = [C.POINTER(BwCsr), C.POINTER(C.c_int32)]
         _gpu = L
     return _gpu
 
@@ -401,3 +414,84 @@ def replay_noalloc(parent, n_keys: int, events, queries, *, blocks: int = 0, cha
     if st.value:
         raise ValueError(f"replay input rejected on the device: {STATUS_NAMES.get(st.value, st.value)}")
     return answers
+
+
+class CsrIndex:
+    """Sparse-key CSR rank-LUT on the device (CsrBase of sparse_engine.hpp:70-102 over
+    a u64 key universe [0, 2^key_bits)).  Built from (key, amount) pairs by
+    bw_csr_build; the index lives in a workspace held by this object.
+
+    point(keys) -> rank where present, -rank-1 where absent (rank = keys below);
+    range(bounds (n, 2)) -> (n, 2) int64 (rank(hi) - rank(lo), amount sum over [lo, hi))."""
+
+    def __init__(self, keys, amounts, *, key_bits: int = 40, lut_budget_bytes: int = 64 << 20):
+        torch = _torch()
+        L = gpu_lib()
+        n = int(keys.numel())
+        assert keys.is_cuda and amounts.is_cuda and amounts.numel() == n
+        self.device = keys.device
+        nbytes = C.c_size_t(0)
+        _check(L.bw_csr_workspace_size(n, int(key_bits), int(lut_budget_bytes), C.byref(nbytes)),
+               "bw_csr_workspace_size")
+        self.workspace = torch.empty(max(256, nbytes.value), dtype=torch.uint8, device=self.device)
+        self.idx = BwCsr()
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        _check(L.bw_csr_build(keys.contiguous().data_ptr() if n else None,
+                              amounts.contiguous().data_ptr() if n else None, n, int(key_bits),
+                              int(lut_budget_bytes), self.workspace.data_ptr(), self.workspace.numel(), st,
+                              C.byref(self.idx)), "bw_csr_build")
+        self.key_bits, self.shift, self.n_buckets = key_bits, self.idx.shift, self.idx.n_buckets
+        self.lut_bytes = self.n_buckets * 4
+        self._src = (keys, amounts, n, int(lut_budget_bytes))
+
+    def rebuild(self):
+        """Enqueue the build again into the same workspace (timing, refresh)."""
+        torch = _torch()
+        keys, amounts, n, budget = self._src
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        _check(gpu_lib().bw_csr_build(keys.data_ptr() if n else None, amounts.data_ptr() if n else None, n,
+                                      int(self.key_bits), budget, self.workspace.data_ptr(),
+                                      self.workspace.numel(), st, C.byref(self.idx)), "bw_csr_build")
+
+    def status(self) -> int:
+        """0, or 1 when a build key lay outside [0, 2^key_bits) (synchronises)."""
+        st = C.c_int32(0)
+        _check(gpu_lib().bw_csr_status(C.byref(self.idx), C.byref(st)), "bw_csr_status")
+        return int(st.value)
+
+    def count(self) -> int:
+        torch = _torch()
+        c = torch.empty(1, dtype=torch.int64, device=self.device)
+        c.copy_(self._view(self.idx.count, 1, torch.int64))
+        return int(c.item())
+
+    def _view(self, ptr: int, n: int, dtype):
+        torch = _torch()
+        base = self.workspace.data_ptr()
+        esz = torch.tensor([], dtype=dtype).element_size()
+        off = (ptr - base)
+        return self.workspace[off:off + n * esz].view(dtype)
+
+    def arrays(self):
+        """(keys u64 as int64, pre int64) device views of the built index."""
+        torch = _torch()
+        m = self.count()
+        return self._view(self.idx.keys, m, torch.int64), self._view(self.idx.pre, m, torch.int64)
+
+    def point(self, keys, out=None):
+        torch = _torch()
+        n = int(keys.numel())
+        out = torch.empty(n, dtype=torch.int64, device=self.device) if out is None else out
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        _check(gpu_lib().bw_csr_point(C.byref(self.idx), keys.data_ptr() if n else None, n,
+                                      out.data_ptr() if n else None, st), "bw_csr_point")
+        return out
+
+    def range(self, bounds, out=None):
+        torch = _torch()
+        n = int(bounds.numel()) // 2
+        out = torch.empty((n, 2), dtype=torch.int64, device=self.device) if out is None else out
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        _check(gpu_lib().bw_csr_range(C.byref(self.idx), bounds.data_ptr() if n else None, n,
+                                      out.data_ptr() if n else None, st), "bw_csr_range")
+        return out

@@ -14,6 +14,9 @@ configured workloads:
   earlier state, 40,000,000 events with Zipf s=1.2 keys over 65,536 cells and
   delta = round(lognormal(7.3, 0.9)), 50,000,000 queries at uniform states with
   uniform intervals.
+* ``csr_lut`` (sparse-key rank index): 10,000,000 distinct u64 keys over
+  [0, 2^40), 20,000,000 (key, delta) events on them, 100,000,000 point and
+  100,000,000 range lookups, half present keys and half absent.
 
 Events and queries are produced grouped by state (a commit log appends each
 version's events when the version is created; answers come back state-major, as
@@ -116,5 +119,66 @@ def trip_tree(seed: int = 0, scale: float = 1.0) -> Workload:
 CONFIGS = {"plain_chain": plain_chain, "trip_tree": trip_tree}
 
 
-def make(name: str, seed: int = 0, scale: float = 1.0) -> Workload:
+def make(name: str, seed: int = 0, scale: float = 1.0):
+    if name == "csr_lut":
+        return csr_lut(seed=seed, scale=scale)
     return CONFIGS[name](seed=seed, scale=scale)
+
+
+@dataclass
+class CsrWorkload:
+    """Sparse-key rank-index workload: `keys`/`amounts` are the event (key, delta)
+    pairs the index is built from; `point` lookups and `ranges` [lo, hi) pairs are
+    each half present keys and half absent ones."""
+    name: str
+    key_bits: int
+    n_distinct: int
+    keys: np.ndarray        # u64[E]
+    amounts: np.ndarray     # int64[E]
+    point: np.ndarray       # u64[L]
+    ranges: np.ndarray      # u64[L, 2], lo <= hi
+
+    def describe(self) -> dict:
+        return {"workload": self.name, "distinct_keys": self.n_distinct, "events": int(len(self.keys)),
+                "point_lookups": int(len(self.point)), "range_lookups": int(len(self.ranges)),
+                "key_universe_bits": self.key_bits}
+
+
+def csr_lut(seed: int = 0, scale: float = 1.0, lookups: int | None = None) -> CsrWorkload:
+    """10,000,000 distinct u64 keys uniform over [0, 2^40), 20,000,000 events on them
+    (every key at least once, the rest uniform; delta = round(lognormal(7.3, 0.9))
+    with a negative sign at p=0.1), 100,000,000 point lookups and 100,000,000 range
+    lookups, half present keys and half absent ones.  (The events' states do not
+    enter the index, so none are drawn.)"""
+    rng = np.random.default_rng(seed)
+    K, E, L, bits = max(1, int(10_000_000 * scale)), max(1, int(20_000_000 * scale)), \
+        max(2, int(100_000_000 * scale) if lookups is None else int(lookups)), 40
+    universe = 1 << bits
+    distinct = np.unique(rng.integers(0, universe, size=int(K * 1.001) + 16, dtype=np.uint64))
+    distinct = rng.permutation(distinct)[:K]
+    pick = np.concatenate([rng.permutation(K), rng.integers(0, K, size=max(0, E - K))])[:E]
+    keys = distinct[pick]
+    amounts = np.rint(rng.lognormal(7.3, 0.9, size=E)).astype(np.int64)
+    amounts[rng.random(E) < 0.1] *= -1
+
+    present_sorted = np.sort(distinct)
+
+    def absent(n):
+        x = rng.integers(0, universe, size=n, dtype=np.uint64)
+        hit = present_sorted[np.minimum(np.searchsorted(present_sorted, x), K - 1)] == x
+        while hit.any():
+            x[hit] = rng.integers(0, universe, size=int(hit.sum()), dtype=np.uint64)
+            hit = present_sorted[np.minimum(np.searchsorted(present_sorted, x), K - 1)] == x
+        return x
+
+    def mixed(n):
+        out = np.empty(n, np.uint64)
+        pres = rng.random(n) < 0.5
+        out[pres] = distinct[rng.integers(0, K, size=int(pres.sum()))]
+        out[~pres] = absent(int((~pres).sum()))
+        return out
+
+    point = mixed(L)
+    a, b = mixed(L), mixed(L)
+    ranges = np.stack([np.minimum(a, b), np.maximum(a, b)], axis=1)
+    return CsrWorkload("csr_lut", bits, int(K), keys, amounts, point, ranges)

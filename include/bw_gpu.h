@@ -177,6 +177,50 @@ int bw_replay_stage_times(float* ms, int32_t* launches);
  * the BW_STATUS_* code; NULL returns once the work is enqueued. */
 int bw_replay_launch_noalloc(const BwReplayArgs* a, int32_t* status);
 
+/* ============================================================ sparse-key rank index */
+/* The CSR rank-LUT of the reference's sparse engine (CsrBase, sparse_engine.hpp:70-102;
+ * build_csr_base, sparse_engine.hpp:287-360) over a sparse key universe
+ * [0, 2^key_bits): a sorted array of the distinct keys, the cumulative amount prefix
+ * over them (pre[i] = sum of the amounts of keys <= keys[i]) and a rank LUT with one
+ * u32 entry per bucket of 2^shift keys (lut[b] = number of keys below b << shift).
+ * rank(k) = lut[k >> shift] + #(keys in that bucket below k), the reference's
+ * rlut[word] + popcount(bits & mask) with buckets in place of 64-key words, so the
+ * table fits a byte budget for any universe.  Keys >= 2^key_bits rank as the count. */
+typedef struct {
+  int32_t key_bits;          /* universe [0, 2^key_bits), 1..63 */
+  int32_t shift;             /* bucket width 2^shift */
+  int64_t n_buckets;         /* 2^(key_bits - shift) */
+  const int64_t* count;      /* device, 1: number of distinct keys m */
+  const int32_t* status;     /* device, 1: 0, or 1 when a build key was >= 2^key_bits */
+  const uint64_t* keys;      /* device, m ascending distinct keys */
+  const int64_t* pre;        /* device, m cumulative amounts (wrapping int64) */
+  const uint32_t* lut;       /* device, n_buckets */
+  const uint16_t* low;       /* device, m low `shift` bits of the keys (shift <= 16), else NULL */
+} BwCsr;
+
+/* Workspace for bw_csr_build over n_items (key, amount) pairs with a LUT budget of
+ * lut_budget_bytes (the LUT takes the largest power-of-two bucket count that fits). */
+int bw_csr_workspace_size(int64_t n_items, int32_t key_bits, size_t lut_budget_bytes, size_t* bytes);
+/* Device radix sort of the pairs by key, run-length merge of equal keys (amounts
+ * summed), cumulative amount prefix, and the bucket LUT; all on `stream`,
+ * asynchronous.  The index arrays live in the workspace, which must outlive every
+ * lookup; *out receives their device addresses.  Keys must be < 2^key_bits: a
+ * larger key sets the device status word (bw_csr_status) and leaves the lookups
+ * unspecified but in bounds.  BW_EINVAL for n_items >= 2^31. */
+int bw_csr_build(const uint64_t* keys, const int64_t* amounts, int64_t n_items, int32_t key_bits,
+                 size_t lut_budget_bytes, void* workspace, size_t workspace_bytes, void* stream,
+                 BwCsr* out);
+/* Point lookups: out[i] = rank(keys[i]) when keys[i] is present, -rank-1 when
+ * absent (rank = number of index keys below keys[i]).  Device arrays of n. */
+int bw_csr_point(const BwCsr* idx, const uint64_t* keys, int64_t n, int64_t* out, void* stream);
+/* Range lookups, CsrBase::range semantics (sparse_engine.hpp:89-97):
+ * bounds[2i], bounds[2i+1] = lo, hi; out[2i] = rank(hi) - rank(lo) and
+ * out[2i+1] = pre-sum over the keys in [lo, hi) (both negative when hi < lo,
+ * as in the reference). */
+int bw_csr_range(const BwCsr* idx, const uint64_t* bounds, int64_t n, int64_t* out, void* stream);
+/* Synchronise the device and read the build's status word (0 = valid input). */
+int bw_csr_status(const BwCsr* idx, int32_t* status);
+
 /* Library/device information: SM count of the current device and the library's
  * compile-time architecture tag (e.g. 1030 for sm_103a). */
 int bw_device_info(int32_t* sm_count, int32_t* arch_tag);

@@ -617,3 +617,66 @@ int bwo_ev_blocks(int32_t S, const int32_t* parent, uint32_t C, int64_t E, const
   free(vstart);
   return 0;
 }
+
+/* ---------------------------------------------------------- sparse-key rank index */
+typedef struct { uint64_t key; int64_t amount; } bwo_pair;
+
+static int bwo_pair_cmp(const void* a, const void* b) {
+  const uint64_t x = ((const bwo_pair*)a)->key, y = ((const bwo_pair*)b)->key;
+  return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* build_csr_base (sparse_engine.hpp:287-360): there, pass 1 marks each (group,
+ * class) support in a bitmap, the popcount table gives every support its rank, pass
+ * 2 adds each row's amount at its rank and a final scan makes the cumulative prefix.
+ * Over u64 keys the same result is the sorted distinct keys with summed amounts and
+ * their running total. */
+int bwo_csr_build(const uint64_t* keys, const int64_t* amounts, int64_t n, uint64_t* out_keys,
+                  int64_t* out_pre, int64_t* m) {
+  *m = 0;
+  if (n <= 0) return 0;
+  bwo_pair* p = (bwo_pair*)malloc((size_t)n * sizeof(bwo_pair));
+  if (!p) return 1;
+  for (int64_t i = 0; i < n; ++i) { p[i].key = keys[i]; p[i].amount = amounts[i]; }
+  qsort(p, (size_t)n, sizeof(bwo_pair), bwo_pair_cmp);
+  uint64_t run = 0;
+  int64_t u = -1;
+  for (int64_t i = 0; i < n; ++i) {
+    run += (uint64_t)p[i].amount;
+    if (u < 0 || out_keys[u] != p[i].key) out_keys[++u] = p[i].key;
+    out_pre[u] = (int64_t)run;
+  }
+  *m = u + 1;
+  free(p);
+  return 0;
+}
+
+/* number of ukeys[0..m) below k (CsrBase::rank, sparse_engine.hpp:79-88) */
+static int64_t bwo_csr_rank(const uint64_t* ukeys, int64_t m, uint64_t k) {
+  int64_t lo = 0, hi = m;
+  while (lo < hi) {
+    const int64_t mid = lo + (hi - lo) / 2;
+    if (ukeys[mid] < k) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+void bwo_csr_point(const uint64_t* ukeys, int64_t m, const uint64_t* q, int64_t n, int64_t* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t r = bwo_csr_rank(ukeys, m, q[i]);
+    out[i] = (r < m && ukeys[r] == q[i]) ? r : -r - 1;
+  }
+}
+
+/* CsrBase::range (sparse_engine.hpp:89-97) */
+void bwo_csr_range(const uint64_t* ukeys, const int64_t* pre, int64_t m, const uint64_t* bounds,
+                   int64_t n, int64_t* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t a = bwo_csr_rank(ukeys, m, bounds[2 * i]);
+    const int64_t b = bwo_csr_rank(ukeys, m, bounds[2 * i + 1]);
+    uint64_t s = 0;
+    if (a != b) s = (uint64_t)(b ? pre[b - 1] : 0) - (uint64_t)(a ? pre[a - 1] : 0);
+    out[2 * i] = b - a;
+    out[2 * i + 1] = (int64_t)s;
+  }
+}

@@ -121,6 +121,21 @@ int bwo_ev_blocks(int32_t n_states, const int32_t* parent, uint32_t n_keys, int6
                   int64_t* answers, int32_t blocks, int32_t threads);
 int bwo_max_threads(void);
 
+/* -------------------------------------------------------- sparse-key rank index */
+/* CSR build (build_csr_base, sparse_engine.hpp:287-360, over u64 keys): the
+ * distinct keys ascending (out_keys) and the cumulative amount prefix over them
+ * (out_pre[i] = wrapping sum of the amounts of every key <= out_keys[i]); *m
+ * receives the distinct count.  out_* hold n entries. */
+int bwo_csr_build(const uint64_t* keys, const int64_t* amounts, int64_t n, uint64_t* out_keys,
+                  int64_t* out_pre, int64_t* m);
+/* rank(k) = number of index keys below k (CsrBase::rank, sparse_engine.hpp:79-88);
+ * point: out[i] = rank when keys[i] is present, -rank-1 when absent. */
+void bwo_csr_point(const uint64_t* ukeys, int64_t m, const uint64_t* q, int64_t n, int64_t* out);
+/* CsrBase::range (sparse_engine.hpp:89-97): out[2i] = rank(hi)-rank(lo), out[2i+1] =
+ * pre[rank(hi)-1] - pre[rank(lo)-1] (0 when the ranks are equal). */
+void bwo_csr_range(const uint64_t* ukeys, const int64_t* pre, int64_t m, const uint64_t* bounds,
+                   int64_t n, int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

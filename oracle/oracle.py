@@ -75,6 +75,10 @@ def lib():
                                                     C.POINTER(C.c_double)]
         L.bwo_ev_blocks.argtypes = ev_args + [C.c_int32, C.c_int32]
         L.bwo_max_threads.restype = C.c_int
+        L.bwo_csr_build.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                    C.POINTER(C.c_int64)]
+        L.bwo_csr_point.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
+        L.bwo_csr_range.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
         _lib = L
     return _lib
 
@@ -176,6 +180,38 @@ def ev_blocks(parent, n_keys: int, events, queries, blocks: int = 0, threads: in
     if rc:
         raise ValueError(f"block executor needs a chain and valid input (rc={rc})")
     return ans
+
+
+def csr_build(keys, amounts):
+    """Sorted distinct keys and their cumulative amount prefix (build_csr_base)."""
+    k = np.ascontiguousarray(keys, dtype=np.uint64)
+    a = np.ascontiguousarray(amounts, dtype=np.int64)
+    assert k.shape == a.shape
+    uk = np.empty(max(1, k.size), np.uint64)
+    pre = np.empty(max(1, k.size), np.int64)
+    m = C.c_int64(0)
+    rc = lib().bwo_csr_build(_ptr(k), _ptr(a), k.size, _ptr(uk), _ptr(pre), C.byref(m))
+    if rc:
+        raise MemoryError("bwo_csr_build")
+    return uk[:m.value].copy(), pre[:m.value].copy()
+
+
+def csr_point(ukeys, q):
+    uk = np.ascontiguousarray(ukeys, dtype=np.uint64)
+    qq = np.ascontiguousarray(q, dtype=np.uint64)
+    out = np.empty(qq.size, np.int64)
+    lib().bwo_csr_point(_ptr(uk), uk.size, _ptr(qq), qq.size, _ptr(out))
+    return out
+
+
+def csr_range(ukeys, pre, bounds):
+    """bounds: (n, 2) u64 [lo, hi) pairs -> (n, 2) int64 (count, amount sum)."""
+    uk = np.ascontiguousarray(ukeys, dtype=np.uint64)
+    pr = np.ascontiguousarray(pre, dtype=np.int64)
+    b = np.ascontiguousarray(bounds, dtype=np.uint64).reshape(-1, 2)
+    out = np.empty((b.shape[0], 2), np.int64)
+    lib().bwo_csr_range(_ptr(uk), _ptr(pr), uk.size, _ptr(b), b.shape[0], _ptr(out))
+    return out
 
 
 def max_threads() -> int:

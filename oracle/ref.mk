@@ -10,7 +10,7 @@ OUT ?= oracle/_ref
 CXX ?= g++
 CC ?= gcc
 
-all: $(OUT)/oracle_$(STATES) $(OUT)/compiled_$(STATES)
+all: $(OUT)/oracle_$(STATES) $(OUT)/compiled_$(STATES) $(OUT)/csr_ref
 
 $(OUT)/sha_shim.o: oracle/ref_shim/sha256_shim.c oracle/bw_oracle.c
 	mkdir -p $(OUT)
@@ -24,5 +24,10 @@ $(OUT)/oracle_$(STATES):
 $(OUT)/compiled_$(STATES): $(OUT)/sha_shim.o
 	$(CXX) -std=c++17 -O3 -fopenmp -DBWH_STATES=$(STATES) -DBWH_MAXQ=$(MAXQ) -Ioracle/ref_shim -I$(REF)/src \
 	  $(REF)/src/panel_batch_v7fix.cpp $(OUT)/sha_shim.o $(OUT)/bwo.o -o $@
+
+# The reference's CsrBase rank/range (sparse_engine.hpp:70-102) behind a small harness.
+$(OUT)/csr_ref: oracle/ref_csr.cpp
+	mkdir -p $(OUT)
+	$(CXX) -std=c++17 -O2 -fopenmp -Ioracle/ref_shim -I$(REF)/src oracle/ref_csr.cpp -o $@
 
 .PHONY: all
