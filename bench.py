@@ -1,7 +1,14 @@
 #!/usr/bin/env python3
-"""Benchmark: bit-exact range-sum answers/s of the plain version-tree replay on GB300.
+"""Benchmark: bit-exact range-sum answers/s on GB300, batched vs plain.
 
-Workload (default): the trip-log-shaped single tree -- 300,000 states (extend
+Default workload (``--workload batched_trees``): 4,096 independent version trees
+of uneven size (lognormal state counts, median 2,000, about 30M states, 240M
+events, 4.1M queries; see biworlddb-artifact_gb300/workloads.py).  One step = one
+replay of the whole batch as a single autotuned pipeline replayed from a CUDA
+graph.  The same line reports the plain form -- 4,096 sequential bw_replay_launch
+calls, one per tree -- and its answers/s, with answers compared bit for bit.
+
+Single-tree workload (``--workload trip_tree``): the trip-log-shaped single tree -- 300,000 states (extend
 with p=0.9, fork from a uniform earlier state otherwise), 40,000,000 int64 delta
 events with Zipf s=1.2 keys over 65,536 cells, 50,000,000 range-sum queries at
 uniform states with uniform intervals; seeded synthetic data (see
@@ -45,6 +52,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "bit-exact range-sum answers/s (plain version-tree replay)"
+BATCHED_METRIC = "bit-exact range-sum answers/s (batched uneven trees: one autotuned CUDA-graph launch)"
 
 
 def parse():
@@ -53,13 +61,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="trip_tree")
+    ap.add_argument("--workload", default="batched_trees")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--blocks", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample duration")
+    ap.add_argument("--plain-steps", type=int, default=2, help="steps of the sequential plain form")
+    ap.add_argument("--full-check", action="store_true", help="check every answer against the oracle")
     return ap.parse_args()
 
 
@@ -153,11 +163,56 @@ def cpu_baseline(w, seconds: float):
                       f"{done} answers, {secs:.1f} s)"}
 
 
+def forest_cpu_sample(w, seconds: float, threads: int = 1, seed: int = 5):
+    """Oracle preorder replay (the reference's tree path, batch_engine_v7.hpp:1021-1059,
+    ported) of whole trees in a seeded random order until `seconds` of work; trees run
+    on `threads` host threads (the oracle call releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    order = np.random.default_rng(seed).permutation(w.n_trees)
+
+    def one(t):
+        tr = w.tree(int(t))
+        oracle.ev_sweep(tr.parent, tr.n_keys, tr.events, tr.queries)
+        return len(tr.queries), len(tr.parent)
+
+    answers = states = trees = 0
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        i = 0
+        while i < len(order) and time.perf_counter() - t0 < seconds:
+            batch = order[i:i + 4 * threads]
+            for a, st in pool.map(one, batch):
+                answers += a
+                states += st
+            trees += len(batch)
+            i += len(batch)
+    secs = time.perf_counter() - t0
+    return {"value": answers / max(secs, 1e-9), "unit": "answers/s", "cores": threads, "kind": "port",
+            "sample": f"preorder replay of {trees} of {w.n_trees} trees in a seeded random order "
+                      f"({states} states, {answers} answers, {secs:.1f} s)"}
+
+
 def reference_arm(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     w = load_pkg().workloads.make(args.workload, args.seed, args.scale)
+    if args.workload == "batched_trees":
+        threads = os.cpu_count() or 1
+        vals = [forest_cpu_sample(w, max(1.0, args.cpu_seconds / max(1, args.steps)), threads, seed=5 + i)
+                for i in range(args.warmup + args.steps)][args.warmup:]
+        v = statistics.median([x["value"] for x in vals])
+        line = {"impl": "reference", "metric": BATCHED_METRIC, "value": v, "unit": "answers/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+                "data": "synthetic", "config": dict(w.describe(), l2="inputs larger than L2"),
+                "cpu_baseline": {"value": v, "unit": "answers/s", "cores": threads, "kind": "port",
+                                 "sample": vals[-1]["sample"]},
+                "e2e": {"value": v, "unit": "answers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
     vals = []
     for _ in range(args.warmup):
         cpu_baseline(w, min(3.0, args.cpu_seconds / 4))
@@ -250,6 +305,197 @@ def bench_csr(args):
     return 0
 
 
+def bench_batched(args):
+    """Batched uneven trees: autotuned forest plan replayed from a CUDA graph, against
+    4,096 sequential plain launches (one bw_replay_launch per tree)."""
+    import ctypes as C
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    bw = load_pkg()
+    bw.build()
+    t_gen = time.perf_counter()
+    w = bw.workloads.make("batched_trees", args.seed, args.scale)
+    gen_s = time.perf_counter() - t_gen
+    T, S, E, Q = w.n_trees, len(w.parent), len(w.events), len(w.queries)
+    shape = (w.state_off, w.event_off, w.query_off, w.n_keys)
+    h_parent = torch.from_numpy(w.parent).pin_memory()
+    h_events = torch.from_numpy(w.events.view(np.int64).reshape(-1, 2)).pin_memory()
+    h_queries = torch.from_numpy(w.queries.view(np.int32).reshape(-1, 3)).pin_memory()
+    h_answers = torch.empty(Q, dtype=torch.int64).pin_memory()
+    d_parent, d_events, d_queries = h_parent.to(dev), h_events.to(dev), h_queries.to(dev)
+    d_answers = torch.empty(Q, dtype=torch.int64, device=dev)
+    stream = torch.cuda.Stream(dev)
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    def ev_timer():
+        return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    with torch.cuda.stream(stream):
+        t_tune = time.perf_counter()
+        tuning, tune_ms = bw.forest_autotune(*shape, d_parent, d_events, d_queries, d_answers, reps=2, stream=stream)
+        tune_s = time.perf_counter() - t_tune
+        f = bw.Forest(*shape, tuning=tuning, device=dev, stream=stream)
+        f.launch_timed(d_parent, d_events, d_queries, d_answers, stream)
+        st = f.status(stream)
+        if st:
+            raise SystemExit(f"device rejected the workload: {bw.STATUS_NAMES.get(st, st)}")
+        ans0 = d_answers.cpu().numpy()
+        # parity: every tree when asked, else the largest tree and a seeded sample
+        if args.full_check:
+            check = np.arange(T)
+        else:
+            rng = np.random.default_rng(123)
+            check = np.unique(np.concatenate([[int(np.argmax(np.diff(w.state_off)))],
+                                              rng.choice(T, size=min(T, 64), replace=False)]))
+        for t in check:
+            tr = w.tree(int(t))
+            q0, q1 = int(w.query_off[t]), int(w.query_off[t + 1])
+            if not np.array_equal(ans0[q0:q1], oracle.ev_sweep(tr.parent, tr.n_keys, tr.events, tr.queries)):
+                raise SystemExit(f"batched answers of tree {t} differ from the oracle")
+        digest = oracle.sha256_hex(ans0.tobytes())
+        stages = [f.launch_timed(d_parent, d_events, d_queries, d_answers, stream) for _ in range(3)]
+        stage_ms = {k: statistics.median([x[k] for x in stages]) for k in stages[0]}
+        f.capture(d_parent, d_events, d_queries, d_answers, stream)
+        for _ in range(args.warmup):
+            f.replay(stream)
+        stream.synchronize()
+
+        # ---- timed region: graph replays, inputs resident in HBM
+        clocks = ClockSampler(local)
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        clocks.start()
+        t0, t1 = ev_timer()
+        t0.record(stream)
+        for _ in range(args.steps):
+            f.replay(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        clk = clocks.stop()
+        ms = t0.elapsed_time(t1) / args.steps
+        if not np.array_equal(d_answers.cpu().numpy(), ans0):
+            raise SystemExit("answers changed between graph replays")
+        if ws > 1:
+            tt = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ms = float(tt.item())
+        info = f.info()
+
+        # ---- e2e through the public API: pinned host inputs in, answers out, every step
+        e2e = None
+        if not args.no_e2e:
+            torch.cuda.synchronize()
+            e0, e1 = ev_timer()
+            e0.record(stream)
+            for _ in range(args.steps):
+                d_parent.copy_(h_parent, non_blocking=True)
+                d_events.copy_(h_events, non_blocking=True)
+                d_queries.copy_(h_queries, non_blocking=True)
+                f.replay(stream)
+                h_answers.copy_(d_answers, non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ems = e0.elapsed_time(e1) / args.steps
+            if not np.array_equal(h_answers.numpy(), ans0):
+                raise SystemExit("e2e answers differ")
+            if ws > 1:
+                tt = torch.tensor([ems], device=dev)
+                torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+                ems = float(tt.item())
+            e2e = {"value": ws * Q / (ems / 1e3), "unit": "answers/s",
+                   "h2d_bytes_per_step": 4 * S + 16 * E + 12 * Q, "d2h_bytes_per_step": 8 * Q, "ms_per_step": ems}
+
+        # ---- plain form: one bw_replay_launch per tree, in sequence, same stream
+        lib = bw.gpu_lib()
+        args_t = []
+        need = 0
+        for t in range(T):
+            a = bw.BwReplayArgs()
+            s0, e0_, q0 = int(w.state_off[t]), int(w.event_off[t]), int(w.query_off[t])
+            a.n_states = int(w.state_off[t + 1]) - s0
+            a.parent = d_parent.data_ptr() + 4 * s0
+            a.n_keys = int(w.n_keys[t])
+            a.n_events = int(w.event_off[t + 1]) - e0_
+            a.events = d_events.data_ptr() + 16 * e0_ if a.n_events else None
+            a.n_queries = int(w.query_off[t + 1]) - q0
+            a.queries = d_queries.data_ptr() + 12 * q0 if a.n_queries else None
+            a.answers = d_answers.data_ptr() + 8 * q0 if a.n_queries else None
+            a.stream = stream.cuda_stream
+            nb = C.c_size_t(0)
+            if lib.bw_replay_workspace_size(C.byref(a), C.byref(nb)):
+                raise SystemExit("plain workspace size failed")
+            need = max(need, int(nb.value))
+            args_t.append(a)
+        pws = torch.empty(need, dtype=torch.uint8, device=dev)
+        for a in args_t:
+            a.workspace = pws.data_ptr()
+            a.workspace_bytes = need
+        d_answers.zero_()
+        plain_kernels = 0
+        k_info = C.c_int32(0)
+        p0, p1 = ev_timer()
+        torch.cuda.synchronize()
+        p0.record(stream)
+        for _ in range(max(1, args.plain_steps)):
+            for a in args_t:
+                if lib.bw_replay_launch(C.byref(a)):
+                    raise SystemExit("plain launch failed")
+                lib.bw_replay_last_info(C.byref(a), C.byref(k_info), None)
+                plain_kernels += int(k_info.value)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        plain_ms = p0.elapsed_time(p1) / max(1, args.plain_steps)
+        if not np.array_equal(d_answers.cpu().numpy(), ans0):
+            raise SystemExit("plain per-tree answers differ from the batched answers")
+
+    peak, peak_kind = measured_peaks()
+    sweep_bytes = 16 * E + 20 * Q
+    top = max(stage_ms, key=stage_ms.get)
+    achieved = sweep_bytes / (stage_ms["sweep"] / 1e3) / 1e9
+    value = ws * Q / (ms / 1e3)
+    plain_value = ws * Q / (plain_ms / 1e3)
+    line = {
+        "metric": BATCHED_METRIC, "value": value, "unit": "answers/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+        "config": dict(w.describe(), blocks=info["blocks"], tuning=info["tuning"],
+                       l2="inputs (3.9 GB) larger than L2 (no flush needed)", answers_sha256=digest,
+                       parallelism=f"replicas{ws}" if ws > 1 else "single"),
+        "plain": {"value": plain_value, "unit": "answers/s", "ms_per_step": plain_ms,
+                  "launches_per_step": T, "kernels_per_step": plain_kernels // max(1, args.plain_steps),
+                  "form": "one bw_replay_launch per tree, sequential on one stream"},
+        "batched_vs_plain": value / plain_value,
+        "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": profiled_traffic(w.name),
+                     "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": stage_ms["sweep"]},
+        "pipeline": {"stages_ms": stage_ms, "dominant_stage": top,
+                     "whole_step_gbs": w.algorithmic_bytes / (ms / 1e3) / 1e9,
+                     "whole_step_frac": w.algorithmic_bytes / (ms / 1e3) / 1e9 / peak},
+        "autotune": {"seconds": tune_s, "best_ms": tune_ms, "tuning": tuning},
+        "gpu_launches": info["kernels"] * args.steps,
+        "clocks": clk,
+        "setup": {"generate_s": gen_s},
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = forest_cpu_sample(w, args.cpu_seconds, 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def load_pkg():
     import __graft_entry__ as g
     return g.package()
@@ -261,6 +507,8 @@ def main():
         return reference_arm(args)
     if args.workload == "csr_lut":
         return bench_csr(args)
+    if args.workload == "batched_trees":
+        return bench_batched(args)
     import torch
     ws, rank, local = dist_env()
     if ws > 1:

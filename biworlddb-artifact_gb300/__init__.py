@@ -51,11 +51,29 @@ class BwCsr(C.Structure):
                 ("low", C.c_void_p)]
 
 
+class BwForestShape(C.Structure):
+    _fields_ = [("n_trees", C.c_int32), ("state_off", C.c_void_p), ("event_off", C.c_void_p),
+                ("query_off", C.c_void_p), ("n_keys", C.c_void_p)]
+
+
+class BwForestTuning(C.Structure):
+    _fields_ = [("block_work", C.c_int64), ("ctas_per_sm", C.c_int32), ("slice_ranks", C.c_int32),
+                ("tile", C.c_int32), ("reserved", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {"block_work": int(self.block_work), "ctas_per_sm": int(self.ctas_per_sm),
+                "slice_ranks": int(self.slice_ranks), "tile": int(self.tile)}
+
+
 GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch",
                "bw_replay_workspace_size", "bw_replay_launch", "bw_replay_status",
                "bw_replay_last_info", "bw_replay_timing_reset", "bw_replay_stage_times",
                "bw_device_info", "bw_replay_launch_noalloc",
-               "bw_csr_workspace_size", "bw_csr_build", "bw_csr_point", "bw_csr_range", "bw_csr_status"]
+               "bw_csr_workspace_size", "bw_csr_build", "bw_csr_point", "bw_csr_range", "bw_csr_status",
+               "bw_forest_create", "bw_forest_workspace_size", "bw_forest_bind", "bw_forest_launch",
+               "bw_forest_capture", "bw_forest_graph_launch", "bw_forest_status", "bw_forest_info",
+               "bw_forest_destroy", "bw_forest_autotune_workspace", "bw_forest_autotune",
+               "bw_forest_launch_timed"]
 
 _gpu = None
 
@@ -91,6 +109,20 @@ def gpu_lib(build_if_missing: bool = True):
         L.bw_csr_point.argtypes = [C.POINTER(BwCsr), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
         L.bw_csr_range.argtypes = [C.POINTER(BwCsr), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
         L.bw_csr_status.argtypes = [C.POINTER(BwCsr), C.POINTER(C.c_int32)]
+        P = C.c_void_p
+        L.bw_forest_create.argtypes = [C.POINTER(BwForestShape), C.POINTER(BwForestTuning), C.POINTER(P)]
+        L.bw_forest_workspace_size.argtypes = [P, C.POINTER(C.c_size_t)]
+        L.bw_forest_bind.argtypes = [P, P, C.c_size_t, P]
+        L.bw_forest_launch.argtypes = [P, P, P, P, P, P]
+        L.bw_forest_capture.argtypes = [P, P, P, P, P, P]
+        L.bw_forest_graph_launch.argtypes = [P, P]
+        L.bw_forest_launch_timed.argtypes = [P, P, P, P, P, P, C.POINTER(C.c_float)]
+        L.bw_forest_status.argtypes = [P, P, C.POINTER(C.c_int32)]
+        L.bw_forest_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(BwForestTuning)]
+        L.bw_forest_destroy.argtypes = [P]
+        L.bw_forest_autotune_workspace.argtypes = [C.POINTER(BwForestShape), C.POINTER(C.c_size_t)]
+        L.bw_forest_autotune.argtypes = [C.POINTER(BwForestShape), P, P, P, P, P, C.c_size_t, P, C.c_int32,
+                                         C.POINTER(BwForestTuning), C.POINTER(C.c_float)]
         _gpu = L
     return _gpu
 
@@ -181,6 +213,151 @@ def replay(parent, n_keys: int, events, queries, *, blocks: int = 0, chain: bool
         st = r.status()
         if st:
             raise ValueError(f"replay input rejected on the device: {STATUS_NAMES.get(st, st)}")
+    return answers
+
+
+class _ForestShape:
+    """Host copies of a forest's offsets (kept alive while the C struct points at them)."""
+
+    def __init__(self, state_off, event_off, query_off, n_keys):
+        import numpy as np
+        self.soff = np.ascontiguousarray(state_off, dtype=np.int64)
+        self.eoff = np.ascontiguousarray(event_off, dtype=np.int64)
+        self.qoff = np.ascontiguousarray(query_off, dtype=np.int64)
+        self.keys = np.ascontiguousarray(n_keys, dtype=np.uint32)
+        T = self.keys.size
+        if not (self.soff.size == self.eoff.size == self.qoff.size == T + 1):
+            raise ValueError("offset arrays need n_trees + 1 entries")
+        self.c = BwForestShape(T, self.soff.ctypes.data, self.eoff.ctypes.data, self.qoff.ctypes.data,
+                               self.keys.ctypes.data)
+
+
+def _tuning(t) -> "BwForestTuning | None":
+    if t is None:
+        return None
+    if isinstance(t, BwForestTuning):
+        return t
+    return BwForestTuning(int(t.get("block_work", 0)), int(t.get("ctas_per_sm", 0)), int(t.get("slice_ranks", 0)),
+                          int(t.get("tile", 0)), 0)
+
+
+class Forest:
+    """Batched replay of many independent version trees (bw_forest_* in bw_gpu.h).
+
+    ``state_off``/``event_off``/``query_off`` (n_trees + 1) and ``n_keys`` (n_trees)
+    are host arrays; tree t's slice of the concatenated ``parent`` (int32, local ids),
+    ``events`` (int64[E, 2], local states and keys) and ``queries`` (int32[Q, 3]) is a
+    plain replay input.  The plan owns its device workspace (bound once)."""
+
+    def __init__(self, state_off, event_off, query_off, n_keys, *, tuning=None, device=None, stream=None):
+        torch = _torch()
+        self.lib = gpu_lib()
+        self.shape = _ForestShape(state_off, event_off, query_off, n_keys)
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.handle = C.c_void_p()
+        tu = _tuning(tuning)
+        _check(self.lib.bw_forest_create(C.byref(self.shape.c), C.byref(tu) if tu is not None else None,
+                                         C.byref(self.handle)), "bw_forest_create")
+        nbytes = C.c_size_t(0)
+        _check(self.lib.bw_forest_workspace_size(self.handle, C.byref(nbytes)), "bw_forest_workspace_size")
+        self.workspace = torch.empty(max(int(nbytes.value), 256), dtype=torch.uint8, device=self.device)
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _check(self.lib.bw_forest_bind(self.handle, self.workspace.data_ptr(), self.workspace.numel(),
+                                       s.cuda_stream), "bw_forest_bind")
+        self.n_events = int(self.shape.eoff[-1])
+        self.n_queries = int(self.shape.qoff[-1])
+        self.n_states = int(self.shape.soff[-1])
+
+    def _ptrs(self, parent, events, queries, answers):
+        torch = _torch()
+        if parent.dtype != torch.int32 or events.dtype != torch.int64 or queries.dtype != torch.int32 or \
+                answers.dtype != torch.int64:
+            raise TypeError("parent int32, events int64[E,2], queries int32[Q,3], answers int64[Q] expected")
+        if parent.numel() != self.n_states or events.numel() != 2 * self.n_events or \
+                queries.numel() != 3 * self.n_queries or answers.numel() != self.n_queries:
+            raise ValueError("input sizes differ from the plan")
+        for t in (parent, events, queries, answers):
+            if not t.is_cuda or not t.is_contiguous():
+                raise ValueError("inputs must be contiguous CUDA tensors")
+        return (parent.data_ptr(), events.data_ptr() if self.n_events else None,
+                queries.data_ptr() if self.n_queries else None, answers.data_ptr() if self.n_queries else None)
+
+    def launch(self, parent, events, queries, answers, stream=None) -> None:
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _check(self.lib.bw_forest_launch(self.handle, *self._ptrs(parent, events, queries, answers), s.cuda_stream),
+               "bw_forest_launch")
+
+    def launch_timed(self, parent, events, queries, answers, stream=None) -> dict:
+        """One launch with CUDA events between the stages; returns per-stage ms (synchronises)."""
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        ms = (C.c_float * len(STAGES))()
+        _check(self.lib.bw_forest_launch_timed(self.handle, *self._ptrs(parent, events, queries, answers),
+                                               s.cuda_stream, ms), "bw_forest_launch_timed")
+        return dict(zip(STAGES, [float(x) for x in ms]))
+
+    def capture(self, parent, events, queries, answers, stream) -> None:
+        """Capture the launch with these tensors into a CUDA graph (on a non-default stream)."""
+        _check(self.lib.bw_forest_capture(self.handle, *self._ptrs(parent, events, queries, answers),
+                                          stream.cuda_stream), "bw_forest_capture")
+        self._graph_inputs = (parent, events, queries, answers)   # keep the captured buffers alive
+
+    def replay(self, stream=None) -> None:
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        _check(self.lib.bw_forest_graph_launch(self.handle, s.cuda_stream), "bw_forest_graph_launch")
+
+    def status(self, stream=None) -> int:
+        torch = _torch()
+        s = stream if stream is not None else torch.cuda.current_stream(self.device)
+        st = C.c_int32(0)
+        _check(self.lib.bw_forest_status(self.handle, s.cuda_stream, C.byref(st)), "bw_forest_status")
+        return int(st.value)
+
+    def info(self) -> dict:
+        b, k, tu = C.c_int32(0), C.c_int32(0), BwForestTuning()
+        _check(self.lib.bw_forest_info(self.handle, C.byref(b), C.byref(k), C.byref(tu)), "bw_forest_info")
+        return {"blocks": int(b.value), "kernels": int(k.value), "tuning": tu.as_dict()}
+
+    def __del__(self):
+        try:
+            if self.handle:
+                self.lib.bw_forest_destroy(self.handle)
+                self.handle = C.c_void_p()
+        except Exception:
+            pass
+
+
+def forest_autotune(state_off, event_off, query_off, n_keys, parent, events, queries, answers, *, reps: int = 3,
+                    stream=None):
+    """Time the autotuner's candidate tunings on these inputs; returns (tuning dict, ms)."""
+    torch = _torch()
+    lib = gpu_lib()
+    shape = _ForestShape(state_off, event_off, query_off, n_keys)
+    nbytes = C.c_size_t(0)
+    _check(lib.bw_forest_autotune_workspace(C.byref(shape.c), C.byref(nbytes)), "bw_forest_autotune_workspace")
+    ws = torch.empty(max(int(nbytes.value), 256), dtype=torch.uint8, device=parent.device)
+    s = stream if stream is not None else torch.cuda.current_stream(parent.device)
+    best, ms = BwForestTuning(), C.c_float(0)
+    _check(lib.bw_forest_autotune(C.byref(shape.c), parent.data_ptr(), events.data_ptr() if events.numel() else None,
+                                  queries.data_ptr() if queries.numel() else None,
+                                  answers.data_ptr() if answers.numel() else None, ws.data_ptr(), ws.numel(),
+                                  s.cuda_stream, int(reps), C.byref(best), C.byref(ms)), "bw_forest_autotune")
+    return best.as_dict(), float(ms.value)
+
+
+def forest_replay(state_off, event_off, query_off, n_keys, parent, events, queries, *, tuning=None,
+                  check: bool = True):
+    """One batched replay on the current stream; returns int64 answers on the device."""
+    torch = _torch()
+    f = Forest(state_off, event_off, query_off, n_keys, tuning=tuning, device=parent.device)
+    answers = torch.empty(f.n_queries, dtype=torch.int64, device=parent.device)
+    f.launch(parent, events, queries, answers)
+    if check:
+        st = f.status()
+        if st:
+            raise ValueError(f"forest input rejected on the device: {STATUS_NAMES.get(st, st)}")
     return answers
 
 

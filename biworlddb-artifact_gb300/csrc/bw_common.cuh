@@ -187,12 +187,5 @@ inline int device_inclusive_scan_i64(int64_t* x, int64_t n, int64_t* tmp, cudaSt
   return (int)cudaGetLastError();
 }
 
-// Clamp block bounds to the trimmed step count (steps after the last query step
-// cannot change any answer).
-__global__ void k_trim_bounds(int32_t* bounds, int32_t B, const int32_t* last_q) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b <= B) bounds[b] = min(bounds[b], *last_q);
-}
-
 }  // namespace
 }  // namespace bw

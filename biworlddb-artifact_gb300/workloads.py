@@ -14,6 +14,13 @@ configured workloads:
   earlier state, 40,000,000 events with Zipf s=1.2 keys over 65,536 cells and
   delta = round(lognormal(7.3, 0.9)), 50,000,000 queries at uniform states with
   uniform intervals.
+* ``batched_trees`` (batched uneven trees): 4,096 independent version trees
+  with lognormal state counts (median 2,000, sigma 1.6, capped at 200,000;
+  about 30M states in all), each extending the previous state with p=0.95 or
+  forking from a uniform earlier state, a key domain per tree drawn uniformly from
+  the powers of two 1,024 ... 262,144, Poisson(8) events per state with Zipf s=1.1
+  keys and delta = round(lognormal(7, 1)) with a negative sign at p=0.1, and
+  1,000 range queries per tree (uniform states, uniform intervals).
 * ``csr_lut`` (sparse-key rank index): 10,000,000 distinct u64 keys over
   [0, 2^40), 20,000,000 (key, delta) events on them, 100,000,000 point and
   100,000,000 range lookups, half present keys and half absent.
@@ -122,7 +129,108 @@ CONFIGS = {"plain_chain": plain_chain, "trip_tree": trip_tree}
 def make(name: str, seed: int = 0, scale: float = 1.0):
     if name == "csr_lut":
         return csr_lut(seed=seed, scale=scale)
+    if name == "batched_trees":
+        return batched_trees(seed=seed, scale=scale)
     return CONFIGS[name](seed=seed, scale=scale)
+
+
+@dataclass
+class ForestWorkload:
+    """Independent version trees concatenated: tree t owns states
+    [state_off[t], state_off[t+1]) of ``parent`` (tree-local ids), events
+    [event_off[t], event_off[t+1]) and queries [query_off[t], query_off[t+1]) (local
+    states, keys in [0, n_keys[t]))."""
+    name: str
+    state_off: np.ndarray   # int64[T+1]
+    event_off: np.ndarray   # int64[T+1]
+    query_off: np.ndarray   # int64[T+1]
+    n_keys: np.ndarray      # uint32[T]
+    parent: np.ndarray      # int32[S]
+    events: np.ndarray      # EVENT_DTYPE[E]
+    queries: np.ndarray     # QUERY_DTYPE[Q]
+
+    @property
+    def n_trees(self) -> int:
+        return int(self.n_keys.size)
+
+    @property
+    def algorithmic_bytes(self) -> int:
+        """4S + 16E + 20Q: parent arrays, event records, query records + answers."""
+        return 4 * len(self.parent) + 16 * len(self.events) + 20 * len(self.queries)
+
+    def tree(self, t: int) -> Workload:
+        s0, s1 = int(self.state_off[t]), int(self.state_off[t + 1])
+        e0, e1 = int(self.event_off[t]), int(self.event_off[t + 1])
+        q0, q1 = int(self.query_off[t]), int(self.query_off[t + 1])
+        par = self.parent[s0:s1]
+        chain = bool(np.all(par[1:] == np.arange(s1 - s0 - 1, dtype=np.int32)))
+        return Workload(f"{self.name}[{t}]", par, int(self.n_keys[t]), self.events[e0:e1], self.queries[q0:q1],
+                        chain)
+
+    def describe(self) -> dict:
+        sizes = np.diff(self.state_off)
+        return {"workload": self.name, "trees": self.n_trees, "states": int(len(self.parent)),
+                "events": int(len(self.events)), "queries": int(len(self.queries)),
+                "states_per_tree": {"median": int(np.median(sizes)), "max": int(sizes.max()),
+                                    "min": int(sizes.min())},
+                "key_domains": sorted({int(c) for c in self.n_keys})}
+
+
+_ZIPF_CACHE: dict = {}
+
+
+def _zipf_table(C: int, s: float, seed: int):
+    key = (C, s, seed)
+    if key not in _ZIPF_CACHE:
+        w = np.arange(1, C + 1, dtype=np.float64) ** (-s)
+        cdf = np.cumsum(w)
+        cdf /= cdf[-1]
+        perm = np.random.default_rng((seed, C)).permutation(C).astype(np.uint32)
+        _ZIPF_CACHE[key] = (cdf, perm)
+    return _ZIPF_CACHE[key]
+
+
+def batched_trees(seed: int = 0, scale: float = 1.0, *, trees: int = 4096, median: float = 2000.0,
+                  sigma: float = 1.6, cap: int = 200_000, p_extend: float = 0.95, events_per_state: float = 8.0,
+                  queries_per_tree: int = 1000, domain_bits=(10, 18), zipf: float = 1.1) -> ForestWorkload:
+    """Batched uneven trees (``scale`` multiplies the tree count)."""
+    rng = np.random.default_rng(seed)
+    T = max(1, int(round(trees * scale)))
+    sizes = np.clip(np.rint(rng.lognormal(np.log(median), sigma, size=T)), 2, cap).astype(np.int64)
+    n_keys = (1 << rng.integers(domain_bits[0], domain_bits[1] + 1, size=T)).astype(np.uint32)
+    state_off = np.zeros(T + 1, np.int64)
+    np.cumsum(sizes, out=state_off[1:])
+    S = int(state_off[-1])
+    parent = np.empty(S, np.int32)
+    counts = rng.poisson(events_per_state, size=S).astype(np.int64)
+    for t in range(T):
+        parent[state_off[t]:state_off[t + 1]] = _fork_tree(rng, int(sizes[t]), p_extend)
+    cum = np.zeros(S + 1, np.int64)
+    np.cumsum(counts, out=cum[1:])
+    event_off = cum[state_off]
+    E = int(event_off[-1])
+    ev = np.empty(E, dtype=EVENT_DTYPE)
+    Qt = int(queries_per_tree)
+    qs = np.empty(T * Qt, dtype=QUERY_DTYPE)
+    query_off = np.arange(T + 1, dtype=np.int64) * Qt
+    for t in range(T):
+        s0, s1 = int(state_off[t]), int(state_off[t + 1])
+        e0, e1 = int(event_off[t]), int(event_off[t + 1])
+        C = int(n_keys[t])
+        n = e1 - e0
+        ev["state"][e0:e1] = np.repeat(np.arange(s1 - s0, dtype=np.uint32), counts[s0:s1])
+        cdf, perm = _zipf_table(C, zipf, seed)
+        ranks = np.minimum(np.searchsorted(cdf, rng.random(n)), C - 1)
+        ev["key"][e0:e1] = perm[ranks]
+        d = np.rint(rng.lognormal(7.0, 1.0, size=n)).astype(np.int64)
+        d[rng.random(n) < 0.1] *= -1
+        ev["delta"][e0:e1] = d
+        q = qs[t * Qt:(t + 1) * Qt]
+        q["state"] = np.sort(rng.integers(0, s1 - s0, size=Qt)).astype(np.uint32)
+        a = rng.integers(0, C + 1, size=Qt, dtype=np.int64)
+        b = rng.integers(0, C + 1, size=Qt, dtype=np.int64)
+        q["lo"], q["hi"] = np.minimum(a, b), np.maximum(a, b)
+    return ForestWorkload("batched_trees", state_off, event_off, query_off, n_keys, parent, ev, qs)
 
 
 @dataclass

@@ -117,7 +117,7 @@ typedef struct {
   int32_t flags;             /* BW_REPLAY_* */
 } BwReplayArgs;
 
-#define BW_REPLAY_CHAIN_HINT 1  /* caller asserts parent[v] == v-1 (skips tree linearisation) */
+#define BW_REPLAY_CHAIN_HINT 1  /* caller asserts parent[v] == v-1; any fork is rejected (BW_STATUS_BAD_PARENT) */
 #define BW_REPLAY_TIMING 2      /* record CUDA events between pipeline stages (see below) */
 
 /* Pipeline stages timed under BW_REPLAY_TIMING, in order. */
@@ -176,6 +176,75 @@ int bw_replay_stage_times(float* ms, int32_t* launches);
  * race.  A non-NULL host `status` makes the call wait for its stream and receive
  * the BW_STATUS_* code; NULL returns once the work is enqueued. */
 int bw_replay_launch_noalloc(const BwReplayArgs* a, int32_t* status);
+
+/* ============================================================ batched version forests
+ * Thousands of independent version trees replayed in one pipeline (the reference
+ * replays one chain per worker process, panel_batch_gpu.cpp:182-214, and its
+ * parallel_jobs.py runs many of those side by side).  Tree t owns states
+ * [state_off[t], state_off[t+1]), events [event_off[t], event_off[t+1]), queries
+ * [query_off[t], query_off[t+1]) and the key domain [0, n_keys[t]); each tree's
+ * slice of `parent`, `events` and `queries` is exactly a plain replay input
+ * (tree-local state ids, parent[local 0] = -1, parent[l] < l, events and queries
+ * grouped by local state).  answers[j] is the plain answer of query j within its
+ * tree.  Every tree is cut into state blocks that never span trees; persistent
+ * CTAs take the blocks from one queue, largest estimated work first. */
+typedef struct {
+  int32_t n_trees;
+  const int64_t* state_off;  /* host, n_trees+1 (state_off[0] = 0; every tree has >= 1 state) */
+  const int64_t* event_off;  /* host, n_trees+1 */
+  const int64_t* query_off;  /* host, n_trees+1 */
+  const uint32_t* n_keys;    /* host, n_trees */
+} BwForestShape;
+
+typedef struct {
+  int64_t block_work;   /* target work of one state block, in event units (an event 2,
+                           a query 2, an Euler step 64); 0 = auto */
+  int32_t ctas_per_sm;  /* persistent sweep CTAs per SM, 1 or 2; 0 = auto */
+  int32_t slice_ranks;  /* cap on the distinct keys of one rank-LUT slice held in
+                           shared memory; 0 = as many as fit */
+  int32_t tile;         /* sweep tile geometry: 1 narrow (2 events + 2 queries staged per
+                           thread, 32 steps), 2 wide (4 events + 1 query, 64 steps);
+                           0 = by the query/event ratio */
+  int32_t reserved;
+} BwForestTuning;
+
+typedef struct BwForest BwForest;   /* opaque plan: host tables, layout, CUDA graph */
+
+/* Plan a forest (host only; NULL tuning = auto).  BW_EINVAL for malformed shapes. */
+int bw_forest_create(const BwForestShape* shape, const BwForestTuning* tuning, BwForest** out);
+int bw_forest_workspace_size(const BwForest* f, size_t* bytes);
+/* Attach a device workspace (>= bw_forest_workspace_size, 256-byte aligned) and
+ * upload the plan's tables into it; synchronises `stream`.  Needed once per
+ * workspace, before any launch or capture. */
+int bw_forest_bind(BwForest* f, void* workspace, size_t workspace_bytes, void* stream);
+/* Enqueue the whole replay on `stream`: kernels and one memset, no host copies. */
+int bw_forest_launch(BwForest* f, const int32_t* parent, const BwEvent* events, const BwQuery* queries,
+                     int64_t* answers, void* stream);
+/* Capture bw_forest_launch with these device pointers into a CUDA graph owned by
+ * the plan (stream must not be the legacy default stream); bw_forest_graph_launch
+ * replays it. */
+int bw_forest_capture(BwForest* f, const int32_t* parent, const BwEvent* events, const BwQuery* queries,
+                      int64_t* answers, void* stream);
+int bw_forest_graph_launch(BwForest* f, void* stream);
+/* One launch with CUDA events between the pipeline stages; synchronises `stream`
+ * and writes the milliseconds of each stage (ms[BW_STAGE_COUNT], BW_STAGE_*). */
+int bw_forest_launch_timed(BwForest* f, const int32_t* parent, const BwEvent* events, const BwQuery* queries,
+                           int64_t* answers, void* stream, float* ms);
+/* Synchronise `stream` and read the device status word (BW_STATUS_*). */
+int bw_forest_status(BwForest* f, void* stream, int32_t* status);
+/* Blocks, kernels per launch, and the tuning in effect. */
+int bw_forest_info(const BwForest* f, int32_t* blocks, int32_t* kernels, BwForestTuning* tuning);
+int bw_forest_destroy(BwForest* f);
+/* Autotuner: times candidate tunings on the caller's inputs (sweep CTAs per SM x
+ * block work, then the other tile geometry, then narrower LUT slices, each at the
+ * best so far) with `reps` launches after a warm-up, skips candidates the device
+ * rejects, and returns the fastest in *best (and its mean milliseconds).  The
+ * workspace must hold bw_forest_autotune_workspace bytes; answers are overwritten.
+ * BW_EINVAL when no candidate ran (invalid input). */
+int bw_forest_autotune_workspace(const BwForestShape* shape, size_t* bytes);
+int bw_forest_autotune(const BwForestShape* shape, const int32_t* parent, const BwEvent* events,
+                       const BwQuery* queries, int64_t* answers, void* workspace, size_t workspace_bytes,
+                       void* stream, int32_t reps, BwForestTuning* best, float* best_ms);
 
 /* ============================================================ sparse-key rank index */
 /* The CSR rank-LUT of the reference's sparse engine (CsrBase, sparse_engine.hpp:70-102;

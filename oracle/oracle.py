@@ -157,6 +157,20 @@ def ev_sweep(parent, n_keys: int, events, queries) -> np.ndarray:
     return ans
 
 
+def ev_forest(state_off, event_off, query_off, n_keys, parent, events, queries, fn=None) -> np.ndarray:
+    """Answers of a forest of independent trees: each tree's slice replayed alone
+    with the preorder checker (or ``fn``), concatenated in tree order."""
+    fn = fn or (lambda p, C, e, q: ev_sweep(p, C, e, q))
+    out = np.zeros(int(query_off[-1]), dtype=np.int64)
+    for t in range(len(n_keys)):
+        s0, s1 = int(state_off[t]), int(state_off[t + 1])
+        e0, e1 = int(event_off[t]), int(event_off[t + 1])
+        q0, q1 = int(query_off[t]), int(query_off[t + 1])
+        if q1 > q0:
+            out[q0:q1] = fn(parent[s0:s1], int(n_keys[t]), events[e0:e1], queries[q0:q1])
+    return out
+
+
 def ev_sweep_prefix(parent, n_keys: int, events, queries, limit_steps: int):
     """Preorder replay of the first `limit_steps` states; returns (answers,
     answered, seconds of the replay loop)."""

@@ -1,0 +1,135 @@
+"""GPU parity of the batched forest replay (bw_forest_* through the C ABI) against
+the oracle, tree by tree: uneven tree sizes and shapes, per-tree key domains,
+trees without events or queries, one-state trees, many blocks per tree (multi-group
+carry scans), CUDA-graph replays, the autotuner, and per-tree input errors."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import evgen
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["chain", "bushy", "star", "fork"]
+
+
+def make_forest(rng, T, max_states=3000, max_keys=70000, ev_per_state=6.0, q_per_tree=200, big=False):
+    parents, events, queries, soff, eoff, qoff, keys = [], [], [], [0], [0], [0], []
+    for t in range(T):
+        S = int(rng.integers(1, max_states + 1)) if t % 7 else 1 + int(rng.integers(0, 3))
+        C = int(rng.integers(1, max_keys + 1)) if t % 5 else int(rng.choice([1, 64, 65]))
+        kind = KINDS[t % len(KINDS)]
+        parents.append(evgen.make_tree(S, kind, rng, p_extend=0.95) if S > 1 else np.array([-1], np.int32))
+        E = 0 if t % 11 == 3 else int(rng.poisson(ev_per_state * S))
+        Q = 0 if t % 13 == 4 else int(rng.integers(1, q_per_tree + 1))
+        events.append(evgen.make_events(S, C, E, rng, zipf=1.1 if t % 2 else 0.0, big=big))
+        queries.append(evgen.make_queries(S, C, Q, rng))
+        soff.append(soff[-1] + S); eoff.append(eoff[-1] + E); qoff.append(qoff[-1] + Q); keys.append(C)
+    return (np.array(soff, np.int64), np.array(eoff, np.int64), np.array(qoff, np.int64),
+            np.array(keys, np.uint32), np.concatenate(parents).astype(np.int32),
+            np.concatenate(events), np.concatenate(queries))
+
+
+def run_forest(bw, torch, F, tuning=None):
+    soff, eoff, qoff, keys, par, ev, qs = F
+    p, e, q = evgen.to_device(torch, par, ev, qs)
+    return bw.forest_replay(soff, eoff, qoff, keys, p, e, q, tuning=tuning).cpu().numpy()
+
+
+@pytest.mark.parametrize("seed,T,tuning", [
+    (1, 40, None),
+    (2, 120, None),
+    (3, 30, {"block_work": 65536}),                     # many blocks per tree
+    (4, 25, {"block_work": 20000, "ctas_per_sm": 1}),   # > 16 rows: two-pass carry scan
+    (5, 60, {"slice_ranks": 512}),                       # several key slices per block
+    (6, 50, {"tile": 1, "block_work": 65536}),           # narrow sweep tiles
+    (7, 50, {"tile": 2, "ctas_per_sm": 1}),              # wide sweep tiles, one CTA per SM
+])
+def test_forest_matches_oracle(bw, torch_cuda, oracle_mod, seed, T, tuning):
+    rng = np.random.default_rng(seed)
+    F = make_forest(rng, T)
+    want = oracle_mod.ev_forest(*F)
+    got = run_forest(bw, torch_cuda, F, tuning)
+    np.testing.assert_array_equal(got, want)
+
+
+def test_forest_wrapping_deltas(bw, torch_cuda, oracle_mod):
+    rng = np.random.default_rng(11)
+    F = make_forest(rng, 30, max_states=800, big=True)
+    np.testing.assert_array_equal(run_forest(bw, torch_cuda, F, {"block_work": 40000}), oracle_mod.ev_forest(*F))
+
+
+def test_forest_equals_plain_per_tree(bw, torch_cuda):
+    rng = np.random.default_rng(12)
+    F = make_forest(rng, 16, max_states=2000)
+    soff, eoff, qoff, keys, par, ev, qs = F
+    got = run_forest(bw, torch_cuda, F)
+    for t in range(len(keys)):
+        s0, s1, e0, e1, q0, q1 = soff[t], soff[t + 1], eoff[t], eoff[t + 1], qoff[t], qoff[t + 1]
+        p, e, q = evgen.to_device(torch_cuda, par[s0:s1], ev[e0:e1], qs[q0:q1])
+        plain = bw.replay(p, int(keys[t]), e, q).cpu().numpy()
+        np.testing.assert_array_equal(got[q0:q1], plain)
+
+
+def test_forest_graph_replay_and_autotune(bw, torch_cuda, oracle_mod):
+    torch = torch_cuda
+    rng = np.random.default_rng(13)
+    F = make_forest(rng, 64, max_states=4000)
+    soff, eoff, qoff, keys, par, ev, qs = F
+    want = oracle_mod.ev_forest(*F)
+    p, e, q = evgen.to_device(torch, par, ev, qs)
+    ans = torch.empty(len(qs), dtype=torch.int64, device="cuda")
+    tuning, ms = bw.forest_autotune(soff, eoff, qoff, keys, p, e, q, ans, reps=2)
+    assert ms > 0 and tuning["ctas_per_sm"] in (1, 2) and tuning["block_work"] > 0
+    np.testing.assert_array_equal(ans.cpu().numpy(), want)
+    f = bw.Forest(soff, eoff, qoff, keys, tuning=tuning)
+    s = torch.cuda.Stream()
+    ans.fill_(0)
+    with torch.cuda.stream(s):
+        f.capture(p, e, q, ans, s)
+        for _ in range(3):
+            f.replay(s)
+    s.synchronize()
+    assert f.status(s) == 0
+    np.testing.assert_array_equal(ans.cpu().numpy(), want)
+    info = f.info()
+    assert info["blocks"] >= len(keys) and info["kernels"] > 10
+
+
+@pytest.mark.parametrize("bad", ["parent", "key", "query", "state"])
+def test_forest_rejects_bad_tree(bw, torch_cuda, bad):
+    rng = np.random.default_rng(14)
+    F = list(make_forest(rng, 12, max_states=300))
+    soff, eoff, qoff, keys, par, ev, qs = F
+    par, ev, qs = par.copy(), ev.copy(), qs.copy()
+    t = 5
+    if bad == "parent":
+        par[soff[t] + soff[t + 1] - soff[t] - 1] = soff[t + 1] - soff[t] + 3   # parent beyond itself
+        if soff[t + 1] - soff[t] == 1:
+            par[soff[t]] = 0
+        code = 5
+    elif bad == "key":
+        i = next(i for i in range(len(keys)) if eoff[i + 1] > eoff[i])
+        ev["key"][eoff[i]] = keys[i]
+        code = 2
+    elif bad == "query":
+        i = next(i for i in range(len(keys)) if qoff[i + 1] > qoff[i])
+        qs["hi"][qoff[i]] = keys[i] + 1
+        code = 4
+    else:
+        i = next(i for i in range(len(keys)) if eoff[i + 1] > eoff[i])
+        ev["state"][eoff[i + 1] - 1] = soff[i + 1] - soff[i]
+        code = 7
+    p, e, q = evgen.to_device(torch_cuda, par, ev, qs)
+    f = bw.Forest(soff, eoff, qoff, keys)
+    ans = torch_cuda.empty(len(qs), dtype=torch_cuda.int64, device="cuda")
+    f.launch(p, e, q, ans)
+    assert f.status() == code
+
+
+def test_forest_shape_errors(bw, torch_cuda):
+    with pytest.raises(RuntimeError):
+        bw.Forest([0, 0], [0, 0], [0, 0], [4])           # a tree without states
+    with pytest.raises(RuntimeError):
+        bw.Forest([0, 3], [0, 2], [0, 1], [0])           # empty key domain

@@ -136,3 +136,22 @@ def test_event_inputs_rejected(oracle_mod):
     badp[5] = 7
     with pytest.raises(ValueError):
         oracle_mod.ev_sweep(badp, 8, ev, qs)
+
+
+def test_forest_oracle_is_per_tree_replay(oracle_mod):
+    """ev_forest answers each tree's queries from that tree alone (checked against
+    the ancestor-walk brute force)."""
+    rng = np.random.default_rng(3)
+    soff, eoff, qoff, keys, parts = [0], [0], [0], [], ([], [], [])
+    for t in range(6):
+        S, C = int(rng.integers(1, 300)), int(rng.integers(1, 500))
+        par = evgen.make_tree(S, ["chain", "fork", "star"][t % 3], rng) if S > 1 else np.array([-1], np.int32)
+        ev = evgen.make_events(S, C, int(rng.integers(0, 3000)), rng)
+        qs = evgen.make_queries(S, C, int(rng.integers(0, 400)), rng)
+        for lst, x in zip(parts, (par, ev, qs)):
+            lst.append(x)
+        soff.append(soff[-1] + S); eoff.append(eoff[-1] + len(ev)); qoff.append(qoff[-1] + len(qs)); keys.append(C)
+    F = (np.array(soff), np.array(eoff), np.array(qoff), np.array(keys), np.concatenate(parts[0]),
+         np.concatenate(parts[1]), np.concatenate(parts[2]))
+    brute = oracle_mod.ev_forest(*F, fn=lambda p, C, e, q: oracle_mod.ev_bruteforce(p, e, q))
+    np.testing.assert_array_equal(oracle_mod.ev_forest(*F), brute)

@@ -153,3 +153,23 @@ def test_rejected_inputs_report_status(bw, torch_cuda, bad):
     # the context stays usable after a rejected input
     ok = evgen.make_events(S, C, 100, rng)
     run(bw, torch_cuda, evgen.make_tree(S, "chain", rng), C, ok, evgen.make_queries(S, C, 10, rng))
+
+
+@pytest.mark.parametrize("kind,blocks", [("fork", 0), ("chain", 3), ("star", 0)])
+def test_heavy_states(bw, torch_cuda, oracle_mod, kind, blocks):
+    """States with more events and more queries than one sweep tile stages, between
+    ordinary states, on enter and exit steps."""
+    rng = np.random.default_rng(21 + blocks)
+    S, C = 600, 5000
+    parent = evgen.make_tree(S, kind, rng)
+    ecount = rng.poisson(3, S)
+    qcount = rng.poisson(2, S)
+    heavy = rng.choice(S, 12, replace=False)
+    ecount[heavy] = rng.integers(800, 4000, heavy.size)
+    qcount[heavy[:6]] = rng.integers(600, 2000, 6)
+    ev = evgen.make_events(S, C, int(ecount.sum()), rng, zipf=1.1)
+    ev["state"] = np.repeat(np.arange(S, dtype=np.uint32), ecount)
+    qs = evgen.make_queries(S, C, int(qcount.sum()), rng)
+    qs["state"] = np.repeat(np.arange(S, dtype=np.uint32), qcount)
+    want = oracle_mod.ev_sweep(parent, C, ev, qs)
+    np.testing.assert_array_equal(run(bw, torch_cuda, parent, C, ev, qs, blocks=blocks), want)
