@@ -70,6 +70,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample duration")
     ap.add_argument("--plain-steps", type=int, default=2, help="steps of the sequential plain form")
     ap.add_argument("--full-check", action="store_true", help="check every answer against the oracle")
+    ap.add_argument("--no-autotune", action="store_true", help="batched: use the default tuning")
+    ap.add_argument("--no-serving", action="store_true", help="batched: skip the served-store runs")
+    ap.add_argument("--loads", default="1e6,5e6,2e7", help="serving: offered loads in requests/s")
+    ap.add_argument("--hbm-cap-gb", type=float, default=120.0, help="serving: admission cap of the store")
     return ap.parse_args()
 
 
@@ -338,7 +342,11 @@ def bench_batched(args):
 
     with torch.cuda.stream(stream):
         t_tune = time.perf_counter()
-        tuning, tune_ms = bw.forest_autotune(*shape, d_parent, d_events, d_queries, d_answers, reps=2, stream=stream)
+        if args.no_autotune:
+            tuning, tune_ms = None, None
+        else:
+            tuning, tune_ms = bw.forest_autotune(*shape, d_parent, d_events, d_queries, d_answers, reps=2,
+                                                 stream=stream)
         tune_s = time.perf_counter() - t_tune
         f = bw.Forest(*shape, tuning=tuning, device=dev, stream=stream)
         f.launch_timed(d_parent, d_events, d_queries, d_answers, stream)
@@ -415,6 +423,7 @@ def bench_batched(args):
                    "h2d_bytes_per_step": 4 * S + 16 * E + 12 * Q, "d2h_bytes_per_step": 8 * Q, "ms_per_step": ems}
 
         # ---- plain form: one bw_replay_launch per tree, in sequence, same stream
+        plain_ms = None
         lib = bw.gpu_lib()
         args_t = []
         need = 0
@@ -439,30 +448,31 @@ def bench_batched(args):
         for a in args_t:
             a.workspace = pws.data_ptr()
             a.workspace_bytes = need
-        d_answers.zero_()
         plain_kernels = 0
-        k_info = C.c_int32(0)
-        p0, p1 = ev_timer()
-        torch.cuda.synchronize()
-        p0.record(stream)
-        for _ in range(max(1, args.plain_steps)):
-            for a in args_t:
-                if lib.bw_replay_launch(C.byref(a)):
-                    raise SystemExit("plain launch failed")
-                lib.bw_replay_last_info(C.byref(a), C.byref(k_info), None)
-                plain_kernels += int(k_info.value)
-        p1.record(stream)
-        torch.cuda.synchronize()
-        plain_ms = p0.elapsed_time(p1) / max(1, args.plain_steps)
-        if not np.array_equal(d_answers.cpu().numpy(), ans0):
-            raise SystemExit("plain per-tree answers differ from the batched answers")
+        if args.plain_steps > 0:
+            d_answers.zero_()
+            k_info = C.c_int32(0)
+            p0, p1 = ev_timer()
+            torch.cuda.synchronize()
+            p0.record(stream)
+            for _ in range(args.plain_steps):
+                for a in args_t:
+                    if lib.bw_replay_launch(C.byref(a)):
+                        raise SystemExit("plain launch failed")
+                    lib.bw_replay_last_info(C.byref(a), C.byref(k_info), None)
+                    plain_kernels += int(k_info.value)
+            p1.record(stream)
+            torch.cuda.synchronize()
+            plain_ms = p0.elapsed_time(p1) / args.plain_steps
+            if not np.array_equal(d_answers.cpu().numpy(), ans0):
+                raise SystemExit("plain per-tree answers differ from the batched answers")
 
     peak, peak_kind = measured_peaks()
     sweep_bytes = 16 * E + 20 * Q
     top = max(stage_ms, key=stage_ms.get)
     achieved = sweep_bytes / (stage_ms["sweep"] / 1e3) / 1e9
     value = ws * Q / (ms / 1e3)
-    plain_value = ws * Q / (plain_ms / 1e3)
+    plain_value = ws * Q / (plain_ms / 1e3) if plain_ms else None
     line = {
         "metric": BATCHED_METRIC, "value": value, "unit": "answers/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -473,7 +483,7 @@ def bench_batched(args):
         "plain": {"value": plain_value, "unit": "answers/s", "ms_per_step": plain_ms,
                   "launches_per_step": T, "kernels_per_step": plain_kernels // max(1, args.plain_steps),
                   "form": "one bw_replay_launch per tree, sequential on one stream"},
-        "batched_vs_plain": value / plain_value,
+        "batched_vs_plain": value / plain_value if plain_value else None,
         "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": profiled_traffic(w.name),
                      "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": stage_ms["sweep"]},
@@ -489,10 +499,77 @@ def bench_batched(args):
         line["e2e"] = e2e
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = forest_cpu_sample(w, args.cpu_seconds, 1)
+    if not args.no_serving:
+        del d_events, d_queries, d_parent, d_answers, f, pws
+        torch.cuda.empty_cache()
+        line["served"] = run_serving(args, bw, args.seed, args.scale)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_serving(args, bw, seed: int, scale: float):
+    """Served store on the trip-log tree: the request log at each offered load (open
+    loop, Poisson arrivals), every answer checked against the oracle's replay of the
+    final tree.  Returns a dict of per-load latency percentiles and rates."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    t = time.perf_counter()
+    log = bw.workloads.serving(seed, scale)
+    gen_s = time.perf_counter() - t
+    b = log.base
+    t = time.perf_counter()
+    srv = bw.Server(b.parent, b.n_keys, b.events, max_versions=len(b.parent) + len(log.requests),
+                    max_events=len(b.events) + len(log.commit_events),
+                    hbm_cap_bytes=int(args.hbm_cap_gb * 1e9))
+    build_s = time.perf_counter() - t
+    par, ev, qs, order = log.final_forest()
+    want = np.zeros(len(log.requests), dtype=np.int64)
+    want[order] = oracle.ev_sweep(par, b.n_keys, ev, qs)
+    q = log.requests["kind"] == 0
+    loads = []
+    for rate in [float(x) for x in args.loads.split(",") if x]:
+        srv.reset()
+        ans, lat, st = srv.run(log.requests, log.commit_events, log.arrival / rate, max_inflight=1 << 16)
+        if not np.array_equal(ans[q], want[q]):
+            raise SystemExit(f"served answers differ from the oracle at {rate:g} requests/s")
+        loads.append({"offered_rps": rate, "achieved_rps": st["requests"] / st["wall_s"],
+                      "answers_per_s": st["queries"] / st["wall_s"],
+                      "p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
+                      "p50_query_us": float(np.percentile(lat[q], 50)),
+                      "p99_query_us": float(np.percentile(lat[q], 99)), "wall_s": st["wall_s"]})
+    info = srv.info()
+    srv.close()
+    return {"config": log.describe(), "store": {"checkpoints": info["checkpoints"], "spacing": info["spacing"],
+                                                "store_gb": info["store_bytes"] / 1e9,
+                                                "cap_gb": args.hbm_cap_gb,
+                                                "loop_warps": info["warps"]},
+            "loads": loads, "exact": True, "answers_sha256": oracle.sha256_hex(want[q].tobytes()),
+            "setup_s": {"generate": gen_s, "store_build": build_s}}
+
+
+def bench_serving(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    bw = load_pkg()
+    bw.build()
+    clocks = ClockSampler(local)
+    clocks.start()
+    res = run_serving(args, bw, args.seed, args.scale)
+    clk = clocks.stop()
+    top = res["loads"][-1]
+    line = {"metric": "served range-sum answers/s (persistent request loop, open-loop Poisson arrivals)",
+            "value": top["answers_per_s"], "unit": "answers/s", "n_gpus": 1, "steps": len(res["loads"]),
+            "warmup": 0, "ms_per_step": top["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+            "config": dict(res["config"], offered_rps=top["offered_rps"]),
+            "p50_us": top["p50_us"], "p99_us": top["p99_us"], "served": res, "gpu_launches": 1 + len(res["loads"]),
+            "clocks": clk}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     return 0
 
 
@@ -509,6 +586,8 @@ def main():
         return bench_csr(args)
     if args.workload == "batched_trees":
         return bench_batched(args)
+    if args.workload == "serving":
+        return bench_serving(args)
     import torch
     ws, rank, local = dist_env()
     if ws > 1:

@@ -65,6 +65,22 @@ class BwForestTuning(C.Structure):
                 "slice_ranks": int(self.slice_ranks), "tile": int(self.tile)}
 
 
+class BwServeConfig(C.Structure):
+    _fields_ = [("n_states", C.c_int32), ("parent", C.c_void_p), ("n_keys", C.c_uint32), ("n_events", C.c_int64),
+                ("events", C.c_void_p), ("max_versions", C.c_int32), ("max_events", C.c_int64),
+                ("hbm_cap_bytes", C.c_size_t), ("chain_limit", C.c_int32)]
+
+
+class BwServeStats(C.Structure):
+    _fields_ = [("requests", C.c_int64), ("queries", C.c_int64), ("commits", C.c_int64), ("forks", C.c_int64),
+                ("wall_s", C.c_double), ("checkpoints", C.c_int32), ("spacing", C.c_int32),
+                ("store_bytes", C.c_size_t), ("warps", C.c_int32), ("reserved", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {k: (float(getattr(self, k)) if k == "wall_s" else int(getattr(self, k)))
+                for k, _ in self._fields_ if k != "reserved"}
+
+
 GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch",
                "bw_replay_workspace_size", "bw_replay_launch", "bw_replay_status",
                "bw_replay_last_info", "bw_replay_timing_reset", "bw_replay_stage_times",
@@ -73,7 +89,8 @@ GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch",
                "bw_forest_create", "bw_forest_workspace_size", "bw_forest_bind", "bw_forest_launch",
                "bw_forest_capture", "bw_forest_graph_launch", "bw_forest_status", "bw_forest_info",
                "bw_forest_destroy", "bw_forest_autotune_workspace", "bw_forest_autotune",
-               "bw_forest_launch_timed"]
+               "bw_forest_launch_timed",
+               "bw_serve_create", "bw_serve_reset", "bw_serve_run", "bw_serve_info", "bw_serve_destroy"]
 
 _gpu = None
 
@@ -117,6 +134,12 @@ def gpu_lib(build_if_missing: bool = True):
         L.bw_forest_capture.argtypes = [P, P, P, P, P, P]
         L.bw_forest_graph_launch.argtypes = [P, P]
         L.bw_forest_launch_timed.argtypes = [P, P, P, P, P, P, C.POINTER(C.c_float)]
+        L.bw_serve_create.argtypes = [C.POINTER(BwServeConfig), C.POINTER(P)]
+        L.bw_serve_reset.argtypes = [P]
+        L.bw_serve_run.argtypes = [P, P, C.c_int64, P, C.c_int64, P, C.c_int32, C.c_double, P, P,
+                                   C.POINTER(BwServeStats)]
+        L.bw_serve_info.argtypes = [P, C.POINTER(BwServeStats)]
+        L.bw_serve_destroy.argtypes = [P]
         L.bw_forest_status.argtypes = [P, P, C.POINTER(C.c_int32)]
         L.bw_forest_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(BwForestTuning)]
         L.bw_forest_destroy.argtypes = [P]
@@ -359,6 +382,75 @@ def forest_replay(state_off, event_off, query_off, n_keys, parent, events, queri
         if st:
             raise ValueError(f"forest input rejected on the device: {STATUS_NAMES.get(st, st)}")
     return answers
+
+
+REQ_QUERY, REQ_COMMIT, REQ_FORK = 0, 1, 2
+
+
+class Server:
+    """Device-resident version store with a persistent request loop (bw_serve_* in
+    bw_gpu.h).  Built from an initial tree given as host numpy arrays (parent int32,
+    events EVENT_DTYPE grouped by state); requests are ``workloads.REQUEST_DTYPE``
+    records served with open-loop arrival times."""
+
+    def __init__(self, parent, n_keys: int, events, *, max_versions: int, max_events: int,
+                 hbm_cap_bytes: int, chain_limit: int = 0):
+        import numpy as np
+        _torch()
+        self.lib = gpu_lib()
+        par = np.ascontiguousarray(parent, dtype=np.int32)
+        ev = np.ascontiguousarray(events)
+        if ev.dtype != workloads.EVENT_DTYPE:
+            raise TypeError("events must be workloads.EVENT_DTYPE records")
+        cfg = BwServeConfig(int(par.size), par.ctypes.data, int(n_keys), int(ev.size),
+                            ev.ctypes.data if ev.size else None, int(max_versions), int(max_events),
+                            int(hbm_cap_bytes), int(chain_limit))
+        self.handle = C.c_void_p()
+        _check(self.lib.bw_serve_create(C.byref(cfg), C.byref(self.handle)), "bw_serve_create")
+        self.n_keys = int(n_keys)
+        self.n_states = int(par.size)
+
+    def info(self) -> dict:
+        st = BwServeStats()
+        _check(self.lib.bw_serve_info(self.handle, C.byref(st)), "bw_serve_info")
+        return st.as_dict()
+
+    def reset(self) -> None:
+        _check(self.lib.bw_serve_reset(self.handle), "bw_serve_reset")
+
+    def run(self, requests, commit_events=None, arrival_s=None, *, max_inflight: int = 1 << 16,
+            timeout_s: float = 300.0):
+        """Serve a request log; returns (answers int64[n], latency_us float32[n], stats dict)."""
+        import numpy as np
+        req = np.ascontiguousarray(requests)
+        if req.dtype != workloads.REQUEST_DTYPE:
+            raise TypeError("requests must be workloads.REQUEST_DTYPE records")
+        cev = np.ascontiguousarray(commit_events if commit_events is not None
+                                   else np.empty(0, dtype=workloads.EVENT_DTYPE))
+        arr = None if arrival_s is None else np.ascontiguousarray(arrival_s, dtype=np.float64)
+        if arr is not None and arr.size != req.size:
+            raise ValueError("one arrival time per request")
+        n = int(req.size)
+        answers = np.zeros(n, dtype=np.int64)
+        lat = np.zeros(n, dtype=np.float32)
+        st = BwServeStats()
+        _check(self.lib.bw_serve_run(self.handle, req.ctypes.data if n else None, n,
+                                     cev.ctypes.data if cev.size else None, int(cev.size),
+                                     arr.ctypes.data if arr is not None else None, int(max_inflight),
+                                     float(timeout_s), answers.ctypes.data if n else None,
+                                     lat.ctypes.data if n else None, C.byref(st)), "bw_serve_run")
+        return answers, lat, st.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.bw_serve_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def device_info():

@@ -21,6 +21,12 @@ configured workloads:
   the powers of two 1,024 ... 262,144, Poisson(8) events per state with Zipf s=1.1
   keys and delta = round(lognormal(7, 1)) with a negative sign at p=0.1, and
   1,000 range queries per tree (uniform states, uniform intervals).
+* ``serving`` (request log of the served store): 2,000,000 requests on the
+  trip-log tree -- 90% range-sum queries (version uniform among the versions that
+  exist, lo uniform, width geometric with mean 1,024, clipped to the domain), 8%
+  commits of 1-64 events (Zipf s=1.2 keys, delta = round(lognormal(7.3, 0.9))) to
+  a uniformly chosen live leaf, 2% forks of a uniformly chosen existing version --
+  with Poisson arrival times (unit rate; divide by the offered load).
 * ``csr_lut`` (sparse-key rank index): 10,000,000 distinct u64 keys over
   [0, 2^40), 20,000,000 (key, delta) events on them, 100,000,000 point and
   100,000,000 range lookups, half present keys and half absent.
@@ -39,6 +45,8 @@ import numpy as np
 
 EVENT_DTYPE = np.dtype([("state", "<u4"), ("key", "<u4"), ("delta", "<i8")])
 QUERY_DTYPE = np.dtype([("state", "<u4"), ("lo", "<u4"), ("hi", "<u4")])
+REQUEST_DTYPE = np.dtype([("kind", "<u4"), ("version", "<u4"), ("lo", "<u4"), ("hi", "<u4"),
+                          ("new_version", "<u4"), ("n_events", "<u4"), ("events_off", "<u8")])
 
 
 @dataclass
@@ -290,3 +298,118 @@ def csr_lut(seed: int = 0, scale: float = 1.0, lookups: int | None = None) -> Cs
     a, b = mixed(L), mixed(L)
     ranges = np.stack([np.minimum(a, b), np.maximum(a, b)], axis=1)
     return CsrWorkload("csr_lut", bits, int(K), keys, amounts, point, ranges)
+
+
+@dataclass
+class ServeLog:
+    """A request log on an initial tree: ``requests`` (REQUEST_DTYPE), the events of
+    its commits (``commit_events``, EVENT_DTYPE, state = the created version) and
+    unit-rate Poisson arrival times (``arrival``, seconds at 1 request/s)."""
+    name: str
+    base: Workload
+    requests: np.ndarray
+    commit_events: np.ndarray
+    arrival: np.ndarray
+
+    def describe(self) -> dict:
+        k = self.requests["kind"]
+        return {"workload": self.name, "initial_states": int(len(self.base.parent)),
+                "initial_events": int(len(self.base.events)), "key_domain": int(self.base.n_keys),
+                "requests": int(k.size), "queries": int((k == 0).sum()), "commits": int((k == 1).sum()),
+                "forks": int((k == 2).sum()), "commit_events": int(len(self.commit_events))}
+
+    def final_forest(self):
+        """(parent, events grouped by state, queries grouped by state, order) of the
+        tree after the whole log; order[i] is the request index of query row i."""
+        base = self.base
+        r = self.requests
+        created = r["kind"] != 0
+        S0 = len(base.parent)
+        par = np.concatenate([base.parent, r["version"][created].astype(np.int32)])
+        ev = np.concatenate([base.events, self.commit_events])
+        qi = np.nonzero(r["kind"] == 0)[0]
+        order = qi[np.argsort(r["version"][qi], kind="stable")]
+        qs = np.empty(order.size, dtype=QUERY_DTYPE)
+        qs["state"], qs["lo"], qs["hi"] = r["version"][order], r["lo"][order], r["hi"][order]
+        assert np.all(np.diff(ev["state"].astype(np.int64)) >= 0) and par.size >= S0
+        return par, ev, qs, order
+
+
+def serving(seed: int = 0, scale: float = 1.0, *, requests: int = 2_000_000, base: Workload | None = None,
+            p_query: float = 0.90, p_commit: float = 0.08, max_commit: int = 64,
+            mean_width: float = 1024.0) -> ServeLog:
+    """The serving request log on the trip-log tree (``scale`` shrinks the tree and
+    the number of requests together)."""
+    rng = np.random.default_rng(seed + 7)
+    if base is None:
+        base = trip_tree_base(seed, scale)
+    C = base.n_keys
+    n = max(1, int(round(requests * scale)))
+    u = rng.random(n)
+    kind = np.where(u < p_query, 0, np.where(u < p_query + p_commit, 1, 2)).astype(np.uint32)
+    req = np.zeros(n, dtype=REQUEST_DTYPE)
+    req["kind"] = kind
+    S0 = len(base.parent)
+    made = np.cumsum(kind != 0) - (kind != 0)          # versions created before request i
+    avail = S0 + made
+    q = kind == 0
+    req["version"][q] = (rng.random(int(q.sum())) * avail[q]).astype(np.uint32)
+    lo = rng.integers(0, C, size=int(q.sum()))
+    width = rng.geometric(1.0 / mean_width, size=int(q.sum()))
+    req["lo"][q], req["hi"][q] = lo, np.minimum(lo + width, C)
+    # live leaves: versions without children; commits extend one, forks branch anywhere
+    has_child = np.zeros(S0 + int((kind != 0).sum()), dtype=bool)
+    has_child[base.parent[1:]] = True
+    leaves = list(np.nonzero(~has_child[:S0])[0])
+    pos = {int(v): i for i, v in enumerate(leaves)}
+    nxt = S0
+    ce_states, ce_n = [], []
+    cw = np.cumsum(np.arange(1, C + 1, dtype=np.float64) ** -1.2)
+    cw /= cw[-1]
+    perm = rng.permutation(C).astype(np.uint32)
+    for i in np.nonzero(kind != 0)[0]:
+        if kind[i] == 1:
+            j = int(rng.integers(0, len(leaves)))
+            p = int(leaves[j])
+            leaves[j] = nxt                                  # the leaf is extended
+            pos.pop(p, None)
+            pos[nxt] = j
+            m = int(rng.integers(1, max_commit + 1))
+            req["n_events"][i] = m
+            req["events_off"][i] = sum(ce_n)
+            ce_states.append(nxt)
+            ce_n.append(m)
+        else:
+            p = int(rng.integers(0, nxt))
+            if p in pos:                                     # a forked leaf stops being a leaf
+                j = pos.pop(p)
+                last = leaves.pop()
+                if j < len(leaves):
+                    leaves[j] = last
+                    pos[int(last)] = j
+            pos[nxt] = len(leaves)
+            leaves.append(nxt)
+        req["version"][i] = p
+        req["new_version"][i] = nxt
+        nxt += 1
+    total = int(sum(ce_n))
+    cev = np.empty(total, dtype=EVENT_DTYPE)
+    cev["state"] = np.repeat(np.array(ce_states, dtype=np.uint32), ce_n) if total else []
+    ranks = np.minimum(np.searchsorted(cw, rng.random(total)), C - 1)
+    cev["key"] = perm[ranks]
+    cev["delta"] = np.rint(rng.lognormal(7.3, 0.9, size=total)).astype(np.int64)
+    arrival = np.cumsum(rng.exponential(1.0, size=n))
+    return ServeLog("serving", base, req, cev, arrival)
+
+
+def trip_tree_base(seed: int = 0, scale: float = 1.0) -> Workload:
+    """The trip-log tree's states and events without its query batch."""
+    rng = np.random.default_rng(seed)
+    S, C = max(2, int(300_000 * scale)), 65536
+    E = int(40_000_000 * scale)
+    parent = _fork_tree(rng, S, 0.9)
+    ev = np.empty(E, dtype=EVENT_DTYPE)
+    ev["state"] = _grouped_states(rng, E, S)
+    ev["key"] = _zipf_keys(rng, E, C, 1.2)
+    ev["delta"] = np.rint(rng.lognormal(7.3, 0.9, size=E)).astype(np.int64)
+    return Workload("trip_tree_base", parent, C, ev, np.empty(0, dtype=QUERY_DTYPE), False)

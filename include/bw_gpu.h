@@ -246,6 +246,73 @@ int bw_forest_autotune(const BwForestShape* shape, const int32_t* parent, const 
                        const BwQuery* queries, int64_t* answers, void* workspace, size_t workspace_bytes,
                        void* stream, int32_t reps, BwForestTuning* best, float* best_ms);
 
+/* ============================================================ served version store
+ * A device-resident version store answering range-sum queries and creating
+ * versions (commits of int64 delta events, forks) as requests arrive, from a
+ * persistent request loop (one request per warp) fed through host-mapped memory.
+ * It starts from an initial tree (the event-model inputs of bw_replay, on the
+ * host).  Every version keeps its own events as a key-sorted overlay; versions on
+ * a regular spacing keep a dense key-prefix row of their whole root path
+ * (checkpoints), the others read their nearest checkpoint ancestor's row plus the
+ * overlays of at most `spacing` member versions.  The spacing is the densest whose
+ * store fits hbm_cap_bytes.  No counterpart in the reference, which answers one
+ * offline batch per worker process (panel_gpu_session.cpp:110-137 runs repeated
+ * batches against one session). */
+enum { BW_REQ_QUERY = 0, BW_REQ_COMMIT = 1, BW_REQ_FORK = 2 };
+
+typedef struct {
+  uint32_t kind;         /* BW_REQ_* */
+  uint32_t version;      /* query: the version read; commit/fork: the parent version */
+  uint32_t lo, hi;       /* query: key interval [lo, hi) */
+  uint32_t new_version;  /* commit/fork: the next free version id (ids are created in log order) */
+  uint32_t n_events;     /* commit: events commit_events[events_off, events_off + n_events), <= 128 */
+  uint64_t events_off;
+} BwServeRequest;        /* 32 bytes */
+
+typedef struct {
+  int32_t n_states;          /* initial tree: states 0..n_states-1 */
+  const int32_t* parent;     /* host, n_states (parent[0] = -1, parent[v] < v) */
+  uint32_t n_keys;           /* key domain */
+  int64_t n_events;
+  const BwEvent* events;     /* host, grouped by state */
+  int32_t max_versions;      /* capacity: initial states + versions runs may create */
+  int64_t max_events;        /* event arena: initial events + events runs may commit */
+  size_t hbm_cap_bytes;      /* admission cap of the whole store */
+  int32_t chain_limit;       /* largest checkpoint spacing allowed (<= 32; 0 = 32) */
+} BwServeConfig;
+
+typedef struct {
+  int64_t requests, queries, commits, forks;
+  double wall_s;             /* first arrival to last completion */
+  int32_t checkpoints;       /* dense rows in the store */
+  int32_t spacing;           /* checkpoint spacing in versions */
+  size_t store_bytes;        /* device bytes of the store */
+  int32_t warps;             /* request-loop warps */
+  int32_t reserved;
+} BwServeStats;
+
+typedef struct BwServe BwServe;
+
+/* Build the store on the current device (allocates it; checkpoint rows are built
+ * level by level).  BW_EINVAL for malformed input or a store over the cap. */
+int bw_serve_create(const BwServeConfig* cfg, BwServe** out);
+/* Forget every version and event created by runs (back to the initial tree). */
+int bw_serve_reset(BwServe* s);
+/* Serve a request log: request i is published at t0 + arrival_s[i] (NULL: at
+ * once) while at most max_inflight requests are unfinished; the persistent loop
+ * executes requests concurrently (a request waits only for the versions it reads).
+ * answers[i] receives the range sum of query i (0 for commits and forks) and
+ * latency_us[i] its completion time minus its arrival time, both on the host
+ * clock.  The log is checked first (versions exist before they are read, new ids
+ * are consecutive, bounds and keys in range) and admitted only if its commit
+ * events fit the free event arena.  Blocks until every request completes or
+ * timeout_s elapses (BW_EINVAL). */
+int bw_serve_run(BwServe* s, const BwServeRequest* reqs, int64_t n, const BwEvent* commit_events,
+                 int64_t n_commit_events, const double* arrival_s, int32_t max_inflight, double timeout_s,
+                 int64_t* answers, float* latency_us, BwServeStats* stats);
+int bw_serve_info(const BwServe* s, BwServeStats* stats);
+int bw_serve_destroy(BwServe* s);
+
 /* ============================================================ sparse-key rank index */
 /* The CSR rank-LUT of the reference's sparse engine (CsrBase, sparse_engine.hpp:70-102;
  * build_csr_base, sparse_engine.hpp:287-360) over a sparse key universe
