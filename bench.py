@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2, help="steps of the sequential plain form")
     ap.add_argument("--full-check", action="store_true", help="check every answer against the oracle")
     ap.add_argument("--no-autotune", action="store_true", help="batched: use the default tuning")
+    ap.add_argument("--tuning", default=None, help="batched: JSON tuning to use instead of the autotuner")
     ap.add_argument("--no-serving", action="store_true", help="batched: skip the served-store runs")
     ap.add_argument("--loads", default="1e6,5e6,2e7", help="serving: offered loads in requests/s")
     ap.add_argument("--hbm-cap-gb", type=float, default=120.0, help="serving: admission cap of the store")
@@ -342,7 +343,9 @@ def bench_batched(args):
 
     with torch.cuda.stream(stream):
         t_tune = time.perf_counter()
-        if args.no_autotune:
+        if args.tuning:
+            tuning, tune_ms = json.loads(args.tuning), None
+        elif args.no_autotune:
             tuning, tune_ms = None, None
         else:
             tuning, tune_ms = bw.forest_autotune(*shape, d_parent, d_events, d_queries, d_answers, reps=2,

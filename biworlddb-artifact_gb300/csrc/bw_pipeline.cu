@@ -782,11 +782,12 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
   int64_t* qpre = reinterpret_cast<int64_t*>(smem + L.off_qpre);   // queries before step, per ring slot
   BwEvent* evbuf = reinterpret_cast<BwEvent*>(smem + L.off_ev);     // [2][Cfg::kTileEv]
   uint8_t* emeta = smem + L.off_emeta;                               // [2][Cfg::kTileEv] step << 1 | exit
+  uint8_t* qmeta = smem + L.off_qmeta;                               // [2][Cfg::kTileQ] step
   unsigned char* qbuf = smem + L.off_q;                              // [2][Cfg::kTileQ] x 12 B
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // flattened queries g = qslot + 256 m belong to this thread: consecutive queries
   // go to different warps, so a tile's few queries are probed by different warps
-  const int qslot = lane * kSweepWarps + warp;
+  const int qslot = lane * Cfg::kWarps + warp;
   unsigned long long* Pw = reinterpret_cast<unsigned long long*>(smem + L.off_P) + (size_t)warp * (kMaxChunks + 1);
   constexpr int32_t M = Cfg::kRing - 1;
 
@@ -812,94 +813,134 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     const uint32_t nch = (s.n + kChunk - 1) / kChunk;
     const bool first = si == first_si;
     const bool carried = first && crow != nullptr;
-    for (int i = tid; i < nwd; i += kSweepThreads) {
+    for (int i = tid; i < nwd; i += Cfg::kThreads) {
       sbits[i] = gbits[s.word_lo + i];
       srl[i] = grl[s.word_lo + i] - s.rank_lo;
     }
-    for (uint32_t i = tid; i < nch * kChunkStride; i += kSweepThreads) fine[i] = 0;
-    for (uint32_t i = tid; i < nch; i += kSweepThreads) T[i] = 0;
+    for (uint32_t i = tid; i < nch * kChunkStride; i += Cfg::kThreads) fine[i] = 0;
+    for (uint32_t i = tid; i < nch; i += Cfg::kThreads) T[i] = 0;
 
     // Step ring: descriptors and event/query prefixes of steps [filled - Cfg::kRing, filled);
-    // steps past t1 read as empty.  A refill overwrites the oldest Cfg::kRingFill slots.
+    // steps past t1 read as empty.  A refill overwrites the oldest Cfg::kRingFill slots;
+    // warp 0 loads them and scans their counts (the running totals live in warp 0).
     int32_t filled = t0;
     int64_t run_e = 0, run_q = 0;
     auto fill = [&]() {
       __syncthreads();
-      const int32_t t = filled + tid;
-      StepDesc d;
-      d.e0 = 0; d.q0 = 0; d.ne = 0; d.nq = 0;
-      if (tid < Cfg::kRingFill && t < t1) d = p.desc[t];
-      const int64_t ce = tid < Cfg::kRingFill ? (int64_t)d.ne : 0, cq = tid < Cfg::kRingFill && d.nq > 0 ? (int64_t)d.nq : 0;
-      int64_t te = 0, tq = 0;
-      const int64_t xe = block_exclusive_scan<int64_t>(ce, &te);
-      const int64_t xq = block_exclusive_scan<int64_t>(cq, &tq);
-      if (tid < Cfg::kRingFill) {
-        const int32_t sl = t & M;
-        ring[sl] = d;
-        epre[sl] = run_e + xe;
-        qpre[sl] = run_q + xq;
+      if (warp == 0) {
+        constexpr int PER = Cfg::kRingFill / 32;
+        StepDesc d[PER];
+        int64_t le = 0, lq = 0;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+          const int32_t t = filled + lane * PER + j;
+          d[j].e0 = 0; d[j].q0 = 0; d[j].ne = 0; d[j].nq = 0;
+          if (t < t1) d[j] = p.desc[t];
+          le += d[j].ne;
+          lq += d[j].nq > 0 ? d[j].nq : 0;
+        }
+        int64_t ie = le, iq = lq;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int64_t ye = __shfl_up_sync(0xffffffffu, ie, o), yq = __shfl_up_sync(0xffffffffu, iq, o);
+          if (lane >= o) { ie += ye; iq += yq; }
+        }
+        int64_t xe = run_e + ie - le, xq = run_q + iq - lq;
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+          const int32_t sl = (filled + lane * PER + j) & M;
+          ring[sl] = d[j];
+          epre[sl] = xe;
+          qpre[sl] = xq;
+          xe += d[j].ne;
+          xq += d[j].nq > 0 ? d[j].nq : 0;
+        }
+        run_e += __shfl_sync(0xffffffffu, ie, 31);
+        run_q += __shfl_sync(0xffffffffu, iq, 31);
       }
-      run_e += te;
-      run_q += tq;
       filled += Cfg::kRingFill;
       __syncthreads();
     };
-    // Tile from step s: as many whole steps (<= Cfg::kTileSteps) as fit Cfg::kTileEv events and
-    // Cfg::kTileQ queries, at least one.  Every thread computes the same tile.
+    // Tile from step s: as many whole steps (<= kTileSteps) as fit kTileEv events and
+    // kTileQ queries, at least one.  The fit is monotone in the end step, so each
+    // warp counts it with two ballots; every warp computes the same tile.
     auto make_tile = [&](int32_t st) -> Tile {
       const int32_t emax = min(st + Cfg::kTileSteps, t1);
       const int64_t le = epre[st & M] + Cfg::kTileEv, lq = qpre[st & M] + Cfg::kTileQ;
-      int32_t lo = st + 1, hi = emax;
-      while (lo < hi) {
-        const int32_t mid = (lo + hi + 1) >> 1;
-        if (epre[mid & M] <= le && qpre[mid & M] <= lq) lo = mid; else hi = mid - 1;
-      }
+      const int32_t ea = st + 1 + lane, eb2 = st + 33 + lane;
+      const bool oka = ea <= emax && epre[ea & M] <= le && qpre[ea & M] <= lq;
+      const bool okb = eb2 <= emax && epre[eb2 & M] <= le && qpre[eb2 & M] <= lq;
+      int32_t e = st + __popc(__ballot_sync(0xffffffffu, oka)) + __popc(__ballot_sync(0xffffffffu, okb));
+      if (e == st) e = st + 1;
       Tile x;
       x.s = st;
-      x.e = lo;
+      x.e = e;
       const bool qa = st + lane < x.e && ring[(st + lane) & M].nq > 0;
       const bool qb = st + 32 + lane < x.e && ring[(st + 32 + lane) & M].nq > 0;
       x.qmask = (uint64_t)__ballot_sync(0xffffffffu, qa) | ((uint64_t)__ballot_sync(0xffffffffu, qb) << 32);
       return x;
     };
-    // Stage this thread's events (flattened index tid + 256 m) and queries of the tile
-    // with cp.async; own_e = (step - s) << 1 | exit, own_q = step - s, -1 when none.
-    auto stage = [&](const Tile& x, int buf, int32_t* own_e, int32_t* own_q) {
-      const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
-      const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
-#pragma unroll
-      for (int m = 0; m < Cfg::kEvPer; ++m) {
-        const int64_t g = tid + m * kSweepThreads;
-        own_e[m] = -1;
-        if (g < ne) {
-          int32_t lo = x.s, hi = x.e - 1;
-          while (lo < hi) {
-            const int32_t mid = (lo + hi + 1) >> 1;
-            if (epre[mid & M] - pe0 <= g) lo = mid; else hi = mid - 1;
-          }
-          const StepDesc d = ring[lo & M];
-          cp_async16(evbuf + (size_t)buf * Cfg::kTileEv + g, p.ev + (int64_t)d.e0 + (pe0 + g - epre[lo & M]));
-          own_e[m] = ((lo - x.s) << 1) | (d.nq < 0 ? 1 : 0);
-          emeta[(size_t)buf * Cfg::kTileEv + g] = (uint8_t)own_e[m];
+    // Stage a tile cooperatively: warps 0-3 copy (cp.async) the events and warps
+    // 4-7 the queries of 32-step groups, lane l decoding step l of the group and
+    // lanes taking consecutive flattened items (the source step found by a shuffle
+    // search over the group's counts); each item's step (and exit flag) is written
+    // beside it.  A barrier after the copies land makes the tile visible.
+    auto stage = [&](const Tile& x, int buf) {
+      const bool evw = warp < Cfg::kWarps / 2;
+      const int wgrp = evw ? warp : warp - Cfg::kWarps / 2;
+      const int64_t p0 = evw ? epre[x.s & M] : qpre[x.s & M];
+      const int64_t cap = evw ? Cfg::kTileEv : Cfg::kTileQ;
+      BwEvent* eb = evbuf + (size_t)buf * Cfg::kTileEv;
+      uint8_t* em = emeta + (size_t)buf * Cfg::kTileEv;
+      unsigned char* qb = qbuf + (size_t)buf * Cfg::kTileQ * 12;
+      uint8_t* qm = qmeta + (size_t)buf * Cfg::kTileQ;
+      for (int32_t c = x.s + 32 * wgrp; c < x.e; c += 32 * (Cfg::kWarps / 2)) {
+        const int32_t st = c + lane;
+        int32_t cnt = 0;
+        uint32_t src0 = 0;
+        int32_t fpos = 0;
+        uint32_t meta = 0;
+        if (st < x.e) {
+          const StepDesc d = ring[st & M];
+          const int64_t f = (evw ? epre[st & M] : qpre[st & M]) - p0;
+          const int64_t n = evw ? d.ne : (d.nq > 0 ? d.nq : 0);
+          cnt = (int32_t)imin64(n, cap - f > 0 ? cap - f : 0);
+          src0 = evw ? d.e0 : d.q0;
+          fpos = (int32_t)f;
+          meta = evw ? (uint32_t)(((st - x.s) << 1) | (d.nq < 0 ? 1 : 0)) : (uint32_t)(st - x.s);
         }
-      }
+        int32_t incl = cnt;
 #pragma unroll
-      for (int m = 0; m < Cfg::kQPer; ++m) {
-        const int64_t g = qslot + m * kSweepThreads;
-        own_q[m] = -1;
-        if (g < nq) {
-          int32_t lo = x.s, hi = x.e - 1;
-          while (lo < hi) {
-            const int32_t mid = (lo + hi + 1) >> 1;
-            if (qpre[mid & M] - pq0 <= g) lo = mid; else hi = mid - 1;
+        for (int o = 1; o < 32; o <<= 1) {
+          const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        for (int32_t g0 = 0; g0 < total; g0 += 32) {
+          const int32_t g = g0 + lane;
+          int32_t lo = 0, hi = 31;   // first lane whose inclusive count exceeds g
+#pragma unroll
+          for (int it = 0; it < 5; ++it) {
+            const int32_t mid = (lo + hi) >> 1;
+            if (__shfl_sync(0xffffffffu, incl, mid) > g) hi = mid; else lo = mid + 1;
           }
-          const StepDesc d = ring[lo & M];
-          const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + (int64_t)d.q0 + (pq0 + g - qpre[lo & M]));
-          unsigned char* dq = qbuf + ((size_t)buf * Cfg::kTileQ + g) * 12;
-          cp_async4(dq, src);
-          cp_async4(dq + 4, src + 1);
-          cp_async4(dq + 8, src + 2);
-          own_q[m] = lo - x.s;
+          const int32_t s_incl = __shfl_sync(0xffffffffu, incl, lo), s_cnt = __shfl_sync(0xffffffffu, cnt, lo);
+          const uint32_t s_src = __shfl_sync(0xffffffffu, src0, lo), s_meta = __shfl_sync(0xffffffffu, meta, lo);
+          const int32_t s_pos = __shfl_sync(0xffffffffu, fpos, lo);
+          if (g < total) {
+            const int32_t off = g - (s_incl - s_cnt);
+            if (evw) {
+              cp_async16(eb + s_pos + off, p.ev + (int64_t)s_src + off);
+              em[s_pos + off] = (uint8_t)s_meta;
+            } else {
+              const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + (int64_t)s_src + off);
+              unsigned char* dq = qb + (size_t)(s_pos + off) * 12;
+              cp_async4(dq, src);
+              cp_async4(dq + 4, src + 1);
+              cp_async4(dq + 8, src + 2);
+              qm[s_pos + off] = (uint8_t)s_meta;
+            }
+          }
         }
       }
       cp_async_commit();
@@ -949,25 +990,29 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       acc -= slice_prefix2(fine, Pw, s.n, sbits, srl, klo, khi, lo);
       *out = first ? (int64_t)acc : (int64_t)((uint64_t)*out + acc);
     };
-    // Replay a staged tile.  Segment mode: segments of steps ending at each query
-    // step; the updates of a segment, a barrier, the probes of its query step, a
-    // barrier.  Offline mode (few queries x events): one barrier, every query of
-    // the tile probed against the state at the tile start plus the staged events of
-    // its own and earlier steps of the tile (summed by the owner's warp), a barrier,
-    // then all of the tile's updates.  Updates after the last probe of a tile run
-    // without a barrier.
-    auto process = [&](const Tile& x, int buf, const int32_t* own_e, const int32_t* own_q) {
+    // Replay a staged, visible tile.  Thread t applies flattened events t + 256 m;
+    // the tile's queries g = qslot + 256 m belong to this thread.  Segment mode:
+    // segments of steps ending at each query step; the updates of a segment, a
+    // barrier, the probes of its query step, a barrier.  Offline mode (few queries x
+    // events): every query of the tile probed against the state at the tile start
+    // plus the tile's events of its own and earlier steps (summed by the owner's
+    // warp), a barrier, then all of the tile's updates.  Updates after the last probe
+    // of a tile run without a barrier.
+    auto process = [&](const Tile& x, int buf) {
       const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
       const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
+      const int64_t ns_e = imin64(ne, Cfg::kTileEv), ns_q = imin64(nq, Cfg::kTileQ);
       const BwEvent* eb = evbuf + (size_t)buf * Cfg::kTileEv;
       const uint8_t* em = emeta + (size_t)buf * Cfg::kTileEv;
       const unsigned char* qb = qbuf + (size_t)buf * Cfg::kTileQ * 12;
+      const uint8_t* qmt = qmeta + (size_t)buf * Cfg::kTileQ;
       uint64_t c_lo[Cfg::kQPer], c_hi[Cfg::kQPer];
 #pragma unroll
       for (int m = 0; m < Cfg::kQPer; ++m) {
         c_lo[m] = c_hi[m] = 0;
-        if (carried && own_q[m] >= 0) {
-          const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(qslot + m * kSweepThreads) * 12);
+        const int64_t g = qslot + m * Cfg::kThreads;
+        if (carried && g < ns_q) {
+          const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
           if (q[2] > q[1]) {
             c_lo[m] = (uint64_t)__ldg(crow + q[1]);
             c_hi[m] = (uint64_t)__ldg(crow + q[2]);
@@ -980,54 +1025,54 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         return (int64_t)ring[u & M].q0 + (pq0 + g - qpre[u & M]);
       };
       if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= Cfg::kTileQ && nq * ne <= kOfflinePairs) {
-        __syncthreads();   // earlier updates applied; this tile's staged events visible
         if (dirty) {
           rebuild();
           dirty = false;
         }
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
-          const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(qslot + m * kSweepThreads) * 12);
-          const bool mine = own_q[m] >= 0;
+          const int64_t g = qslot + m * Cfg::kThreads;
+          const bool mine = g < nq;
+          const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(mine ? g : 0) * 12);
           const uint32_t my_lo = mine ? q[1] : 0u, my_hi = mine ? q[2] : 0u;
+          const int32_t my_u = mine ? (int32_t)qmt[g] : 0;
           uint32_t owners = __ballot_sync(0xffffffffu, mine);
           while (owners) {
             const int src = __ffs(owners) - 1;
             owners &= owners - 1;
             const uint32_t lo = __shfl_sync(0xffffffffu, my_lo, src), hi = __shfl_sync(0xffffffffu, my_hi, src);
-            const int32_t urel = __shfl_sync(0xffffffffu, own_q[m], src);
+            const int32_t urel = __shfl_sync(0xffffffffu, my_u, src);
             const uint32_t a_lo = lo > klo ? lo : klo, a_hi = hi < khi ? hi : khi;
             uint64_t corr = 0;
             if (s.n && a_lo < a_hi) {
+#pragma unroll 4
               for (int64_t i = lane; i < ne; i += 32) {
                 const uint8_t mt = em[i];
-                if ((int32_t)(mt >> 1) <= urel) {
-                  const BwEvent e = eb[i];
-                  if (e.key >= a_lo && e.key < a_hi)
-                    corr += (mt & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
-                }
+                const BwEvent e = eb[i];
+                if ((int32_t)(mt >> 1) <= urel && e.key >= a_lo && e.key < a_hi)
+                  corr += (mt & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
               }
             }
 #pragma unroll
             for (int o = 16; o; o >>= 1) corr += __shfl_xor_sync(0xffffffffu, corr, o);
-            if (lane == src)
-              finish(lo, hi, corr + (c_hi[m] - c_lo[m]), qindex(urel, qslot + m * kSweepThreads));
+            if (lane == src) finish(lo, hi, corr + (c_hi[m] - c_lo[m]), qindex(urel, g));
           }
         }
         __syncthreads();   // probes done before this tile's updates
         if (s.n) {
 #pragma unroll
           for (int m = 0; m < Cfg::kEvPer; ++m) {
-            if (own_e[m] >= 0) {
-              const BwEvent e = eb[tid + m * kSweepThreads];
-              apply(e.key, (uint64_t)e.delta, own_e[m] & 1);
+            const int64_t g = tid + m * Cfg::kThreads;
+            if (g < ne) {
+              const BwEvent e = eb[g];
+              apply(e.key, (uint64_t)e.delta, em[g] & 1);
             }
           }
         }
         if (ne > 0) dirty = true;
         return;
       }
-      uint32_t done = 0;         // own staged events applied so far
+      uint32_t done = 0;         // staged slots tid + 256 m applied so far
       int32_t a = x.s;           // first step of the current segment
       uint64_t qm = x.qmask;
       for (;;) {
@@ -1037,15 +1082,19 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         if (s.n) {
 #pragma unroll
           for (int m = 0; m < Cfg::kEvPer; ++m) {
-            if (!(done >> m & 1u) && own_e[m] >= 0 && (own_e[m] >> 1) <= urel) {
-              const BwEvent e = eb[tid + m * kSweepThreads];
-              apply(e.key, (uint64_t)e.delta, own_e[m] & 1);
-              done |= 1u << m;
+            const int64_t g = tid + m * Cfg::kThreads;
+            if (!(done >> m & 1u) && g < ns_e) {
+              const uint8_t mt = em[g];
+              if ((int32_t)(mt >> 1) <= urel) {
+                const BwEvent e = eb[g];
+                apply(e.key, (uint64_t)e.delta, mt & 1);
+                done |= 1u << m;
+              }
             }
           }
           if (ne > Cfg::kTileEv && a == x.s) {  // one step with more events than a tile stages
             const StepDesc d = ring[x.s & M];
-            for (int64_t g = Cfg::kTileEv + tid; g < ne; g += kSweepThreads) {
+            for (int64_t g = Cfg::kTileEv + tid; g < ne; g += Cfg::kThreads) {
               const BwEvent e = p.ev[(int64_t)d.e0 + g];
               apply(e.key, (uint64_t)e.delta, d.nq < 0);
             }
@@ -1060,14 +1109,15 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         }
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
-          if (own_q[m] == urel) {
-            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(qslot + m * kSweepThreads) * 12);
-            finish(q[1], q[2], c_hi[m] - c_lo[m], qindex(urel, qslot + m * kSweepThreads));
+          const int64_t g = qslot + m * Cfg::kThreads;
+          if (g < ns_q && (int32_t)qmt[g] == urel) {
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
+            finish(q[1], q[2], c_hi[m] - c_lo[m], qindex(urel, g));
           }
         }
         if (nq > Cfg::kTileQ) {  // one step with more queries than a tile stages
           const int64_t qbase = qindex(urel, 0);
-          for (int64_t g = Cfg::kTileQ + tid; g < nq; g += kSweepThreads) {
+          for (int64_t g = Cfg::kTileQ + tid; g < nq; g += Cfg::kThreads) {
             const BwQuery qq = p.qs[qbase + g];
             uint64_t acc = 0;
             if (carried && qq.hi > qq.lo) acc = (uint64_t)__ldg(crow + qq.hi) - (uint64_t)__ldg(crow + qq.lo);
@@ -1082,30 +1132,23 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
 
     fill();
     Tile cur = make_tile(t0);
-    int32_t cur_e[Cfg::kEvPer], cur_q[Cfg::kQPer];
-    stage(cur, 0, cur_e, cur_q);
+    stage(cur, 0);
     int buf = 0;
     for (;;) {
+      cp_async_wait<0>();
+      __syncthreads();   // the current tile is staged and visible; the other buffer is free
       const int32_t ns = cur.e;
       Tile nxt;
-      int32_t nxt_e[Cfg::kEvPer], nxt_q[Cfg::kQPer];
+      nxt.s = nxt.e = t1;
+      nxt.qmask = 0;
       if (ns < t1) {
         if (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
         nxt = make_tile(ns);
-        stage(nxt, buf ^ 1, nxt_e, nxt_q);
-      } else {
-        nxt.s = nxt.e = t1;
-        nxt.qmask = 0;
-        cp_async_commit();
+        stage(nxt, buf ^ 1);
       }
-      cp_async_wait<1>();   // this thread's copies of the current tile have landed
-      process(cur, buf, cur_e, cur_q);
+      process(cur, buf);
       if (ns >= t1) break;
       cur = nxt;
-#pragma unroll
-      for (int m = 0; m < Cfg::kEvPer; ++m) cur_e[m] = nxt_e[m];
-#pragma unroll
-      for (int m = 0; m < Cfg::kQPer; ++m) cur_q[m] = nxt_q[m];
       buf ^= 1;
     }
     cp_async_wait<0>();
@@ -1114,7 +1157,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
 }
 
 template <typename Cfg>
-__global__ void __launch_bounds__(kSweepThreads, 2) k_sweep(SweepParams p, SweepLayout L) {
+__global__ void __launch_bounds__(Cfg::kThreads, Cfg::kMinBlocks) k_sweep(SweepParams p, SweepLayout L) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int32_t s_ticket;
   if (*p.status) return;  // never index with descriptors of rejected input
@@ -1136,10 +1179,17 @@ static inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 static size_t sweep_budget(int ctas_per_sm) { return (size_t)(kSmemPerSM / ctas_per_sm) - 3072; }
 
 static void finish_spec(PipeSpec& s, const Tuning& tune) {
-  s.tile = tune.tile == kTileNarrowId || tune.tile == kTileWideId ? tune.tile
+  s.tile = tune.tile >= kTileNarrowId && tune.tile <= kTileWide512Id ? tune.tile
            : (s.Q * 8 >= s.E ? kTileNarrowId : kTileWideId);
-  s.SL = s.tile == kTileWideId ? sweep_layout<TileWide>(words_of(s.Cmax), sweep_budget(s.ctas_per_sm))
-                               : sweep_layout<TileNarrow>(words_of(s.Cmax), sweep_budget(s.ctas_per_sm));
+  if (s.tile >= kTileNarrow512Id) s.ctas_per_sm = 1;   // a 512-thread CTA takes the SM's registers
+  const int32_t nw = words_of(s.Cmax);
+  const size_t bud = sweep_budget(s.ctas_per_sm);
+  switch (s.tile) {
+    case kTileWideId: s.SL = sweep_layout<TileWide>(nw, bud); break;
+    case kTileNarrow512Id: s.SL = sweep_layout<TileNarrow512>(nw, bud); break;
+    case kTileWide512Id: s.SL = sweep_layout<TileWide512>(nw, bud); break;
+    default: s.SL = sweep_layout<TileNarrow>(nw, bud); break;
+  }
   if (tune.slice_ranks > 0) {
     const uint32_t cap = (uint32_t)tune.slice_ranks;
     if (s.SL.cap32 > cap) s.SL.cap32 = cap;
@@ -1269,8 +1319,9 @@ void pipe_layout(const PipeSpec& s, Layout& L) {
   take(W_TCARRY, T * 8);
   take(W_TGSUM, T * 8);
   take(W_LASTQ, T * 4);
-  take(W_UNITS, s.T > 1 ? (size_t)s.n_units * sizeof(CarryUnit) : 0);
-  take(W_ORDER, s.T > 1 ? B * 4 : 0);
+  const bool forest = !s.h_soff.empty();   // tables uploaded by pipe_bind (else written per launch)
+  take(W_UNITS, forest ? (size_t)s.n_units * sizeof(CarryUnit) : 0);
+  take(W_ORDER, forest ? B * 4 : 0);
   take(W_MISC, 64);
   take(W_EOFF, (S + 1) * 8);
   take(W_QOFF, (S + 1) * 8);
@@ -1337,13 +1388,19 @@ static int ensure_attrs() {
   if ((rc = report(cudaFuncSetAttribute(k_sweep<TileWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         kSmemLimit - 1024), "smem attr")))
     return rc;
+  if ((rc = report(cudaFuncSetAttribute(k_sweep<TileNarrow512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kSmemLimit - 1024), "smem attr")))
+    return rc;
+  if ((rc = report(cudaFuncSetAttribute(k_sweep<TileWide512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kSmemLimit - 1024), "smem attr")))
+    return rc;
   if (dev >= 0 && dev < 64) done[dev] = true;
   return 0;
 }
 
 int pipe_bind(const PipeSpec& s, void* workspace, cudaStream_t st) {
   int rc = ensure_attrs();
-  if (rc || s.T == 1) return rc;
+  if (rc || s.h_soff.empty()) return rc;
   Layout L;
   pipe_layout(s, L);
   char* ws = static_cast<char*>(workspace);
@@ -1394,8 +1451,9 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
   int64_t* scan_tmp = reinterpret_cast<int64_t*>(at(W_SCAN));
   BlockTab* blocks = reinterpret_cast<BlockTab*>(at(W_BLOCKS));
   int32_t* bmode = reinterpret_cast<int32_t*>(at(W_BMODE));
-  const CarryUnit* units = s.T > 1 ? reinterpret_cast<const CarryUnit*>(at(W_UNITS)) : nullptr;
-  const int32_t* order = s.T > 1 ? reinterpret_cast<const int32_t*>(at(W_ORDER)) : nullptr;
+  const bool forest = !s.h_soff.empty();
+  const CarryUnit* units = forest ? reinterpret_cast<const CarryUnit*>(at(W_UNITS)) : nullptr;
+  const int32_t* order = forest ? reinterpret_cast<const int32_t*>(at(W_ORDER)) : nullptr;
 
   const int32_t S = s.S, T = s.T, B = s.B;
   const int grid = s.sms * 8;
@@ -1405,7 +1463,7 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
   if ((rc = mark(0))) return rc;
 
   // ---- 0/1. init + ingest
-  k_init<<<(std::max(T, 16) + 255) / 256, 256, 0, st>>>(misc, tt, T, T == 1, S, s.E, s.Q, s.Cmax, s.nb1);
+  k_init<<<(std::max(T, 16) + 255) / 256, 256, 0, st>>>(misc, tt, T, forest ? 0 : 1, S, s.E, s.Q, s.Cmax, s.nb1);
   if ((rc = chk("k_init"))) return rc;
   if (s.E > 0) {
     k_offsets<true><<<grid, 256, 0, st>>>(events, s.E, tt, T, S, eoff, status);
@@ -1490,8 +1548,14 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
     sp.bits = pp.bits; sp.rlut = pp.rlut; sp.slices = pp.slices; sp.nslices = pp.nslices; sp.carry = pp.carry;
     sp.answers = answers; sp.status = status; sp.bmode = bmode; sp.ticket = misc + M_SWEEP_TICKET;
     const int sgrid = std::min(B, s.ctas_per_sm * s.sms);
-    if (s.tile == kTileWideId) k_sweep<TileWide><<<sgrid, kSweepThreads, SL.bytes, st>>>(sp, SL);
-    else k_sweep<TileNarrow><<<sgrid, kSweepThreads, SL.bytes, st>>>(sp, SL);
+    switch (s.tile) {
+      case kTileWideId: k_sweep<TileWide><<<sgrid, TileWide::kThreads, SL.bytes, st>>>(sp, SL); break;
+      case kTileNarrow512Id:
+        k_sweep<TileNarrow512><<<sgrid, TileNarrow512::kThreads, SL.bytes, st>>>(sp, SL);
+        break;
+      case kTileWide512Id: k_sweep<TileWide512><<<sgrid, TileWide512::kThreads, SL.bytes, st>>>(sp, SL); break;
+      default: k_sweep<TileNarrow><<<sgrid, TileNarrow::kThreads, SL.bytes, st>>>(sp, SL); break;
+    }
     if ((rc = chk("k_sweep"))) return rc;
   }
   if ((rc = mark(6))) return rc;

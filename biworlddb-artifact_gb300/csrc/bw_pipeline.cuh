@@ -48,18 +48,21 @@ constexpr int kMaxChunks = 128;
 constexpr int kRebuildPer = 5;
 constexpr int64_t kOfflinePairs = 32768;      // tile (queries x events) below which probes are batched
 
-// Sweep tile geometry: EV events and QP queries staged per thread per tile, at most
-// STEPS steps per tile, a ring of RING step descriptors refilled RING/2 at a time.
-// The ring must hold two tiles plus a refill: RING >= 4 * STEPS.
-template <int EV, int QP, int STEPS, int RING>
+// Sweep tile geometry: THREADS per CTA, EV events and QP queries staged per thread
+// per tile, at most STEPS steps per tile, a ring of RING step descriptors refilled
+// RING/2 at a time.  The ring must hold two tiles plus a refill: RING >= 4 * STEPS.
+template <int EV, int QP, int STEPS, int RING, int THREADS>
 struct TileCfg {
   static constexpr int kEvPer = EV, kQPer = QP, kTileSteps = STEPS, kRing = RING, kRingFill = RING / 2;
-  static constexpr int kTileEv = EV * kSweepThreads, kTileQ = QP * kSweepThreads;
-  static_assert(RING >= 4 * STEPS && STEPS <= 64, "tile ring too small");
+  static constexpr int kThreads = THREADS, kWarps = THREADS / 32, kMinBlocks = THREADS >= 512 ? 1 : 2;
+  static constexpr int kTileEv = EV * THREADS, kTileQ = QP * THREADS;
+  static_assert(RING >= 4 * STEPS && STEPS <= 64 && kRingFill % 32 == 0, "tile ring too small");
 };
-using TileNarrow = TileCfg<2, 2, 32, 128>;   // query-heavy steps: small staging, more Fenwick
-using TileWide = TileCfg<4, 1, 64, 256>;     // event-heavy steps: deep event staging
-enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2 };
+using TileNarrow = TileCfg<2, 2, 32, 128, 256>;      // query-heavy steps: small staging, more Fenwick
+using TileWide = TileCfg<4, 1, 64, 256, 256>;        // event-heavy steps: deep event staging
+using TileNarrow512 = TileCfg<1, 1, 32, 128, 512>;   // the same with 16 warps (one CTA per SM)
+using TileWide512 = TileCfg<2, 1, 64, 256, 512>;
+enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4 };
 
 // ------------------------------------------------------------------ records
 struct StepDesc {        // one Euler step, 16 bytes
@@ -107,7 +110,7 @@ struct SweepLayout {
   int32_t ww;
   int32_t nch32, nch64;
   uint32_t cap32, cap64;
-  size_t off_rl, off_fine, off_T, off_P, off_ring, off_epre, off_qpre, off_ev, off_emeta, off_q, bytes;
+  size_t off_rl, off_fine, off_T, off_P, off_ring, off_epre, off_qpre, off_ev, off_emeta, off_q, off_qmeta, bytes;
 };
 template <typename Cfg>
 __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budget) {
@@ -116,9 +119,9 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const size_t staging = sizeof(StepDesc) * Cfg::kRing + 2 * 8 * (size_t)Cfg::kRing +
                          2 * (size_t)Cfg::kTileEv * 16 + al(2 * (size_t)Cfg::kTileEv) +
-                         al(2 * (size_t)Cfg::kTileQ * 12);
+                         al(2 * (size_t)Cfg::kTileQ * 12) + al(2 * (size_t)Cfg::kTileQ);
   const size_t fixed = al((size_t)L.ww * 8) + al(((size_t)L.ww + 2) * 4) + staging +
-                       (size_t)kSweepWarps * (kMaxChunks + 1) * 8 + 128;
+                       (size_t)Cfg::kWarps * (kMaxChunks + 1) * 8 + 128;
   const size_t per32 = (size_t)kChunkStride * 4 + 8;  // int32 nodes + chunk total
   int32_t n32 = budget > fixed ? (int32_t)((budget - fixed) / per32) : 0;
   if (n32 > kMaxChunks) n32 = kMaxChunks;
@@ -130,13 +133,14 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   L.off_rl = o;   o = al(o + ((size_t)L.ww + 2) * 4);
   L.off_fine = o; o = al(o + (size_t)n32 * kChunkStride * 4);
   L.off_T = o;    o = al(o + (size_t)n32 * 8);
-  L.off_P = o;    o = al(o + (size_t)kSweepWarps * (kMaxChunks + 1) * 8);
+  L.off_P = o;    o = al(o + (size_t)Cfg::kWarps * (kMaxChunks + 1) * 8);
   L.off_ring = o; o = al(o + sizeof(StepDesc) * Cfg::kRing);
   L.off_epre = o; o = al(o + 8 * (size_t)Cfg::kRing);
   L.off_qpre = o; o = al(o + 8 * (size_t)Cfg::kRing);
   L.off_ev = o;   o = al(o + 2 * (size_t)Cfg::kTileEv * 16);
   L.off_emeta = o; o = al(o + 2 * (size_t)Cfg::kTileEv);
   L.off_q = o;    o = al(o + 2 * (size_t)Cfg::kTileQ * 12);
+  L.off_qmeta = o; o = al(o + 2 * (size_t)Cfg::kTileQ);
   L.bytes = o;
   return L;
 }
@@ -171,7 +175,7 @@ struct PipeSpec {
   bool chain_hint = false;
   // one-tree scalars (T == 1): tables are written by a kernel at each launch
   int32_t nb1 = 1;
-  // forest host tables, uploaded once by bind (empty for T == 1)
+  // forest host tables, uploaded once by bind (empty for the plain one-tree spec)
   std::vector<int32_t> h_soff, h_boff;
   std::vector<int64_t> h_eoff, h_qoff, h_bits, h_carry, h_gsum;
   std::vector<uint32_t> h_C;

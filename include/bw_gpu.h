@@ -202,9 +202,10 @@ typedef struct {
   int32_t ctas_per_sm;  /* persistent sweep CTAs per SM, 1 or 2; 0 = auto */
   int32_t slice_ranks;  /* cap on the distinct keys of one rank-LUT slice held in
                            shared memory; 0 = as many as fit */
-  int32_t tile;         /* sweep tile geometry: 1 narrow (2 events + 2 queries staged per
-                           thread, 32 steps), 2 wide (4 events + 1 query, 64 steps);
-                           0 = by the query/event ratio */
+  int32_t tile;         /* sweep tile geometry: 1 narrow (256 threads, 2 events + 2 queries
+                           staged per thread, 32 steps), 2 wide (256 threads, 4 events + 1
+                           query, 64 steps), 3 and 4 the same tiles on 512 threads (one
+                           CTA per SM); 0 = by the query/event ratio */
   int32_t reserved;
 } BwForestTuning;
 

@@ -45,6 +45,8 @@ def run_forest(bw, torch, F, tuning=None):
     (5, 60, {"slice_ranks": 512}),                       # several key slices per block
     (6, 50, {"tile": 1, "block_work": 65536}),           # narrow sweep tiles
     (7, 50, {"tile": 2, "ctas_per_sm": 1}),              # wide sweep tiles, one CTA per SM
+    (8, 40, {"tile": 3}),                                # narrow tiles on 512 threads
+    (9, 40, {"tile": 4, "block_work": 65536}),           # wide tiles on 512 threads
 ])
 def test_forest_matches_oracle(bw, torch_cuda, oracle_mod, seed, T, tuning):
     rng = np.random.default_rng(seed)
@@ -133,3 +135,18 @@ def test_forest_shape_errors(bw, torch_cuda):
         bw.Forest([0, 0], [0, 0], [0, 0], [4])           # a tree without states
     with pytest.raises(RuntimeError):
         bw.Forest([0, 3], [0, 2], [0, 1], [0])           # empty key domain
+
+
+@pytest.mark.parametrize("tuning", [None, {"tile": 3}, {"tile": 4, "block_work": 200000}])
+def test_one_tree_forest_equals_plain(bw, torch_cuda, tuning):
+    """A forest of one tree is the plain replay (its uploaded tables, not the
+    plain path's per-launch ones)."""
+    rng = np.random.default_rng(15)
+    S, C = 6000, 30000
+    parent = evgen.make_tree(S, "fork", rng)
+    ev = evgen.make_events(S, C, 150000, rng, zipf=1.1)
+    qs = evgen.make_queries(S, C, 100000, rng)
+    p, e, q = evgen.to_device(torch_cuda, parent, ev, qs)
+    plain = bw.replay(p, C, e, q).cpu().numpy()
+    got = bw.forest_replay([0, S], [0, len(ev)], [0, len(qs)], [C], p, e, q, tuning=tuning).cpu().numpy()
+    np.testing.assert_array_equal(got, plain)
