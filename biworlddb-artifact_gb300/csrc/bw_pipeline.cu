@@ -825,19 +825,27 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     // warp 0 loads them and scans their counts (the running totals live in warp 0).
     int32_t filled = t0;
     int64_t run_e = 0, run_q = 0;
+    // Warp 0 keeps the descriptors of the next refill in registers (loaded one
+    // refill ahead), so a refill costs a scan and shared stores, not a global load.
+    constexpr int PER = Cfg::kRingFill / 32;
+    StepDesc pf[PER];
+    auto prefetch = [&](int32_t from) {
+#pragma unroll
+      for (int j = 0; j < PER; ++j) {
+        const int32_t t = from + lane * PER + j;
+        pf[j].e0 = 0; pf[j].q0 = 0; pf[j].ne = 0; pf[j].nq = 0;
+        if (t < t1) pf[j] = p.desc[t];
+      }
+    };
+    if (warp == 0) prefetch(t0);
     auto fill = [&]() {
       __syncthreads();
       if (warp == 0) {
-        constexpr int PER = Cfg::kRingFill / 32;
-        StepDesc d[PER];
         int64_t le = 0, lq = 0;
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
-          const int32_t t = filled + lane * PER + j;
-          d[j].e0 = 0; d[j].q0 = 0; d[j].ne = 0; d[j].nq = 0;
-          if (t < t1) d[j] = p.desc[t];
-          le += d[j].ne;
-          lq += d[j].nq > 0 ? d[j].nq : 0;
+          le += pf[j].ne;
+          lq += pf[j].nq > 0 ? pf[j].nq : 0;
         }
         int64_t ie = le, iq = lq;
 #pragma unroll
@@ -849,14 +857,15 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
           const int32_t sl = (filled + lane * PER + j) & M;
-          ring[sl] = d[j];
+          ring[sl] = pf[j];
           epre[sl] = xe;
           qpre[sl] = xq;
-          xe += d[j].ne;
-          xq += d[j].nq > 0 ? d[j].nq : 0;
+          xe += pf[j].ne;
+          xq += pf[j].nq > 0 ? pf[j].nq : 0;
         }
         run_e += __shfl_sync(0xffffffffu, ie, 31);
         run_q += __shfl_sync(0xffffffffu, iq, 31);
+        prefetch(filled + Cfg::kRingFill);
       }
       filled += Cfg::kRingFill;
       __syncthreads();
@@ -880,11 +889,11 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       x.qmask = (uint64_t)__ballot_sync(0xffffffffu, qa) | ((uint64_t)__ballot_sync(0xffffffffu, qb) << 32);
       return x;
     };
-    // Stage a tile cooperatively: warps 0-3 copy (cp.async) the events and warps
-    // 4-7 the queries of 32-step groups, lane l decoding step l of the group and
-    // lanes taking consecutive flattened items (the source step found by a shuffle
-    // search over the group's counts); each item's step (and exit flag) is written
-    // beside it.  A barrier after the copies land makes the tile visible.
+    // Stage a tile cooperatively: the first half of the warps copy (cp.async) the
+    // events and the second half the queries of 32-step groups.  Lane l decodes step
+    // l of the group; small steps are copied lane by lane, large ones by lanes taking
+    // consecutive flattened items.  Each item's step (and exit flag) is written beside
+    // it.  A barrier after the copies land makes the tile visible.
     auto stage = [&](const Tile& x, int buf) {
       const bool evw = warp < Cfg::kWarps / 2;
       const int wgrp = evw ? warp : warp - Cfg::kWarps / 2;
@@ -894,51 +903,65 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       uint8_t* em = emeta + (size_t)buf * Cfg::kTileEv;
       unsigned char* qb = qbuf + (size_t)buf * Cfg::kTileQ * 12;
       uint8_t* qm = qmeta + (size_t)buf * Cfg::kTileQ;
-      for (int32_t c = x.s + 32 * wgrp; c < x.e; c += 32 * (Cfg::kWarps / 2)) {
+      constexpr int HW = Cfg::kWarps / 2;   // warps per half (events / queries)
+      for (int32_t c = x.s, gi = 0; c < x.e; c += 32, ++gi) {
         const int32_t st = c + lane;
         int32_t cnt = 0;
-        uint32_t src0 = 0;
-        int32_t fpos = 0;
-        uint32_t meta = 0;
+        int64_t src = 0, f = 0;
+        uint8_t meta = 0;
         if (st < x.e) {
           const StepDesc d = ring[st & M];
-          const int64_t f = (evw ? epre[st & M] : qpre[st & M]) - p0;
+          f = (evw ? epre[st & M] : qpre[st & M]) - p0;
           const int64_t n = evw ? d.ne : (d.nq > 0 ? d.nq : 0);
           cnt = (int32_t)imin64(n, cap - f > 0 ? cap - f : 0);
-          src0 = evw ? d.e0 : d.q0;
-          fpos = (int32_t)f;
-          meta = evw ? (uint32_t)(((st - x.s) << 1) | (d.nq < 0 ? 1 : 0)) : (uint32_t)(st - x.s);
+          src = evw ? (int64_t)d.e0 : (int64_t)d.q0;
+          meta = evw ? (uint8_t)(((st - x.s) << 1) | (d.nq < 0 ? 1 : 0)) : (uint8_t)(st - x.s);
         }
-        int32_t incl = cnt;
+        int32_t most = cnt;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += y;
-        }
-        const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        for (int32_t g0 = 0; g0 < total; g0 += 32) {
-          const int32_t g = g0 + lane;
-          int32_t lo = 0, hi = 31;   // first lane whose inclusive count exceeds g
-#pragma unroll
-          for (int it = 0; it < 5; ++it) {
-            const int32_t mid = (lo + hi) >> 1;
-            if (__shfl_sync(0xffffffffu, incl, mid) > g) hi = mid; else lo = mid + 1;
+        for (int o = 16; o; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
+        auto put = [&](int64_t fpos, int64_t from, uint8_t mt) {
+          if (evw) {
+            cp_async16(eb + fpos, p.ev + from);
+            em[fpos] = mt;
+          } else {
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(p.qs + from);
+            unsigned char* dq = qb + (size_t)fpos * 12;
+            cp_async4(dq, q);
+            cp_async4(dq + 4, q + 1);
+            cp_async4(dq + 8, q + 2);
+            qm[fpos] = mt;
           }
-          const int32_t s_incl = __shfl_sync(0xffffffffu, incl, lo), s_cnt = __shfl_sync(0xffffffffu, cnt, lo);
-          const uint32_t s_src = __shfl_sync(0xffffffffu, src0, lo), s_meta = __shfl_sync(0xffffffffu, meta, lo);
-          const int32_t s_pos = __shfl_sync(0xffffffffu, fpos, lo);
-          if (g < total) {
-            const int32_t off = g - (s_incl - s_cnt);
-            if (evw) {
-              cp_async16(eb + s_pos + off, p.ev + (int64_t)s_src + off);
-              em[s_pos + off] = (uint8_t)s_meta;
-            } else {
-              const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + (int64_t)s_src + off);
-              unsigned char* dq = qb + (size_t)(s_pos + off) * 12;
-              cp_async4(dq, src);
-              cp_async4(dq + 4, src + 1);
-              cp_async4(dq + 8, src + 2);
-              qm[s_pos + off] = (uint8_t)s_meta;
+        };
+        if (most <= 16) {
+          // small steps: one warp of the half takes the group, lane l copies its step
+          if (gi % HW == wgrp)
+            for (int32_t i = 0; i < most; ++i)
+              if (i < cnt) put(f + i, src + i, meta);
+        } else {
+          // large steps: the half's warps split the group's flattened items; a
+          // lane finds its item's step by a shuffle search over the inclusive counts
+          int32_t incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+          }
+          const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+          for (int32_t g0 = 32 * wgrp; g0 < total; g0 += 32 * HW) {
+            const int32_t g = g0 + lane;
+            int32_t lo = 0, hi = 31;   // first lane whose inclusive count exceeds g
+#pragma unroll
+            for (int it = 0; it < 5; ++it) {
+              const int32_t mid = (lo + hi) >> 1;
+              if (__shfl_sync(0xffffffffu, incl, mid) > g) hi = mid; else lo = mid + 1;
+            }
+            const int32_t s_incl = __shfl_sync(0xffffffffu, incl, lo), s_cnt = __shfl_sync(0xffffffffu, cnt, lo);
+            const int64_t s_src = __shfl_sync(0xffffffffu, src, lo), s_f = __shfl_sync(0xffffffffu, f, lo);
+            const uint8_t s_meta = (uint8_t)__shfl_sync(0xffffffffu, (uint32_t)meta, lo);
+            if (g < total) {
+              const int32_t off = g - (s_incl - s_cnt);
+              put(s_f + off, s_src + off, s_meta);
             }
           }
         }
@@ -1130,26 +1153,221 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       }
     };
 
-    fill();
-    Tile cur = make_tile(t0);
-    stage(cur, 0);
-    int buf = 0;
-    for (;;) {
-      cp_async_wait<0>();
-      __syncthreads();   // the current tile is staged and visible; the other buffer is free
-      const int32_t ns = cur.e;
-      Tile nxt;
-      nxt.s = nxt.e = t1;
-      nxt.qmask = 0;
-      if (ns < t1) {
-        if (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
-        nxt = make_tile(ns);
-        stage(nxt, buf ^ 1);
+    auto stage_own = [&](const Tile& x, int buf, int32_t* own_e, int32_t* own_q) {
+      const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
+      const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
+#pragma unroll
+      for (int m = 0; m < Cfg::kEvPer; ++m) {
+        const int64_t g = tid + m * Cfg::kThreads;
+        own_e[m] = -1;
+        if (g < ne) {
+          int32_t lo = x.s, hi = x.e - 1;
+          while (lo < hi) {
+            const int32_t mid = (lo + hi + 1) >> 1;
+            if (epre[mid & M] - pe0 <= g) lo = mid; else hi = mid - 1;
+          }
+          const StepDesc d = ring[lo & M];
+          cp_async16(evbuf + (size_t)buf * Cfg::kTileEv + g, p.ev + (int64_t)d.e0 + (pe0 + g - epre[lo & M]));
+          own_e[m] = ((lo - x.s) << 1) | (d.nq < 0 ? 1 : 0);
+          emeta[(size_t)buf * Cfg::kTileEv + g] = (uint8_t)own_e[m];
+        }
       }
-      process(cur, buf);
-      if (ns >= t1) break;
-      cur = nxt;
-      buf ^= 1;
+#pragma unroll
+      for (int m = 0; m < Cfg::kQPer; ++m) {
+        const int64_t g = qslot + m * Cfg::kThreads;
+        own_q[m] = -1;
+        if (g < nq) {
+          int32_t lo = x.s, hi = x.e - 1;
+          while (lo < hi) {
+            const int32_t mid = (lo + hi + 1) >> 1;
+            if (qpre[mid & M] - pq0 <= g) lo = mid; else hi = mid - 1;
+          }
+          const StepDesc d = ring[lo & M];
+          const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + (int64_t)d.q0 + (pq0 + g - qpre[lo & M]));
+          unsigned char* dq = qbuf + ((size_t)buf * Cfg::kTileQ + g) * 12;
+          cp_async4(dq, src);
+          cp_async4(dq + 4, src + 1);
+          cp_async4(dq + 8, src + 2);
+          own_q[m] = lo - x.s;
+        }
+      }
+      cp_async_commit();
+    };
+    auto process_own = [&](const Tile& x, int buf, const int32_t* own_e, const int32_t* own_q) {
+      const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
+      const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
+      const BwEvent* eb = evbuf + (size_t)buf * Cfg::kTileEv;
+      const uint8_t* em = emeta + (size_t)buf * Cfg::kTileEv;
+      const unsigned char* qb = qbuf + (size_t)buf * Cfg::kTileQ * 12;
+      uint64_t c_lo[Cfg::kQPer], c_hi[Cfg::kQPer];
+#pragma unroll
+      for (int m = 0; m < Cfg::kQPer; ++m) {
+        c_lo[m] = c_hi[m] = 0;
+        if (carried && own_q[m] >= 0) {
+          const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(qslot + m * Cfg::kThreads) * 12);
+          if (q[2] > q[1]) {
+            c_lo[m] = (uint64_t)__ldg(crow + q[1]);
+            c_hi[m] = (uint64_t)__ldg(crow + q[2]);
+          }
+        }
+      }
+      // answers index of the staged query g of tile step u
+      auto qindex = [&](int32_t urel, int64_t g) -> int64_t {
+        const int32_t u = x.s + urel;
+        return (int64_t)ring[u & M].q0 + (pq0 + g - qpre[u & M]);
+      };
+      if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= Cfg::kTileQ && nq * ne <= kOfflinePairs) {
+        __syncthreads();   // earlier updates applied; this tile's staged events visible
+        if (dirty) {
+          rebuild();
+          dirty = false;
+        }
+#pragma unroll
+        for (int m = 0; m < Cfg::kQPer; ++m) {
+          const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(qslot + m * Cfg::kThreads) * 12);
+          const bool mine = own_q[m] >= 0;
+          const uint32_t my_lo = mine ? q[1] : 0u, my_hi = mine ? q[2] : 0u;
+          uint32_t owners = __ballot_sync(0xffffffffu, mine);
+          while (owners) {
+            const int src = __ffs(owners) - 1;
+            owners &= owners - 1;
+            const uint32_t lo = __shfl_sync(0xffffffffu, my_lo, src), hi = __shfl_sync(0xffffffffu, my_hi, src);
+            const int32_t urel = __shfl_sync(0xffffffffu, own_q[m], src);
+            const uint32_t a_lo = lo > klo ? lo : klo, a_hi = hi < khi ? hi : khi;
+            uint64_t corr = 0;
+            if (s.n && a_lo < a_hi) {
+              for (int64_t i = lane; i < ne; i += 32) {
+                const uint8_t mt = em[i];
+                if ((int32_t)(mt >> 1) <= urel) {
+                  const BwEvent e = eb[i];
+                  if (e.key >= a_lo && e.key < a_hi)
+                    corr += (mt & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
+                }
+              }
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) corr += __shfl_xor_sync(0xffffffffu, corr, o);
+            if (lane == src)
+              finish(lo, hi, corr + (c_hi[m] - c_lo[m]), qindex(urel, qslot + m * Cfg::kThreads));
+          }
+        }
+        __syncthreads();   // probes done before this tile's updates
+        if (s.n) {
+#pragma unroll
+          for (int m = 0; m < Cfg::kEvPer; ++m) {
+            if (own_e[m] >= 0) {
+              const BwEvent e = eb[tid + m * Cfg::kThreads];
+              apply(e.key, (uint64_t)e.delta, own_e[m] & 1);
+            }
+          }
+        }
+        if (ne > 0) dirty = true;
+        return;
+      }
+      uint32_t done = 0;         // own staged events applied so far
+      int32_t a = x.s;           // first step of the current segment
+      uint64_t qm = x.qmask;
+      for (;;) {
+        const bool has_q = qm != 0;
+        const int32_t u = has_q ? x.s + __ffsll((long long)qm) - 1 : x.e - 1;
+        const int32_t urel = u - x.s;
+        if (s.n) {
+#pragma unroll
+          for (int m = 0; m < Cfg::kEvPer; ++m) {
+            if (!(done >> m & 1u) && own_e[m] >= 0 && (own_e[m] >> 1) <= urel) {
+              const BwEvent e = eb[tid + m * Cfg::kThreads];
+              apply(e.key, (uint64_t)e.delta, own_e[m] & 1);
+              done |= 1u << m;
+            }
+          }
+          if (ne > Cfg::kTileEv && a == x.s) {  // one step with more events than a tile stages
+            const StepDesc d = ring[x.s & M];
+            for (int64_t g = Cfg::kTileEv + tid; g < ne; g += Cfg::kThreads) {
+              const BwEvent e = p.ev[(int64_t)d.e0 + g];
+              apply(e.key, (uint64_t)e.delta, d.nq < 0);
+            }
+          }
+        }
+        if (epre[(u + 1) & M] > epre[a & M]) dirty = true;
+        if (!has_q) break;
+        __syncthreads();  // every update of steps <= u is applied
+        if (dirty) {
+          rebuild();
+          dirty = false;
+        }
+#pragma unroll
+        for (int m = 0; m < Cfg::kQPer; ++m) {
+          if (own_q[m] == urel) {
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(qslot + m * Cfg::kThreads) * 12);
+            finish(q[1], q[2], c_hi[m] - c_lo[m], qindex(urel, qslot + m * Cfg::kThreads));
+          }
+        }
+        if (nq > Cfg::kTileQ) {  // one step with more queries than a tile stages
+          const int64_t qbase = qindex(urel, 0);
+          for (int64_t g = Cfg::kTileQ + tid; g < nq; g += Cfg::kThreads) {
+            const BwQuery qq = p.qs[qbase + g];
+            uint64_t acc = 0;
+            if (carried && qq.hi > qq.lo) acc = (uint64_t)__ldg(crow + qq.hi) - (uint64_t)__ldg(crow + qq.lo);
+            finish(qq.lo, qq.hi, acc, qbase + g);
+          }
+        }
+        __syncthreads();  // probes done before the next updates
+        qm &= qm - 1;
+        a = u + 1;
+      }
+    };
+
+    if constexpr (Cfg::kCoop) {
+      fill();
+      Tile cur = make_tile(t0);
+      stage(cur, 0);
+      int buf = 0;
+      for (;;) {
+        cp_async_wait<0>();
+        __syncthreads();   // the current tile is staged and visible; the other buffer is free
+        const int32_t ns = cur.e;
+        Tile nxt;
+        nxt.s = nxt.e = t1;
+        nxt.qmask = 0;
+        if (ns < t1) {
+          if (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
+          nxt = make_tile(ns);
+          stage(nxt, buf ^ 1);
+        }
+        process(cur, buf);
+        if (ns >= t1) break;
+        cur = nxt;
+        buf ^= 1;
+      }
+    } else {
+      fill();
+      Tile cur = make_tile(t0);
+      int32_t cur_e[Cfg::kEvPer], cur_q[Cfg::kQPer];
+      stage_own(cur, 0, cur_e, cur_q);
+      int buf = 0;
+      for (;;) {
+        const int32_t ns = cur.e;
+        Tile nxt;
+        int32_t nxt_e[Cfg::kEvPer], nxt_q[Cfg::kQPer];
+        if (ns < t1) {
+          if (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
+          nxt = make_tile(ns);
+          stage_own(nxt, buf ^ 1, nxt_e, nxt_q);
+        } else {
+          nxt.s = nxt.e = t1;
+          nxt.qmask = 0;
+          cp_async_commit();
+        }
+        cp_async_wait<1>();   // this thread's copies of the current tile have landed
+        process_own(cur, buf, cur_e, cur_q);
+        if (ns >= t1) break;
+        cur = nxt;
+  #pragma unroll
+        for (int m = 0; m < Cfg::kEvPer; ++m) cur_e[m] = nxt_e[m];
+  #pragma unroll
+        for (int m = 0; m < Cfg::kQPer; ++m) cur_q[m] = nxt_q[m];
+        buf ^= 1;
+      }
     }
     cp_async_wait<0>();
     __syncthreads();

@@ -50,18 +50,22 @@ constexpr int64_t kOfflinePairs = 32768;      // tile (queries x events) below w
 
 // Sweep tile geometry: THREADS per CTA, EV events and QP queries staged per thread
 // per tile, at most STEPS steps per tile, a ring of RING step descriptors refilled
-// RING/2 at a time.  The ring must hold two tiles plus a refill: RING >= 4 * STEPS.
-template <int EV, int QP, int STEPS, int RING, int THREADS>
+// RING/2 at a time (the ring must hold two tiles plus a refill: RING >= 4 * STEPS).
+// COOP: the tile is staged cooperatively and made visible by a barrier (suits many
+// small steps); otherwise every thread stages the items it will apply and probe
+// itself and waits for its own copies only (suits few large, query-heavy steps).
+template <int EV, int QP, int STEPS, int RING, int THREADS, bool COOP>
 struct TileCfg {
+  static constexpr bool kCoop = COOP;
   static constexpr int kEvPer = EV, kQPer = QP, kTileSteps = STEPS, kRing = RING, kRingFill = RING / 2;
   static constexpr int kThreads = THREADS, kWarps = THREADS / 32, kMinBlocks = THREADS >= 512 ? 1 : 2;
   static constexpr int kTileEv = EV * THREADS, kTileQ = QP * THREADS;
   static_assert(RING >= 4 * STEPS && STEPS <= 64 && kRingFill % 32 == 0, "tile ring too small");
 };
-using TileNarrow = TileCfg<2, 2, 32, 128, 256>;      // query-heavy steps: small staging, more Fenwick
-using TileWide = TileCfg<4, 1, 64, 256, 256>;        // event-heavy steps: deep event staging
-using TileNarrow512 = TileCfg<1, 1, 32, 128, 512>;   // the same with 16 warps (one CTA per SM)
-using TileWide512 = TileCfg<2, 1, 64, 256, 512>;
+using TileNarrow = TileCfg<2, 2, 32, 128, 256, false>;      // query-heavy steps: small staging, more Fenwick
+using TileWide = TileCfg<4, 1, 64, 256, 256, true>;         // event-heavy steps: deep event staging
+using TileNarrow512 = TileCfg<1, 1, 32, 128, 512, false>;   // the same with 16 warps (one CTA per SM)
+using TileWide512 = TileCfg<2, 1, 64, 256, 512, true>;
 enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4 };
 
 // ------------------------------------------------------------------ records
