@@ -93,37 +93,67 @@ __global__ void k_fill_i64(int64_t* p, int64_t n, int64_t v) {
 // item range holds i; its global state is the tree's first state + the local one.
 // Checks grouping within each tree and key / interval ranges against the tree's
 // domain.
+// Contiguous item range of this warp (whole multiples of 32), so lanes take
+// consecutive items and each lane's tree only moves forward: one tree search per
+// lane and range instead of one per item.
+__device__ __forceinline__ void warp_range(int64_t n, int64_t& lo, int64_t& hi) {
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t per = (((n + warps - 1) / warps) + 31) & ~(int64_t)31;
+  lo = imin64(n, w * per);
+  hi = imin64(n, lo + per);
+}
+template <typename Off>
+__device__ __forceinline__ int32_t tree_forward(const Off* off, int32_t T, int32_t t, int64_t x) {
+  while (t + 1 < T && (int64_t)off[t + 1] <= x) ++t;
+  return t;
+}
+
 template <bool kEvents>
 __global__ void k_offsets(const void* items, int64_t n, TreeTabs tt, int32_t T, int32_t S, int64_t* off,
                           int32_t* status) {
   const int64_t* toff = kEvents ? tt.eoff : tt.qoff;
   const BwEvent* ev = static_cast<const BwEvent*>(items);
   const BwQuery* qs = static_cast<const BwQuery*>(items);
-  auto state_at = [&](int64_t i) -> uint32_t { return kEvents ? ev[i].state : qs[i].state; };
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    const int32_t t = T > 1 ? find_tree(toff, T, i) : 0;
+  const int lane = threadIdx.x & 31;
+  int64_t lo, hi;
+  warp_range(n, lo, hi);
+  if (lo >= hi) return;
+  // global state of item i (-2: out of its tree, reported by its own lane)
+  auto gstate = [&](int32_t t, int64_t i) -> int64_t {
     const int32_t s0 = tt.soff[t], ns = tt.soff[t + 1] - s0;
-    const uint32_t C = tt.C[t];
-    const uint32_t s = state_at(i);
-    if (kEvents) {
-      if (ev[i].key >= C) set_status(status, BW_STATUS_EVENT_KEY_RANGE);
-    } else {
-      if (qs[i].lo > C || qs[i].hi > C) set_status(status, BW_STATUS_QUERY_RANGE);
-    }
-    if (s >= (uint32_t)ns) { set_status(status, BW_STATUS_STATE_RANGE); continue; }
-    const int64_t g = (int64_t)s0 + s;
-    int64_t gprev = -1;
-    if (i > 0) {
-      const int32_t tp = (i - 1 >= toff[t]) ? t : find_tree(toff, T, i - 1);
-      const int32_t sp0 = tt.soff[tp], nsp = tt.soff[tp + 1] - sp0;
-      const uint32_t sp = state_at(i - 1);
-      if (sp >= (uint32_t)nsp) continue;   // reported by that item's thread
-      if (tp == t && sp > s) {
-        set_status(status, kEvents ? BW_STATUS_EVENTS_UNSORTED : BW_STATUS_QUERIES_UNSORTED);
-        continue;
+    const uint32_t s = kEvents ? ev[i].state : qs[i].state;
+    return s < (uint32_t)ns ? (int64_t)s0 + s : -2;
+  };
+  int64_t gcarry = -1;   // global state of the item before this lane 0's item
+  if (lo > 0) {
+    int64_t gp = 0;
+    if (lane == 0) gp = gstate(T > 1 ? find_tree(toff, T, lo - 1) : 0, lo - 1);
+    gcarry = __shfl_sync(0xffffffffu, gp, 0);
+  }
+  int32_t t = T > 1 ? find_tree(toff, T, imin64(lo + lane, n - 1)) : 0;
+  for (int64_t i0 = lo; i0 < hi; i0 += 32) {
+    const int64_t i = i0 + lane;
+    const bool valid = i < hi;
+    int64_t g = -2;
+    if (valid) {
+      if (T > 1) t = tree_forward(toff, T, t, i);
+      const uint32_t C = tt.C[t];
+      if (kEvents) {
+        if (ev[i].key >= C) set_status(status, BW_STATUS_EVENT_KEY_RANGE);
+      } else {
+        if (qs[i].lo > C || qs[i].hi > C) set_status(status, BW_STATUS_QUERY_RANGE);
       }
-      gprev = (int64_t)sp0 + sp;
+      g = gstate(t, i);
+      if (g == -2) set_status(status, BW_STATUS_STATE_RANGE);
+    }
+    int64_t gprev = __shfl_up_sync(0xffffffffu, g, 1);
+    if (lane == 0) gprev = gcarry;
+    gcarry = __shfl_sync(0xffffffffu, g, 31);
+    if (!valid || g == -2 || gprev == -2) continue;
+    if (gprev > g) {   // an earlier tree's states are below every state of this tree
+      set_status(status, kEvents ? BW_STATUS_EVENTS_UNSORTED : BW_STATUS_QUERIES_UNSORTED);
+      continue;
     }
     // off[x] = i for every global state x in (gprev, g]
     for (int64_t x = gprev + 1; x <= g; ++x) off[x] = i;
@@ -139,8 +169,11 @@ __global__ void k_offsets(const void* items, int64_t n, TreeTabs tt, int32_t T, 
 // (a state's answer only depends on its root path), only the step order.
 __global__ void k_lin_children(const int32_t* parent, int32_t S, TreeTabs tt, int32_t T, int32_t* gpar,
                                int32_t* fork_head, int32_t* next_sib, int chain_only, int32_t* status) {
-  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < S; v += gridDim.x * blockDim.x) {
-    const int32_t t = T > 1 ? find_tree(tt.soff, T, v) : 0;
+  int64_t lo, hi;
+  warp_range(S, lo, hi);
+  int32_t t = T > 1 && lo < hi ? find_tree(tt.soff, T, imin64(lo + (threadIdx.x & 31), S - 1)) : 0;
+  for (int32_t v = (int32_t)lo + (threadIdx.x & 31); v < hi; v += 32) {
+    if (T > 1) t = tree_forward(tt.soff, T, t, v);
     const int32_t s0 = tt.soff[t], l = v - s0;
     const int32_t p = parent[v];
     int32_t gp = -1;
@@ -256,8 +289,11 @@ __global__ void k_lin_steps(const uint64_t* r, const int64_t* cnt, const int32_t
                             const int32_t* status) {
   if (*status) return;
   const int64_t He = (uint32_t)(uint64_t)cnt[S - 1];
-  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < S; v += gridDim.x * blockDim.x) {
-    const int32_t t = T > 1 ? find_tree(tt.soff, T, v) : 0;
+  int64_t lo, hi;
+  warp_range(S, lo, hi);
+  int32_t t = T > 1 && lo < hi ? find_tree(tt.soff, T, imin64(lo + (threadIdx.x & 31), S - 1)) : 0;
+  for (int32_t v = (int32_t)lo + (threadIdx.x & 31); v < hi; v += 32) {
+    if (T > 1) t = tree_forward(tt.soff, T, t, v);
     const int32_t s0 = tt.soff[t], ns = tt.soff[t + 1] - s0;
     const int64_t base = 2 * (int64_t)s0 + 2 * (int64_t)ns;
     const uint64_t c = (uint64_t)cnt[v], cp = v ? (uint64_t)cnt[v - 1] : 0ull;
