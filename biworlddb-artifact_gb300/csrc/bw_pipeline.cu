@@ -1507,10 +1507,11 @@ int pipe_spec_forest(int32_t T, const int64_t* soff, const int64_t* eoff, const 
     s.Smax = std::max<int32_t>(s.Smax, (int32_t)ns);
   }
   s.ctas_per_sm = tune.ctas_per_sm > 0 ? tune.ctas_per_sm : 2;
+  finish_spec(s, tune);   // the sweep layout depends only on the domains and the tuning
   int64_t target = tune.block_work > 0 ? tune.block_work
                                        : std::max<int64_t>(65536, Wtot / (4 * (int64_t)s.ctas_per_sm * sms));
   std::vector<int32_t> nb(T);
-  for (;;) {
+  for (;;) {                       // the block work doubles until the carry rows fit
     int64_t carry = 0, blocks = 0;
     for (int32_t t = 0; t < T; ++t) {
       nb[t] = (int32_t)std::max<int64_t>(1, (W[t] + target - 1) / target);
@@ -1556,7 +1557,6 @@ int pipe_spec_forest(int32_t T, const int64_t* soff, const int64_t* eoff, const 
     for (int32_t i = 0; i < nb[t]; ++i) bw[s.h_boff[t] + i] = W[t] / nb[t];
   std::iota(s.h_order.begin(), s.h_order.end(), 0);
   std::stable_sort(s.h_order.begin(), s.h_order.end(), [&](int32_t a, int32_t b) { return bw[a] > bw[b]; });
-  finish_spec(s, tune);
   return 0;
 }
 

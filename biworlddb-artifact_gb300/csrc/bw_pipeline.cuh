@@ -64,7 +64,7 @@ struct TileCfg {
 };
 using TileNarrow = TileCfg<2, 2, 32, 128, 256, false>;      // query-heavy steps: small staging, more Fenwick
 using TileWide = TileCfg<4, 1, 64, 256, 256, true>;         // event-heavy steps: deep event staging
-using TileNarrow512 = TileCfg<1, 1, 32, 128, 512, false>;   // the same with 16 warps (one CTA per SM)
+using TileNarrow512 = TileCfg<1, 1, 64, 256, 512, false>;   // 16 warps (one CTA per SM), 64-step tiles
 using TileWide512 = TileCfg<2, 1, 64, 256, 512, true>;
 enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4 };
 
