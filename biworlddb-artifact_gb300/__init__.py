@@ -352,6 +352,78 @@ class Forest:
             pass
 
 
+class HostForest:
+    """Replay of a forest from host buffers with the copies hidden behind the work:
+    the trees are split into ``chunks`` contiguous groups of about equal events, each
+    with its own plan (captured in a CUDA graph) and device buffers; chunk k+1's
+    inputs are copied host to device on one stream while chunk k replays on another,
+    and each chunk's answers are copied back as soon as they are ready.  Host
+    buffers should be pinned (``torch.Tensor.pin_memory``) for the copies to
+    overlap."""
+
+    def __init__(self, state_off, event_off, query_off, n_keys, *, chunks: int = 4, tuning=None, device=None):
+        import numpy as np
+        torch = _torch()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        soff = np.asarray(state_off, dtype=np.int64)
+        eoff = np.asarray(event_off, dtype=np.int64)
+        qoff = np.asarray(query_off, dtype=np.int64)
+        keys = np.asarray(n_keys, dtype=np.uint32)
+        T = keys.size
+        chunks = max(1, min(int(chunks), T))
+        # cut points: equal shares of events (+ states), at tree boundaries
+        weight = np.cumsum(np.diff(eoff) + np.diff(soff))
+        cuts = [0] + [int(np.searchsorted(weight, weight[-1] * k / chunks)) + 1 for k in range(1, chunks)] + [T]
+        cuts = sorted(set(min(max(c, 0), T) for c in cuts))
+        self.copy_stream = torch.cuda.Stream(self.device)
+        self.work_stream = torch.cuda.Stream(self.device)
+        self.parts = []
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            if b <= a:
+                continue
+            part = {"s": (int(soff[a]), int(soff[b])), "e": (int(eoff[a]), int(eoff[b])),
+                    "q": (int(qoff[a]), int(qoff[b]))}
+            f = Forest(soff[a:b + 1] - soff[a], eoff[a:b + 1] - eoff[a], qoff[a:b + 1] - qoff[a], keys[a:b],
+                       tuning=tuning, device=self.device, stream=self.work_stream)
+            ns, ne, nq = (part["s"][1] - part["s"][0], part["e"][1] - part["e"][0], part["q"][1] - part["q"][0])
+            part["parent"] = torch.empty(ns, dtype=torch.int32, device=self.device)
+            part["events"] = torch.empty((ne, 2), dtype=torch.int64, device=self.device)
+            part["queries"] = torch.empty((nq, 3), dtype=torch.int32, device=self.device)
+            part["answers"] = torch.empty(nq, dtype=torch.int64, device=self.device)
+            part["forest"] = f
+            part["copied"] = torch.cuda.Event()
+            part["done"] = torch.cuda.Event()
+            f.capture(part["parent"], part["events"], part["queries"], part["answers"], self.work_stream)
+            part["done"].record(self.work_stream)
+            self.parts.append(part)
+        self.kernels = sum(p["forest"].info()["kernels"] for p in self.parts)
+
+    def run(self, h_parent, h_events, h_queries, h_answers) -> None:
+        """Enqueue one replay: copies in, graph launches, answers out (asynchronous;
+        synchronise the device or ``self.work_stream`` before reading h_answers)."""
+        cs, ws = self.copy_stream, self.work_stream
+        for part in self.parts:
+            (s0, s1), (e0, e1), (q0, q1) = part["s"], part["e"], part["q"]
+            cs.wait_event(part["done"])          # the previous replay of this chunk is finished
+            with __import__("torch").cuda.stream(cs):
+                part["parent"].copy_(h_parent[s0:s1], non_blocking=True)
+                part["events"].copy_(h_events[e0:e1], non_blocking=True)
+                part["queries"].copy_(h_queries[q0:q1], non_blocking=True)
+            part["copied"].record(cs)
+            ws.wait_event(part["copied"])
+            part["forest"].replay(ws)
+            with __import__("torch").cuda.stream(ws):
+                h_answers[q0:q1].copy_(part["answers"], non_blocking=True)
+            part["done"].record(ws)
+
+    def status(self) -> int:
+        for part in self.parts:
+            st = part["forest"].status(self.work_stream)
+            if st:
+                return st
+        return 0
+
+
 def forest_autotune(state_off, event_off, query_off, n_keys, parent, events, queries, answers, *, reps: int = 3,
                     stream=None):
     """Time the autotuner's candidate tunings on these inputs; returns (tuning dict, ms)."""

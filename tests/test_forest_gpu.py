@@ -150,3 +150,24 @@ def test_one_tree_forest_equals_plain(bw, torch_cuda, tuning):
     plain = bw.replay(p, C, e, q).cpu().numpy()
     got = bw.forest_replay([0, S], [0, len(ev)], [0, len(qs)], [C], p, e, q, tuning=tuning).cpu().numpy()
     np.testing.assert_array_equal(got, plain)
+
+
+@pytest.mark.parametrize("chunks", [1, 3])
+def test_host_forest_chunks(bw, torch_cuda, oracle_mod, chunks):
+    """Replay from pinned host buffers in chunks of trees (copies overlapping the
+    replay of other chunks), twice in a row, equals the oracle."""
+    torch = torch_cuda
+    rng = np.random.default_rng(16 + chunks)
+    soff, eoff, qoff, keys, par, ev, qs = make_forest(rng, 30, max_states=2500)
+    want = oracle_mod.ev_forest(soff, eoff, qoff, keys, par, ev, qs)
+    hp = torch.from_numpy(par).pin_memory()
+    he = torch.from_numpy(np.ascontiguousarray(ev).view(np.int64).reshape(-1, 2)).pin_memory()
+    hq = torch.from_numpy(np.ascontiguousarray(qs).view(np.int32).reshape(-1, 3)).pin_memory()
+    ha = torch.zeros(len(qs), dtype=torch.int64).pin_memory()
+    hf = bw.HostForest(soff, eoff, qoff, keys, chunks=chunks)
+    for _ in range(2):
+        ha.zero_()
+        hf.run(hp, he, hq, ha)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(ha.numpy(), want)
+    assert hf.status() == 0 and len(hf.parts) == chunks
