@@ -819,6 +819,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
   BwEvent* evbuf = reinterpret_cast<BwEvent*>(smem + L.off_ev);     // [2][Cfg::kTileEv]
   uint8_t* emeta = smem + L.off_emeta;                               // [2][Cfg::kTileEv] step << 1 | exit
   uint8_t* qmeta = smem + L.off_qmeta;                               // [2][Cfg::kTileQ] step
+  unsigned long long* corr = reinterpret_cast<unsigned long long*>(smem + L.off_corr);  // [kOfflineQ]
   unsigned char* qbuf = smem + L.off_q;                              // [2][Cfg::kTileQ] x 12 B
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // flattened queries g = qslot + 256 m belong to this thread: consecutive queries
@@ -855,6 +856,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     }
     for (uint32_t i = tid; i < nch * kChunkStride; i += Cfg::kThreads) fine[i] = 0;
     for (uint32_t i = tid; i < nch; i += Cfg::kThreads) T[i] = 0;
+    for (int i = tid; i < kOfflineQ; i += Cfg::kThreads) corr[i] = 0;
 
     // Step ring: descriptors and event/query prefixes of steps [filled - Cfg::kRing, filled);
     // steps past t1 read as empty.  A refill overwrites the oldest Cfg::kRingFill slots;
@@ -1083,7 +1085,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         const int32_t u = x.s + urel;
         return (int64_t)ring[u & M].q0 + (pq0 + g - qpre[u & M]);
       };
-      if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= Cfg::kTileQ && nq * ne <= kOfflinePairs) {
+      if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
         if (dirty) {
           rebuild();
           dirty = false;
@@ -1225,6 +1227,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           cp_async4(dq + 4, src + 1);
           cp_async4(dq + 8, src + 2);
           own_q[m] = lo - x.s;
+          qmeta[(size_t)buf * Cfg::kTileQ + g] = (uint8_t)(lo - x.s);
         }
       }
       cp_async_commit();
@@ -1252,39 +1255,49 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         const int32_t u = x.s + urel;
         return (int64_t)ring[u & M].q0 + (pq0 + g - qpre[u & M]);
       };
-      if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= Cfg::kTileQ && nq * ne <= kOfflinePairs) {
+      if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
         __syncthreads();   // earlier updates applied; this tile's staged events visible
         if (dirty) {
           rebuild();
           dirty = false;
         }
-#pragma unroll
-        for (int m = 0; m < Cfg::kQPer; ++m) {
-          const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(qslot + m * Cfg::kThreads) * 12);
-          const bool mine = own_q[m] >= 0;
-          const uint32_t my_lo = mine ? q[1] : 0u, my_hi = mine ? q[2] : 0u;
-          uint32_t owners = __ballot_sync(0xffffffffu, mine);
-          while (owners) {
-            const int src = __ffs(owners) - 1;
-            owners &= owners - 1;
-            const uint32_t lo = __shfl_sync(0xffffffffu, my_lo, src), hi = __shfl_sync(0xffffffffu, my_hi, src);
-            const int32_t urel = __shfl_sync(0xffffffffu, own_q[m], src);
+        // the tile's event/query pairs: query g's events are cut into `parts` ranges
+        // of whole 32-event chunks, one warp per (query, range); each warp sums its
+        // range and adds the sum to corr[g]
+        {
+          const uint8_t* qmt = qmeta + (size_t)buf * Cfg::kTileQ;
+          const int32_t nchunk = (int32_t)((ne + 31) / 32);
+          const int32_t parts = max(1, min(nchunk, Cfg::kWarps / max(1, (int32_t)nq)));
+          const int32_t per = (nchunk + parts - 1) / parts;
+          for (int32_t it = warp; it < (int32_t)nq * parts; it += Cfg::kWarps) {
+            const int32_t g = it / parts, part = it - g * parts;
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
+            const uint32_t lo = q[1], hi = q[2];
+            const int32_t urel = qmt[g];
             const uint32_t a_lo = lo > klo ? lo : klo, a_hi = hi < khi ? hi : khi;
-            uint64_t corr = 0;
-            if (s.n && a_lo < a_hi) {
-              for (int64_t i = lane; i < ne; i += 32) {
-                const uint8_t mt = em[i];
-                if ((int32_t)(mt >> 1) <= urel) {
-                  const BwEvent e = eb[i];
-                  if (e.key >= a_lo && e.key < a_hi)
-                    corr += (mt & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
-                }
-              }
+            if (!s.n || a_lo >= a_hi) continue;
+            uint64_t v = 0;
+            const int64_t i1 = imin64(ne, (int64_t)(part + 1) * per * 32);
+#pragma unroll 4
+            for (int64_t i = (int64_t)part * per * 32 + lane; i < i1; i += 32) {
+              const uint8_t mt = em[i];
+              const BwEvent e = eb[i];
+              if ((int32_t)(mt >> 1) <= urel && e.key >= a_lo && e.key < a_hi)
+                v += (mt & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
             }
 #pragma unroll
-            for (int o = 16; o; o >>= 1) corr += __shfl_xor_sync(0xffffffffu, corr, o);
-            if (lane == src)
-              finish(lo, hi, corr + (c_hi[m] - c_lo[m]), qindex(urel, qslot + m * Cfg::kThreads));
+            for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && v) shared_add_u64(corr + g, v);
+          }
+        }
+        __syncthreads();   // every pair summed
+#pragma unroll
+        for (int m = 0; m < Cfg::kQPer; ++m) {
+          if (own_q[m] >= 0) {
+            const int64_t g = qslot + m * Cfg::kThreads;
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
+            finish(q[1], q[2], (uint64_t)corr[g] + (c_hi[m] - c_lo[m]), qindex(own_q[m], g));
+            corr[g] = 0;
           }
         }
         __syncthreads();   // probes done before this tile's updates

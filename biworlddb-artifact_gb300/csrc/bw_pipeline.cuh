@@ -47,6 +47,7 @@ constexpr int kChunkStride = 257;
 constexpr int kMaxChunks = 128;
 constexpr int kRebuildPer = 5;
 constexpr int64_t kOfflinePairs = 32768;      // tile (queries x events) below which probes are batched
+constexpr int kOfflineQ = 128;                // and at most this many queries (their sums live in smem)
 
 // Sweep tile geometry: THREADS per CTA, EV events and QP queries staged per thread
 // per tile, at most STEPS steps per tile, a ring of RING step descriptors refilled
@@ -114,7 +115,7 @@ struct SweepLayout {
   int32_t ww;
   int32_t nch32, nch64;
   uint32_t cap32, cap64;
-  size_t off_rl, off_fine, off_T, off_P, off_ring, off_epre, off_qpre, off_ev, off_emeta, off_q, off_qmeta, bytes;
+  size_t off_rl, off_fine, off_T, off_P, off_ring, off_epre, off_qpre, off_ev, off_emeta, off_q, off_qmeta, off_corr, bytes;
 };
 template <typename Cfg>
 __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budget) {
@@ -123,7 +124,7 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const size_t staging = sizeof(StepDesc) * Cfg::kRing + 2 * 8 * (size_t)Cfg::kRing +
                          2 * (size_t)Cfg::kTileEv * 16 + al(2 * (size_t)Cfg::kTileEv) +
-                         al(2 * (size_t)Cfg::kTileQ * 12) + al(2 * (size_t)Cfg::kTileQ);
+                         al(2 * (size_t)Cfg::kTileQ * 12) + al(2 * (size_t)Cfg::kTileQ) + (size_t)kOfflineQ * 8;
   const size_t fixed = al((size_t)L.ww * 8) + al(((size_t)L.ww + 2) * 4) + staging +
                        (size_t)Cfg::kWarps * (kMaxChunks + 1) * 8 + 128;
   const size_t per32 = (size_t)kChunkStride * 4 + 8;  // int32 nodes + chunk total
@@ -145,6 +146,7 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   L.off_emeta = o; o = al(o + 2 * (size_t)Cfg::kTileEv);
   L.off_q = o;    o = al(o + 2 * (size_t)Cfg::kTileQ * 12);
   L.off_qmeta = o; o = al(o + 2 * (size_t)Cfg::kTileQ);
+  L.off_corr = o; o = al(o + (size_t)kOfflineQ * 8);
   L.bytes = o;
   return L;
 }
