@@ -70,7 +70,7 @@ __host__ __device__ __forceinline__ int32_t words_of(uint32_t C) { return (int32
 __global__ void k_init(int32_t* misc, TreeTabs tt, int32_t T, int one_tree, int32_t S, int64_t E, int64_t Q,
                        uint32_t C, int32_t nb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < 16) misc[i] = 0;
+  if (i < 64) misc[i] = 0;
   for (int t = i; t < T; t += gridDim.x * blockDim.x) tt.last_q[t] = 0;
   if (one_tree && i == 0) {
     tt.soff[0] = 0; tt.soff[1] = S;
@@ -265,28 +265,35 @@ __global__ void k_lin_rank_init(const int64_t* cnt, const int32_t* ehead, const 
   }
 }
 
-// One Wyllie pointer-jumping round: dist(x) += dist(next(x)), next(x) = next(next(x)).
-__global__ void k_lin_round(const uint64_t* __restrict__ src, uint64_t* __restrict__ dst, const int64_t* cnt,
-                            int32_t S, const int32_t* status) {
+// One Wyllie pointer-jumping round, in place: dist(x) += dist(next(x)),
+// next(x) = next(next(x)).  A (next, dist) pair is one 64-bit word, so a read sees a
+// consistent pair even while its owner updates it (jumping further ahead keeps
+// dist(x) = the lengths from x up to next(x)).  Round r records whether any pointer
+// is still live; a round after one that found none returns at once.
+__global__ void k_lin_round(uint64_t* __restrict__ r, const int64_t* cnt, int32_t S, int32_t* live, int32_t round,
+                            const int32_t* status) {
   if (*status) return;
+  if (round > 0 && live[round - 1] == 0) return;
   const uint64_t tot = (uint64_t)cnt[S - 1];
   const int64_t H = (int64_t)(uint32_t)tot + (int64_t)(tot >> 32);
+  bool any = false;
   for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < H; x += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t a = src[x];
+    const uint64_t a = r[x];
     const int32_t nx = (int32_t)(a >> 32);
-    if (nx < 0) { dst[x] = a; continue; }
-    const uint64_t b = src[nx];
-    dst[x] = (b & 0xFFFFFFFF00000000ull) | (uint32_t)((uint32_t)a + (uint32_t)b);
+    if (nx < 0) continue;
+    const uint64_t b = r[nx];
+    r[x] = (b & 0xFFFFFFFF00000000ull) | (uint32_t)((uint32_t)a + (uint32_t)b);
+    any |= (int32_t)(b >> 32) >= 0;
   }
+  if (__syncthreads_or(any) && threadIdx.x == 0) live[round] = 1;
 }
 
-// Step sequence, per-step descriptors and work, tin/tout, and each tree's last
+// Step sequence (each step's enter/exit partner), per-step descriptors and work, and each tree's last
 // step that answers a query.  Tree t's tour occupies steps [2 s0, 2 s0 + 2 ns): the
 // head arc of a segment sits at 2 s0 + 2 ns - dist, the other arcs follow it.
 __global__ void k_lin_steps(const uint64_t* r, const int64_t* cnt, const int32_t* ehead, const int32_t* xhead,
                             int32_t S, TreeTabs tt, int32_t T, const int64_t* eoff, const int64_t* qoff,
-                            int32_t* steps, StepDesc* desc, int64_t* work, int32_t* tin, int32_t* tout,
-                            const int32_t* status) {
+                            int32_t* partner, StepDesc* desc, int64_t* work, const int32_t* status) {
   if (*status) return;
   const int64_t He = (uint32_t)(uint64_t)cnt[S - 1];
   int64_t lo, hi;
@@ -304,10 +311,8 @@ __global__ void k_lin_steps(const uint64_t* r, const int64_t* cnt, const int32_t
     const int64_t px = base - (int64_t)(uint32_t)r[He + xid] + (xhead[xid] - v);
     const int64_t e0 = eoff[v], q0 = qoff[v];
     const int32_t ne = (int32_t)(eoff[v + 1] - e0), nq = (int32_t)(qoff[v + 1] - q0);
-    steps[pe] = v;
-    steps[px] = ~v;
-    tin[v] = (int32_t)pe;
-    tout[v] = (int32_t)px;
+    partner[pe] = (int32_t)px;
+    partner[px] = (int32_t)pe;
     StepDesc d;
     d.e0 = (uint32_t)e0; d.q0 = (uint32_t)q0; d.ne = ne; d.nq = nq;
     desc[pe] = d;
@@ -364,9 +369,7 @@ __global__ void k_blocks(const int64_t* work, TreeTabs tt, int32_t T, int32_t B,
 struct PrepParams {
   const BwEvent* ev;
   const StepDesc* desc;
-  const int32_t* steps;
-  const int32_t* tin;
-  const int32_t* tout;
+  const int32_t* partner;  // per step: the step of the same node's enter/exit
   const BlockTab* blocks;
   const int32_t* order;    // queue order of the blocks (NULL: identity)
   int32_t B;
@@ -402,11 +405,10 @@ __device__ __forceinline__ void for_block_events(const PrepParams& p, int32_t t0
     if (t < t1) {
       const StepDesc d = p.desc[t];
       neg = d.nq < 0;
-      const int32_t x = p.steps[t];
-      const int32_t u = x >= 0 ? x : ~x;
-      twice = !neg && p.tout[u] < t1;
+      const int32_t pt = p.partner[t];           // the node's other step (exit of an enter, enter of an exit)
+      twice = !neg && pt < t1;
       bool keep = true;
-      if (neg) keep = p.tin[u] < t0;            // entered in this block: keys known, deltas cancel
+      if (neg) keep = pt < t0;                   // entered in this block: keys known, deltas cancel
       else if (mode == 1 && twice) keep = false; // leaves within this block: net zero
       if (keep) { cnt = d.ne; e0 = d.e0; }
     }
@@ -1589,7 +1591,7 @@ void pipe_layout(const PipeSpec& s, Layout& L) {
   const bool forest = !s.h_soff.empty();   // tables uploaded by pipe_bind (else written per launch)
   take(W_UNITS, forest ? (size_t)s.n_units * sizeof(CarryUnit) : 0);
   take(W_ORDER, forest ? B * 4 : 0);
-  take(W_MISC, 64);
+  take(W_MISC, 256);
   take(W_EOFF, (S + 1) * 8);
   take(W_QOFF, (S + 1) * 8);
   take(W_GPAR, s.T > 1 ? S * 4 : 0);
@@ -1599,11 +1601,11 @@ void pipe_layout(const PipeSpec& s, Layout& L) {
   take(W_EHEAD, S * 4);
   take(W_XHEAD, S * 4);
   take(W_RANKA, S2 * 8);
-  take(W_RANKB, S2 * 8);
+  take(W_RANKB, 0);               // (list ranking runs in place)
   take(W_STEPS, S2 * 4);
   take(W_DESC, S2 * sizeof(StepDesc));
-  take(W_TIN, S * 4);
-  take(W_TOUT, S * 4);
+  take(W_TIN, 0);                 // (enter/exit partners replace tin/tout)
+  take(W_TOUT, 0);
   take(W_WORK, S2 * 8);
   take(W_SCAN, scan_tmp_bytes(S2));
   take(W_BLOCKS, B * sizeof(BlockTab));
@@ -1709,11 +1711,8 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
   int32_t* ehead = reinterpret_cast<int32_t*>(at(W_EHEAD));
   int32_t* xhead = reinterpret_cast<int32_t*>(at(W_XHEAD));
   uint64_t* rank_a = reinterpret_cast<uint64_t*>(at(W_RANKA));
-  uint64_t* rank_b = reinterpret_cast<uint64_t*>(at(W_RANKB));
-  int32_t* steps = reinterpret_cast<int32_t*>(at(W_STEPS));
+  int32_t* partner = reinterpret_cast<int32_t*>(at(W_STEPS));
   StepDesc* desc = reinterpret_cast<StepDesc*>(at(W_DESC));
-  int32_t* tin = reinterpret_cast<int32_t*>(at(W_TIN));
-  int32_t* tout = reinterpret_cast<int32_t*>(at(W_TOUT));
   int64_t* work = reinterpret_cast<int64_t*>(at(W_WORK));
   int64_t* scan_tmp = reinterpret_cast<int64_t*>(at(W_SCAN));
   BlockTab* blocks = reinterpret_cast<BlockTab*>(at(W_BLOCKS));
@@ -1760,15 +1759,13 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
   if ((rc = chk("k_lin_heads"))) return rc;
   k_lin_rank_init<<<grid, 256, 0, st>>>(cnt, ehead, xhead, gp, fork_head, next_sib, S, rank_a, status);
   if ((rc = chk("k_lin_rank_init"))) return rc;
-  uint64_t* src = rank_a;
-  uint64_t* dst = rank_b;
-  for (int64_t span = 1; span < 2 * (int64_t)s.Smax; span <<= 1) {
-    k_lin_round<<<grid, 256, 0, st>>>(src, dst, cnt, S, status);
+  int32_t round = 0;
+  for (int64_t span = 1; span < 2 * (int64_t)s.Smax; span <<= 1, ++round) {
+    k_lin_round<<<grid, 256, 0, st>>>(rank_a, cnt, S, misc + M_ROUNDS, round, status);
     if ((rc = chk("k_lin_round"))) return rc;
-    std::swap(src, dst);
   }
-  k_lin_steps<<<grid, 256, 0, st>>>(src, cnt, ehead, xhead, S, tt, T, eoff, qoff, steps, desc, work, tin, tout,
-                                    status);
+  const uint64_t* src = rank_a;
+  k_lin_steps<<<grid, 256, 0, st>>>(src, cnt, ehead, xhead, S, tt, T, eoff, qoff, partner, desc, work, status);
   if ((rc = chk("k_lin_steps"))) return rc;
 
   if ((rc = mark(2))) return rc;
@@ -1784,7 +1781,7 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
   const size_t psmem = (size_t)SL.ww * 8 + ((size_t)SL.ww + 4) * 4 +
                        std::max(((size_t)SL.cap32 + 1) * 4, ((size_t)SL.cap64 + 1) * 8) + 16;
   PrepParams pp;
-  pp.ev = events; pp.desc = desc; pp.steps = steps; pp.tin = tin; pp.tout = tout; pp.blocks = blocks;
+  pp.ev = events; pp.desc = desc; pp.partner = partner; pp.blocks = blocks;
   pp.order = order; pp.B = B; pp.ww = SL.ww; pp.cap32 = SL.cap32; pp.cap64 = SL.cap64;
   pp.bits = reinterpret_cast<uint64_t*>(at(W_BITS)); pp.rlut = reinterpret_cast<uint32_t*>(at(W_RLUT));
   pp.slices = reinterpret_cast<Slice*>(at(W_SLICES)); pp.nslices = reinterpret_cast<int32_t*>(at(W_NSLICES));
