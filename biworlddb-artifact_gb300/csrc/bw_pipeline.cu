@@ -1092,33 +1092,41 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           rebuild();
           dirty = false;
         }
+        {
+          // the tile's event/query pairs: query g's events are cut into `parts` ranges
+          // of whole 32-event chunks, one warp per (query, range), summed into corr[g]
+          const int32_t nchunk = (int32_t)((ne + 31) / 32);
+          const int32_t parts = max(1, min(nchunk, Cfg::kWarps / max(1, (int32_t)nq)));
+          const int32_t per = (nchunk + parts - 1) / parts;
+          for (int32_t it = warp; it < (int32_t)nq * parts; it += Cfg::kWarps) {
+            const int32_t g = it / parts, part = it - g * parts;
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
+            const uint32_t lo = q[1], hi = q[2];
+            const int32_t urel = qmt[g];
+            const uint32_t a_lo = lo > klo ? lo : klo, a_hi = hi < khi ? hi : khi;
+            if (!s.n || a_lo >= a_hi) continue;
+            uint64_t v = 0;
+            const int64_t i1 = imin64(ne, (int64_t)(part + 1) * per * 32);
+#pragma unroll 4
+            for (int64_t i = (int64_t)part * per * 32 + lane; i < i1; i += 32) {
+              const uint8_t mt = em[i];
+              const BwEvent e = eb[i];
+              if ((int32_t)(mt >> 1) <= urel && e.key >= a_lo && e.key < a_hi)
+                v += (mt & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
+            }
+#pragma unroll
+            for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && v) shared_add_u64(corr + g, v);
+          }
+        }
+        __syncthreads();   // every pair summed
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
           const int64_t g = qslot + m * Cfg::kThreads;
-          const bool mine = g < nq;
-          const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(mine ? g : 0) * 12);
-          const uint32_t my_lo = mine ? q[1] : 0u, my_hi = mine ? q[2] : 0u;
-          const int32_t my_u = mine ? (int32_t)qmt[g] : 0;
-          uint32_t owners = __ballot_sync(0xffffffffu, mine);
-          while (owners) {
-            const int src = __ffs(owners) - 1;
-            owners &= owners - 1;
-            const uint32_t lo = __shfl_sync(0xffffffffu, my_lo, src), hi = __shfl_sync(0xffffffffu, my_hi, src);
-            const int32_t urel = __shfl_sync(0xffffffffu, my_u, src);
-            const uint32_t a_lo = lo > klo ? lo : klo, a_hi = hi < khi ? hi : khi;
-            uint64_t corr = 0;
-            if (s.n && a_lo < a_hi) {
-#pragma unroll 4
-              for (int64_t i = lane; i < ne; i += 32) {
-                const uint8_t mt = em[i];
-                const BwEvent e = eb[i];
-                if ((int32_t)(mt >> 1) <= urel && e.key >= a_lo && e.key < a_hi)
-                  corr += (mt & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
-              }
-            }
-#pragma unroll
-            for (int o = 16; o; o >>= 1) corr += __shfl_xor_sync(0xffffffffu, corr, o);
-            if (lane == src) finish(lo, hi, corr + (c_hi[m] - c_lo[m]), qindex(urel, g));
+          if (g < nq) {
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
+            finish(q[1], q[2], (uint64_t)corr[g] + (c_hi[m] - c_lo[m]), qindex((int32_t)qmt[g], g));
+            corr[g] = 0;
           }
         }
         __syncthreads();   // probes done before this tile's updates
