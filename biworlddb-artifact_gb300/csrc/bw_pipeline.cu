@@ -768,6 +768,14 @@ __device__ __forceinline__ void chunk_add(Node* f, unsigned long long* tot, uint
   }
 }
 
+// Flat chunk update: the rank's own value and the chunk total.
+template <typename Node>
+__device__ __forceinline__ void flat_add(Node* f, unsigned long long* tot, uint32_t i, uint64_t v) {
+  if constexpr (sizeof(Node) == 4) atomicAdd(reinterpret_cast<unsigned*>(f) + i, (unsigned)v);
+  else shared_add_u64(reinterpret_cast<unsigned long long*>(f) + i, v);
+  shared_add_u64(tot, v);
+}
+
 template <typename Node>
 __device__ __forceinline__ uint64_t node_value(Node x) {
   if constexpr (sizeof(Node) == 4) return (uint64_t)(int64_t)(int32_t)x;
@@ -1012,8 +1020,12 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       if (k >= klo && k < khi) {
         if (neg) v = (uint64_t)0 - v;
         const uint32_t r = local_rank(sbits, srl, k - klo);
-        chunk_add<Node>(fine + (size_t)(r >> kChunkBits) * kChunkStride, T + (r >> kChunkBits),
-                        (r & (kChunk - 1u)) + 1u, v);
+        if constexpr (Cfg::kFlat)
+          flat_add<Node>(fine + (size_t)(r >> kChunkBits) * kChunkStride, T + (r >> kChunkBits),
+                         r & (kChunk - 1u), v);
+        else
+          chunk_add<Node>(fine + (size_t)(r >> kChunkBits) * kChunkStride, T + (r >> kChunkBits),
+                          (r & (kChunk - 1u)) + 1u, v);
       }
     };
     bool dirty = true;   // chunk totals changed since the warps' prefix copies were built
@@ -1052,6 +1064,43 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       acc += slice_prefix2(fine, Pw, s.n, sbits, srl, klo, khi, hi);
       acc -= slice_prefix2(fine, Pw, s.n, sbits, srl, klo, khi, lo);
       *out = first ? (int64_t)acc : (int64_t)((uint64_t)*out + acc);
+    };
+    // Flat chunks: this lane's share of the prefix below key k (the chunk prefix
+    // on lane 0 plus every 32nd value of the chunk below the key's rank).
+    auto flat_part = [&](uint32_t k) -> uint64_t {
+      if (k <= klo) return 0;
+      const uint32_t r = k >= khi ? s.n : local_rank(sbits, srl, k - klo);
+      const uint32_t h = r >> kChunkBits, w = r & (kChunk - 1u);
+      const Node* f = fine + (size_t)h * kChunkStride;
+      uint64_t v = lane == 0 ? (uint64_t)Pw[h] : 0ull;
+      for (uint32_t i = lane; i < w; i += 32) v += node_value(f[i]);
+      return v;
+    };
+    // Answer the queries of the lanes with `mine` (warp-uniform call): Fenwick chunks
+    // let each owner finish alone; flat chunks sum the chunk's values with the warp.
+    auto finish_warp = [&](bool mine, uint32_t lo, uint32_t hi, uint64_t acc, int64_t j) {
+      if constexpr (!Cfg::kFlat) {
+        if (mine) finish(lo, hi, acc, j);
+      } else {
+        uint32_t owners = __ballot_sync(0xffffffffu, mine);
+        while (owners) {
+          const int src = __ffs(owners) - 1;
+          owners &= owners - 1;
+          const uint32_t l = __shfl_sync(0xffffffffu, lo, src), h = __shfl_sync(0xffffffffu, hi, src);
+          uint64_t d = h > l ? flat_part(h) - flat_part(l) : 0ull;
+#pragma unroll
+          for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+          if (lane == src) {
+            int64_t* out = p.answers + j;
+            if (hi <= lo) {
+              if (first) *out = 0;
+            } else {
+              const uint64_t a = acc + d;
+              *out = first ? (int64_t)a : (int64_t)((uint64_t)*out + a);
+            }
+          }
+        }
+      }
     };
     // Replay a staged, visible tile.  Thread t applies flattened events t + 256 m;
     // the tile's queries g = qslot + 256 m belong to this thread.  Segment mode:
@@ -1123,11 +1172,18 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
           const int64_t g = qslot + m * Cfg::kThreads;
-          if (g < nq) {
+          const bool mine = g < nq;
+          uint32_t lo = 0, hi = 0;
+          uint64_t acc = 0;
+          int64_t j = 0;
+          if (mine) {
             const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
-            finish(q[1], q[2], (uint64_t)corr[g] + (c_hi[m] - c_lo[m]), qindex((int32_t)qmt[g], g));
+            lo = q[1]; hi = q[2];
+            acc = (uint64_t)corr[g] + (c_hi[m] - c_lo[m]);
+            j = qindex((int32_t)qmt[g], g);
             corr[g] = 0;
           }
+          finish_warp(mine, lo, hi, acc, j);
         }
         __syncthreads();   // probes done before this tile's updates
         if (s.n) {
@@ -1181,18 +1237,27 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
           const int64_t g = qslot + m * Cfg::kThreads;
-          if (g < ns_q && (int32_t)qmt[g] == urel) {
+          const bool mine = g < ns_q && (int32_t)qmt[g] == urel;
+          uint32_t lo = 0, hi = 0;
+          if (mine) {
             const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
-            finish(q[1], q[2], c_hi[m] - c_lo[m], qindex(urel, g));
+            lo = q[1]; hi = q[2];
           }
+          finish_warp(mine, lo, hi, c_hi[m] - c_lo[m], mine ? qindex(urel, g) : 0);
         }
         if (nq > Cfg::kTileQ) {  // one step with more queries than a tile stages
           const int64_t qbase = qindex(urel, 0);
-          for (int64_t g = Cfg::kTileQ + tid; g < nq; g += Cfg::kThreads) {
-            const BwQuery qq = p.qs[qbase + g];
+          for (int64_t g0 = Cfg::kTileQ + (tid & ~31); g0 < nq; g0 += Cfg::kThreads) {   // warp-uniform
+            const int64_t g = g0 + lane;
+            const bool mine = g < nq;
+            BwQuery qq;
+            qq.lo = qq.hi = 0;
             uint64_t acc = 0;
-            if (carried && qq.hi > qq.lo) acc = (uint64_t)__ldg(crow + qq.hi) - (uint64_t)__ldg(crow + qq.lo);
-            finish(qq.lo, qq.hi, acc, qbase + g);
+            if (mine) {
+              qq = p.qs[qbase + g];
+              if (carried && qq.hi > qq.lo) acc = (uint64_t)__ldg(crow + qq.hi) - (uint64_t)__ldg(crow + qq.lo);
+            }
+            finish_warp(mine, qq.lo, qq.hi, acc, qbase + g);
           }
         }
         __syncthreads();  // probes done before the next updates
@@ -1303,12 +1368,19 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         __syncthreads();   // every pair summed
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
-          if (own_q[m] >= 0) {
-            const int64_t g = qslot + m * Cfg::kThreads;
+          const bool mine = own_q[m] >= 0;
+          const int64_t g = qslot + m * Cfg::kThreads;
+          uint32_t lo = 0, hi = 0;
+          uint64_t acc = 0;
+          int64_t j = 0;
+          if (mine) {
             const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
-            finish(q[1], q[2], (uint64_t)corr[g] + (c_hi[m] - c_lo[m]), qindex(own_q[m], g));
+            lo = q[1]; hi = q[2];
+            acc = (uint64_t)corr[g] + (c_hi[m] - c_lo[m]);
+            j = qindex(own_q[m], g);
             corr[g] = 0;
           }
+          finish_warp(mine, lo, hi, acc, j);
         }
         __syncthreads();   // probes done before this tile's updates
         if (s.n) {
@@ -1356,18 +1428,27 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         }
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
-          if (own_q[m] == urel) {
+          const bool mine = own_q[m] == urel;
+          uint32_t lo = 0, hi = 0;
+          if (mine) {
             const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)(qslot + m * Cfg::kThreads) * 12);
-            finish(q[1], q[2], c_hi[m] - c_lo[m], qindex(urel, qslot + m * Cfg::kThreads));
+            lo = q[1]; hi = q[2];
           }
+          finish_warp(mine, lo, hi, c_hi[m] - c_lo[m], mine ? qindex(urel, qslot + m * Cfg::kThreads) : 0);
         }
         if (nq > Cfg::kTileQ) {  // one step with more queries than a tile stages
           const int64_t qbase = qindex(urel, 0);
-          for (int64_t g = Cfg::kTileQ + tid; g < nq; g += Cfg::kThreads) {
-            const BwQuery qq = p.qs[qbase + g];
+          for (int64_t g0 = Cfg::kTileQ + (tid & ~31); g0 < nq; g0 += Cfg::kThreads) {   // warp-uniform
+            const int64_t g = g0 + lane;
+            const bool mine = g < nq;
+            BwQuery qq;
+            qq.lo = qq.hi = 0;
             uint64_t acc = 0;
-            if (carried && qq.hi > qq.lo) acc = (uint64_t)__ldg(crow + qq.hi) - (uint64_t)__ldg(crow + qq.lo);
-            finish(qq.lo, qq.hi, acc, qbase + g);
+            if (mine) {
+              qq = p.qs[qbase + g];
+              if (carried && qq.hi > qq.lo) acc = (uint64_t)__ldg(crow + qq.hi) - (uint64_t)__ldg(crow + qq.lo);
+            }
+            finish_warp(mine, qq.lo, qq.hi, acc, qbase + g);
           }
         }
         __syncthreads();  // probes done before the next updates

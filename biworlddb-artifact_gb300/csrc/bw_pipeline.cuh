@@ -55,18 +55,22 @@ constexpr int kOfflineQ = 128;                // and at most this many queries (
 // COOP: the tile is staged cooperatively and made visible by a barrier (suits many
 // small steps); otherwise every thread stages the items it will apply and probe
 // itself and waits for its own copies only (suits few large, query-heavy steps).
-template <int EV, int QP, int STEPS, int RING, int THREADS, bool COOP>
+// FLAT: the rank structure keeps plain values per rank with chunk totals (two
+// atomics per update, probes summed by a warp: suits few queries per many events);
+// otherwise a Fenwick tree inside every chunk (<= 9 atomics per update, probes by one
+// thread: suits many queries).
+template <int EV, int QP, int STEPS, int RING, int THREADS, bool COOP, bool FLAT>
 struct TileCfg {
-  static constexpr bool kCoop = COOP;
+  static constexpr bool kCoop = COOP, kFlat = FLAT;
   static constexpr int kEvPer = EV, kQPer = QP, kTileSteps = STEPS, kRing = RING, kRingFill = RING / 2;
   static constexpr int kThreads = THREADS, kWarps = THREADS / 32, kMinBlocks = THREADS >= 512 ? 1 : 2;
   static constexpr int kTileEv = EV * THREADS, kTileQ = QP * THREADS;
   static_assert(RING >= 4 * STEPS && STEPS <= 64 && kRingFill % 32 == 0, "tile ring too small");
 };
-using TileNarrow = TileCfg<2, 2, 32, 128, 256, false>;      // query-heavy steps: small staging, more Fenwick
-using TileWide = TileCfg<4, 1, 64, 256, 256, true>;         // event-heavy steps: deep event staging
-using TileNarrow512 = TileCfg<1, 1, 64, 256, 512, false>;   // 16 warps (one CTA per SM), 64-step tiles
-using TileWide512 = TileCfg<2, 1, 64, 256, 512, true>;
+using TileNarrow = TileCfg<2, 2, 32, 128, 256, false, false>;      // query-heavy steps: small staging, Fenwick
+using TileWide = TileCfg<4, 1, 64, 256, 256, true, true>;          // event-heavy steps: deep staging, flat
+using TileNarrow512 = TileCfg<1, 1, 64, 256, 512, false, true>;    // 16 warps (one CTA per SM), own staging, flat
+using TileWide512 = TileCfg<2, 1, 64, 256, 512, true, true>;
 enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4 };
 
 // ------------------------------------------------------------------ records
