@@ -90,7 +90,8 @@ GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch",
                "bw_forest_capture", "bw_forest_graph_launch", "bw_forest_status", "bw_forest_info",
                "bw_forest_destroy", "bw_forest_autotune_workspace", "bw_forest_autotune",
                "bw_forest_launch_timed",
-               "bw_serve_create", "bw_serve_reset", "bw_serve_run", "bw_serve_info", "bw_serve_destroy"]
+               "bw_serve_create", "bw_serve_reset", "bw_serve_run", "bw_serve_info", "bw_serve_destroy",
+               "bw_forest_plan_stats"]
 
 _gpu = None
 
@@ -143,6 +144,8 @@ def gpu_lib(build_if_missing: bool = True):
         L.bw_forest_status.argtypes = [P, P, C.POINTER(C.c_int32)]
         L.bw_forest_info.argtypes = [P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(BwForestTuning)]
         L.bw_forest_destroy.argtypes = [P]
+        L.bw_forest_plan_stats.argtypes = [C.POINTER(BwForestShape), C.POINTER(BwForestTuning), C.c_int32,
+                                           C.POINTER(C.c_int32), C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
         L.bw_forest_autotune_workspace.argtypes = [C.POINTER(BwForestShape), C.POINTER(C.c_size_t)]
         L.bw_forest_autotune.argtypes = [C.POINTER(BwForestShape), P, P, P, P, P, C.c_size_t, P, C.c_int32,
                                          C.POINTER(BwForestTuning), C.POINTER(C.c_float)]
@@ -422,6 +425,17 @@ class HostForest:
             if st:
                 return st
         return 0
+
+
+def forest_plan_stats(state_off, event_off, query_off, n_keys, *, tuning=None, sms: int = 152) -> dict:
+    """Host-only planning of a forest (no GPU needed): blocks, workspace and carry bytes."""
+    lib = gpu_lib()
+    shape = _ForestShape(state_off, event_off, query_off, n_keys)
+    tu = _tuning(tuning)
+    b, ws, cb = C.c_int32(0), C.c_size_t(0), C.c_size_t(0)
+    _check(lib.bw_forest_plan_stats(C.byref(shape.c), C.byref(tu) if tu is not None else None, int(sms), C.byref(b),
+                                    C.byref(ws), C.byref(cb)), "bw_forest_plan_stats")
+    return {"blocks": int(b.value), "workspace_bytes": int(ws.value), "carry_bytes": int(cb.value)}
 
 
 def forest_autotune(state_off, event_off, query_off, n_keys, parent, events, queries, answers, *, reps: int = 3,

@@ -213,6 +213,25 @@ extern "C" int bw_forest_destroy(BwForest* f) {
   return 0;
 }
 
+extern "C" int bw_forest_plan_stats(const BwForestShape* sh, const BwForestTuning* tu, int32_t sms, int32_t* blocks,
+                                    size_t* workspace_bytes, size_t* carry_bytes) {
+  if (!sh || sh->n_trees < 1 || !sh->state_off || !sh->event_off || !sh->query_off || !sh->n_keys || sms < 1)
+    return BW_EINVAL;
+  if (tu && (tu->ctas_per_sm < 0 || tu->ctas_per_sm > 2 || tu->block_work < 0 || tu->slice_ranks < 0 ||
+             tu->tile < 0 || tu->tile > 4))
+    return BW_EINVAL;
+  PipeSpec s;
+  const int rc = pipe_spec_forest(sh->n_trees, sh->state_off, sh->event_off, sh->query_off, sh->n_keys, to_tuning(tu),
+                                  sms, s);
+  if (rc) return rc;
+  Layout L;
+  pipe_layout(s, L);
+  if (blocks) *blocks = s.B;
+  if (workspace_bytes) *workspace_bytes = L.total;
+  if (carry_bytes) *carry_bytes = (size_t)s.carry_words * 8;
+  return 0;
+}
+
 extern "C" int bw_forest_autotune_workspace(const BwForestShape* shape, size_t* bytes) {
   if (!shape || !bytes) return BW_EINVAL;
   int sms = 0;

@@ -236,6 +236,11 @@ int bw_forest_status(BwForest* f, void* stream, int32_t* status);
 /* Blocks, kernels per launch, and the tuning in effect. */
 int bw_forest_info(const BwForest* f, int32_t* blocks, int32_t* kernels, BwForestTuning* tuning);
 int bw_forest_destroy(BwForest* f);
+/* Host-only planning (no device call): the blocks, workspace bytes and dense carry
+ * bytes bw_forest_create would plan for this shape and tuning on a GPU with `sms`
+ * multiprocessors. */
+int bw_forest_plan_stats(const BwForestShape* shape, const BwForestTuning* tuning, int32_t sms, int32_t* blocks,
+                         size_t* workspace_bytes, size_t* carry_bytes);
 /* Autotuner: times candidate tunings on the caller's inputs (sweep CTAs per SM x
  * block work, then the other tile geometry, then narrower LUT slices, each at the
  * best so far) with `reps` launches after a warm-up, skips candidates the device
