@@ -447,16 +447,16 @@ __device__ __forceinline__ void for_block_events(const PrepParams& p, int32_t t0
   }
 }
 
-__device__ void prepare_block(const PrepParams& p, int32_t b, unsigned char* smem) {
+// Pass A of block b: per window of the key domain, the bitmap of the keys the
+// block's events touch, its popcount rank table, the greedy slices the sweep's
+// rank capacity allows, and the block's node mode (int32 when the applied |delta|
+// sum stays below 2^31).
+__device__ void prepare_block_a(const PrepParams& p, int32_t b, unsigned char* smem) {
   const BlockTab bt = p.blocks[b];
   const int32_t nwords = bt.nwords;
   const uint32_t C = bt.C;
   uint64_t* sbits = reinterpret_cast<uint64_t*>(smem);                    // ww words
   uint32_t* srl = reinterpret_cast<uint32_t*>(sbits + p.ww);              // ww + 2
-  // histogram: int32 per rank when the block's nodes are int32 (exact, same
-  // bound), int64 otherwise; both fit the same bytes (cap32 ~ 2 * cap64)
-  unsigned char* hist_raw = reinterpret_cast<unsigned char*>(srl + p.ww + 2 + (p.ww & 1));  // 8-byte aligned
-  __shared__ uint64_t s_wsum[kPrepThreads / 32];
   __shared__ int32_t s_nsl;
   __shared__ int32_t s_mode;
 
@@ -524,12 +524,28 @@ __device__ void prepare_block(const PrepParams& p, int32_t b, unsigned char* sme
     p.bmode[b] = s_mode;
   }
   __syncthreads();
-  if (bt.carry_out < 0) return;   // the last block of a tree hands no carry on
-  const int32_t nsl = min(s_nsl, kMaxSlices);
+}
 
-  // ---- pass B: per slice, net key deltas of the block -> dense key-prefix row
+// Pass B of block b (only blocks that hand a carry on, i.e. all but the last
+// block of each tree): per slice of pass A, the block's net key deltas gathered
+// in a shared histogram over the slice's ranks, written out as the dense
+// key-prefix row carry[carry_out .. carry_out + C].
+__device__ void prepare_block_b(const PrepParams& p, int32_t b, unsigned char* smem) {
+  const BlockTab bt = p.blocks[b];
+  const uint32_t C = bt.C;
+  uint64_t* sbits = reinterpret_cast<uint64_t*>(smem);                    // ww words
+  uint32_t* srl = reinterpret_cast<uint32_t*>(sbits + p.ww);              // ww + 2
+  // histogram: int32 per rank when the block's nodes are int32 (exact, same
+  // bound), int64 otherwise; both fit the same bytes (cap32 ~ 2 * cap64)
+  unsigned char* hist_raw = reinterpret_cast<unsigned char*>(srl + p.ww + 2 + (p.ww & 1));  // 8-byte aligned
+  __shared__ uint64_t s_wsum[kPrepThreads / 32];
+  const int32_t t0 = bt.t0, t1 = bt.t1;
+  const uint64_t* gbits = p.bits + bt.bits_off;
+  const uint32_t* grl = p.rlut + bt.bits_off + b;
+  const Slice* gsl = p.slices + (size_t)b * kMaxSlices;
+  const int32_t nsl = p.nslices[b];
   int64_t* row = p.carry + bt.carry_out;
-  const bool h32 = s_mode != 0;
+  const bool h32 = p.bmode[b] != 0;
   unsigned* hist32 = reinterpret_cast<unsigned*>(hist_raw);
   unsigned long long* hist64 = reinterpret_cast<unsigned long long*>(hist_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -601,8 +617,11 @@ __device__ void prepare_block(const PrepParams& p, int32_t b, unsigned char* sme
   if (threadIdx.x == 0) row[C] = (int64_t)base;
 }
 
-// Persistent: CTAs take blocks from the queue until it is empty.
-__global__ void __launch_bounds__(kPrepThreads, 2) k_prepare(PrepParams p) {
+// Persistent: CTAs take blocks from the queue until it is empty.  Pass A needs
+// only the bitmap window (several CTAs per SM); pass B also holds the slice
+// histogram, so it runs as its own kernel over the blocks that hand a carry on.
+template <int Pass>
+__global__ void __launch_bounds__(kPrepThreads, Pass == 0 ? 3 : 2) k_prepare(PrepParams p) {
   if (*p.status) return;  // bounds/descriptors are not trustworthy after an input error
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ int32_t s_ticket;
@@ -612,7 +631,9 @@ __global__ void __launch_bounds__(kPrepThreads, 2) k_prepare(PrepParams p) {
     __syncthreads();
     const int32_t i = s_ticket;
     if (i >= p.B) break;
-    prepare_block(p, p.order ? p.order[i] : i, smem);
+    const int32_t b = p.order ? p.order[i] : i;
+    if (Pass == 0) prepare_block_a(p, b, smem);
+    else if (p.blocks[b].carry_out >= 0) prepare_block_b(p, b, smem);
   }
 }
 
@@ -1737,7 +1758,10 @@ static int ensure_attrs() {
   if (rc) return rc;
   std::lock_guard<std::mutex> g(mu);
   if (dev >= 0 && dev < 64 && done[dev]) return 0;
-  if ((rc = report(cudaFuncSetAttribute(k_prepare, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit - 1024),
+  if ((rc = report(cudaFuncSetAttribute(k_prepare<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit - 1024),
+                   "smem attr")))
+    return rc;
+  if ((rc = report(cudaFuncSetAttribute(k_prepare<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit - 1024),
                    "smem attr")))
     return rc;
   if ((rc = report(cudaFuncSetAttribute(k_sweep<TileNarrow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1867,8 +1891,8 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
   if ((rc = mark(3))) return rc;
   // ---- 4. prepare
   const SweepLayout& SL = s.SL;
-  const size_t psmem = (size_t)SL.ww * 8 + ((size_t)SL.ww + 4) * 4 +
-                       std::max(((size_t)SL.cap32 + 1) * 4, ((size_t)SL.cap64 + 1) * 8) + 16;
+  const size_t asmem = (size_t)SL.ww * 8 + ((size_t)SL.ww + 4) * 4 + 16;
+  const size_t psmem = asmem + std::max(((size_t)SL.cap32 + 1) * 4, ((size_t)SL.cap64 + 1) * 8);
   PrepParams pp;
   pp.ev = events; pp.desc = desc; pp.partner = partner; pp.blocks = blocks;
   pp.order = order; pp.B = B; pp.ww = SL.ww; pp.cap32 = SL.cap32; pp.cap64 = SL.cap64;
@@ -1876,8 +1900,17 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
   pp.slices = reinterpret_cast<Slice*>(at(W_SLICES)); pp.nslices = reinterpret_cast<int32_t*>(at(W_NSLICES));
   pp.carry = reinterpret_cast<int64_t*>(at(W_CARRY)); pp.status = status; pp.bmode = bmode;
   pp.ticket = misc + M_PREP_TICKET;
-  k_prepare<<<std::min(B, 2 * s.sms), kPrepThreads, psmem, st>>>(pp);
-  if ((rc = chk("k_prepare"))) return rc;
+  int occ_a = 0;
+  if ((rc = report(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_prepare<0>, kPrepThreads, asmem),
+                   "occupancy")))
+    return rc;
+  k_prepare<0><<<std::min(B, std::max(occ_a, 1) * s.sms), kPrepThreads, asmem, st>>>(pp);
+  if ((rc = chk("k_prepare<0>"))) return rc;
+  if (s.carry_words > 0) {   // some block hands a carry on
+    pp.ticket = misc + M_PREPB_TICKET;
+    k_prepare<1><<<std::min(B, 2 * s.sms), kPrepThreads, psmem, st>>>(pp);
+    if ((rc = chk("k_prepare<1>"))) return rc;
+  }
 
   if ((rc = mark(4))) return rc;
   // ---- 5. carry

@@ -206,7 +206,7 @@ enum {
 };
 
 // misc words
-enum { M_STATUS = 0, M_PREP_TICKET = 1, M_SWEEP_TICKET = 2, M_CHAIN = 3, M_ROUNDS = 32 };  // 64 words
+enum { M_STATUS = 0, M_PREP_TICKET = 1, M_SWEEP_TICKET = 2, M_CHAIN = 3, M_PREPB_TICKET = 4, M_ROUNDS = 32 };  // 64 words
 
 // Stage timing events of one launch.
 struct EventSet { cudaEvent_t ev[BW_STAGE_COUNT + 1]; };
