@@ -752,9 +752,11 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // 1..kChunk, stopping below the chunk top, at most kChunkLevels nodes) and the
 // chunk total.  int64 nodes use exact 32-bit-pair atomics with all low-word
 // atomics issued before any high-word one (one shared-atomic round trip);
-// int32 nodes take plain 32-bit atomics with no return value.
+// int32 nodes (and the int32 chunk total beside them: every partial sum of a
+// block whose applied |delta| sum is below 2^31 fits) take plain 32-bit atomics
+// with no return value.
 template <typename Node>
-__device__ __forceinline__ void chunk_add(Node* f, unsigned long long* tot, uint32_t l, uint64_t v) {
+__device__ __forceinline__ void chunk_add(Node* f, Node* tot, uint32_t l, uint64_t v) {
   const unsigned lo = (unsigned)v, hi = (unsigned)(v >> 32);
   unsigned* tw = reinterpret_cast<unsigned*>(tot);
   if constexpr (sizeof(Node) == 4) {
@@ -764,7 +766,7 @@ __device__ __forceinline__ void chunk_add(Node* f, unsigned long long* tot, uint
       if (x < (uint32_t)kChunk) atomicAdd(reinterpret_cast<unsigned*>(f) + x, lo);
       x += x & (0u - x);
     }
-    shared_add_u64(tot, v);
+    atomicAdd(tw, lo);
   } else {
     unsigned* fw = reinterpret_cast<unsigned*>(f);
     unsigned old[kChunkLevels];
@@ -789,12 +791,17 @@ __device__ __forceinline__ void chunk_add(Node* f, unsigned long long* tot, uint
   }
 }
 
-// Flat chunk update: the rank's own value and the chunk total.
+// Flat chunk update: the rank's own value and the chunk total (both of the
+// node type, so int32 blocks make two no-return atomics).
 template <typename Node>
-__device__ __forceinline__ void flat_add(Node* f, unsigned long long* tot, uint32_t i, uint64_t v) {
-  if constexpr (sizeof(Node) == 4) atomicAdd(reinterpret_cast<unsigned*>(f) + i, (unsigned)v);
-  else shared_add_u64(reinterpret_cast<unsigned long long*>(f) + i, v);
-  shared_add_u64(tot, v);
+__device__ __forceinline__ void flat_add(Node* f, Node* tot, uint32_t i, uint64_t v) {
+  if constexpr (sizeof(Node) == 4) {
+    atomicAdd(reinterpret_cast<unsigned*>(f) + i, (unsigned)v);
+    atomicAdd(reinterpret_cast<unsigned*>(tot), (unsigned)v);
+  } else {
+    shared_add_u64(reinterpret_cast<unsigned long long*>(f) + i, v);
+    shared_add_u64(reinterpret_cast<unsigned long long*>(tot), v);
+  }
 }
 
 template <typename Node>
@@ -843,7 +850,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
   uint64_t* sbits = reinterpret_cast<uint64_t*>(smem);
   uint32_t* srl = reinterpret_cast<uint32_t*>(smem + L.off_rl);
   Node* fine = reinterpret_cast<Node*>(smem + L.off_fine);
-  unsigned long long* T = reinterpret_cast<unsigned long long*>(smem + L.off_T);
+  Node* T = reinterpret_cast<Node*>(smem + L.off_T);   // chunk totals
   StepDesc* ring = reinterpret_cast<StepDesc*>(smem + L.off_ring);
   int64_t* epre = reinterpret_cast<int64_t*>(smem + L.off_epre);   // events before step, per ring slot
   int64_t* qpre = reinterpret_cast<int64_t*>(smem + L.off_qpre);   // queries before step, per ring slot
@@ -1058,7 +1065,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       uint64_t sum = 0;
 #pragma unroll
       for (int i = 0; i < kRebuildPer; ++i) {
-        tv[i] = ((uint32_t)i < per && lo + i < nch) ? T[lo + i] : 0;
+        tv[i] = ((uint32_t)i < per && lo + i < nch) ? node_value(T[lo + i]) : 0;
         sum += tv[i];
       }
       uint64_t xx = sum;
@@ -1086,15 +1093,28 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       acc -= slice_prefix2(fine, Pw, s.n, sbits, srl, klo, khi, lo);
       *out = first ? (int64_t)acc : (int64_t)((uint64_t)*out + acc);
     };
-    // Flat chunks: this lane's share of the prefix below key k (the chunk prefix
-    // on lane 0 plus every 32nd value of the chunk below the key's rank).
-    auto flat_part = [&](uint32_t k) -> uint64_t {
-      if (k <= klo) return 0;
-      const uint32_t r = k >= khi ? s.n : local_rank(sbits, srl, k - klo);
-      const uint32_t h = r >> kChunkBits, w = r & (kChunk - 1u);
-      const Node* f = fine + (size_t)h * kChunkStride;
-      uint64_t v = lane == 0 ? (uint64_t)Pw[h] : 0ull;
-      for (uint32_t i = lane; i < w; i += 32) v += node_value(f[i]);
+    // Flat chunks: this lane's share of the sum over the slice ranks of keys in
+    // [lo, hi): every 32nd value of the partial chunks at both ends and every 32nd
+    // chunk total between them (read straight from the shared chunk totals, so no
+    // prefix copy has to be rebuilt after updates).
+    auto key_rank = [&](uint32_t k) -> uint32_t {
+      return k <= klo ? 0u : (k >= khi ? s.n : local_rank(sbits, srl, k - klo));
+    };
+    auto flat_range = [&](uint32_t lo, uint32_t hi) -> uint64_t {
+      const uint32_t ra = key_rank(lo), rb = key_rank(hi);
+      if (rb <= ra) return 0;
+      const uint32_t ha = ra >> kChunkBits, hb = (rb - 1u) >> kChunkBits;
+      const uint32_t ia = ra & (kChunk - 1u), ib = ((rb - 1u) & (kChunk - 1u)) + 1u;   // [ia, kChunk) of ha, [0, ib) of hb
+      const Node* fa = fine + (size_t)ha * kChunkStride;
+      uint64_t v = 0;
+      if (ha == hb) {
+        for (uint32_t i = ia + lane; i < ib; i += 32) v += node_value(fa[i]);
+      } else {
+        const Node* fb = fine + (size_t)hb * kChunkStride;
+        for (uint32_t i = ia + lane; i < (uint32_t)kChunk; i += 32) v += node_value(fa[i]);
+        for (uint32_t c = ha + 1u + lane; c < hb; c += 32) v += node_value(T[c]);
+        for (uint32_t i = lane; i < ib; i += 32) v += node_value(fb[i]);
+      }
       return v;
     };
     // Answer the queries of the lanes with `mine` (warp-uniform call): Fenwick chunks
@@ -1108,7 +1128,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           const int src = __ffs(owners) - 1;
           owners &= owners - 1;
           const uint32_t l = __shfl_sync(0xffffffffu, lo, src), h = __shfl_sync(0xffffffffu, hi, src);
-          uint64_t d = h > l ? flat_part(h) - flat_part(l) : 0ull;
+          uint64_t d = h > l ? flat_range(l, h) : 0ull;
 #pragma unroll
           for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
           if (lane == src) {
@@ -1158,7 +1178,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         return (int64_t)ring[u & M].q0 + (pq0 + g - qpre[u & M]);
       };
       if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
-        if (dirty) {
+        if (!Cfg::kFlat && dirty) {
           rebuild();
           dirty = false;
         }
@@ -1251,7 +1271,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         if (epre[(u + 1) & M] > epre[a & M]) dirty = true;
         if (!has_q) break;
         __syncthreads();  // every update of steps <= u is applied
-        if (dirty) {
+        if (!Cfg::kFlat && dirty) {
           rebuild();
           dirty = false;
         }
@@ -1353,7 +1373,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       };
       if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
         __syncthreads();   // earlier updates applied; this tile's staged events visible
-        if (dirty) {
+        if (!Cfg::kFlat && dirty) {
           rebuild();
           dirty = false;
         }
@@ -1443,7 +1463,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         if (epre[(u + 1) & M] > epre[a & M]) dirty = true;
         if (!has_q) break;
         __syncthreads();  // every update of steps <= u is applied
-        if (dirty) {
+        if (!Cfg::kFlat && dirty) {
           rebuild();
           dirty = false;
         }

@@ -129,8 +129,10 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   const size_t staging = sizeof(StepDesc) * Cfg::kRing + 2 * 8 * (size_t)Cfg::kRing +
                          2 * (size_t)Cfg::kTileEv * 16 + al(2 * (size_t)Cfg::kTileEv) +
                          al(2 * (size_t)Cfg::kTileQ * 12) + al(2 * (size_t)Cfg::kTileQ) + (size_t)kOfflineQ * 8;
-  const size_t fixed = al((size_t)L.ww * 8) + al(((size_t)L.ww + 2) * 4) + staging +
-                       (size_t)Cfg::kWarps * (kMaxChunks + 1) * 8 + 128;
+  // per-warp copies of the chunk-total prefix: Fenwick chunks only (flat chunks
+  // probe the chunk totals directly)
+  const size_t pcopies = Cfg::kFlat ? 0 : (size_t)Cfg::kWarps * (kMaxChunks + 1) * 8;
+  const size_t fixed = al((size_t)L.ww * 8) + al(((size_t)L.ww + 2) * 4) + staging + pcopies + 128;
   const size_t per32 = (size_t)kChunkStride * 4 + 8;  // int32 nodes + chunk total
   int32_t n32 = budget > fixed ? (int32_t)((budget - fixed) / per32) : 0;
   if (n32 > kMaxChunks) n32 = kMaxChunks;
@@ -142,7 +144,7 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   L.off_rl = o;   o = al(o + ((size_t)L.ww + 2) * 4);
   L.off_fine = o; o = al(o + (size_t)n32 * kChunkStride * 4);
   L.off_T = o;    o = al(o + (size_t)n32 * 8);
-  L.off_P = o;    o = al(o + (size_t)Cfg::kWarps * (kMaxChunks + 1) * 8);
+  L.off_P = o;    o = al(o + pcopies);
   L.off_ring = o; o = al(o + sizeof(StepDesc) * Cfg::kRing);
   L.off_epre = o; o = al(o + 8 * (size_t)Cfg::kRing);
   L.off_qpre = o; o = al(o + 8 * (size_t)Cfg::kRing);
