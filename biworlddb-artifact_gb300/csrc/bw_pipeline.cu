@@ -898,10 +898,12 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
 
     // Step ring: descriptors and event/query prefixes of steps [filled - Cfg::kRing, filled);
     // steps past t1 read as empty.  A refill overwrites the oldest Cfg::kRingFill slots;
-    // warp 0 loads them and scans their counts (the running totals live in warp 0).
+    // the last warp (FW) loads them and scans their counts (the running totals live in
+    // that warp).
     int32_t filled = t0;
     int64_t run_e = 0, run_q = 0;
-    // Warp 0 keeps the descriptors of the next refill in registers (loaded one
+    constexpr int FW = Cfg::kWarps - 1;
+    // Warp FW keeps the descriptors of the next refill in registers (loaded one
     // refill ahead), so a refill costs a scan and shared stores, not a global load.
     constexpr int PER = Cfg::kRingFill / 32;
     StepDesc pf[PER];
@@ -913,10 +915,11 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         if (t < t1) pf[j] = p.desc[t];
       }
     };
-    if (warp == 0) prefetch(t0);
-    auto fill = [&]() {
-      __syncthreads();
-      if (warp == 0) {
+    if (warp == FW) prefetch(t0);
+    // Warp FW's part of a refill (the caller keeps readers of the overwritten slots
+    // and of the new ones on the right sides of barriers).
+    auto refill = [&]() {
+      if (warp == FW) {
         int64_t le = 0, lq = 0;
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
@@ -944,6 +947,10 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         prefetch(filled + Cfg::kRingFill);
       }
       filled += Cfg::kRingFill;
+    };
+    auto fill = [&]() {
+      __syncthreads();
+      refill();
       __syncthreads();
     };
     // Tile from step s: as many whole steps (<= kTileSteps) as fit kTileEv events and
@@ -1348,7 +1355,10 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       }
       cp_async_commit();
     };
-    auto process_own = [&](const Tile& x, int buf, const int32_t* own_e, const int32_t* own_q) {
+    // need: ring steps the next make_tile reads (filled must exceed it); the offline
+    // path refills the ring between its two barriers (the overwritten slots hold
+    // steps before x.s, which needs Cfg::kRing >= 3 * kTileSteps + kRingFill).
+    auto process_own = [&](const Tile& x, int buf, const int32_t* own_e, const int32_t* own_q, int32_t need) {
       const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
       const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
       const BwEvent* eb = evbuf + (size_t)buf * Cfg::kTileEv;
@@ -1377,53 +1387,58 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           rebuild();
           dirty = false;
         }
-        // the tile's event/query pairs: query g's events are cut into `parts` ranges
-        // of whole 32-event chunks, one warp per (query, range); each warp sums its
-        // range and adds the sum to corr[g]
-        {
-          const uint8_t* qmt = qmeta + (size_t)buf * Cfg::kTileQ;
-          const int32_t nchunk = (int32_t)((ne + 31) / 32);
-          const int32_t parts = max(1, min(nchunk, Cfg::kWarps / max(1, (int32_t)nq)));
-          const int32_t per = (nchunk + parts - 1) / parts;
-          for (int32_t it = warp; it < (int32_t)nq * parts; it += Cfg::kWarps) {
-            const int32_t g = it / parts, part = it - g * parts;
-            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
-            const uint32_t lo = q[1], hi = q[2];
-            const int32_t urel = qmt[g];
-            const uint32_t a_lo = lo > klo ? lo : klo, a_hi = hi < khi ? hi : khi;
-            if (!s.n || a_lo >= a_hi) continue;
-            uint64_t v = 0;
-            const int64_t i1 = imin64(ne, (int64_t)(part + 1) * per * 32);
-#pragma unroll 4
-            for (int64_t i = (int64_t)part * per * 32 + lane; i < i1; i += 32) {
-              const uint8_t mt = em[i];
-              const BwEvent e = eb[i];
-              if ((int32_t)(mt >> 1) <= urel && e.key >= a_lo && e.key < a_hi)
-                v += (mt & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
-            }
-#pragma unroll
-            for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0 && v) shared_add_u64(corr + g, v);
-          }
-        }
-        __syncthreads();   // every pair summed
+        // Each query's owner warp sums, in one pass with its probe, the tile's events of
+        // the query's own and earlier steps (a prefix of the staged events) whose key
+        // lies in both [lo, hi) and the slice.  Flat chunks fold the probe's partial
+        // sums into the same warp reduction; Fenwick chunks hand the correction to the
+        // owner lane, which probes alone.
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
           const bool mine = own_q[m] >= 0;
           const int64_t g = qslot + m * Cfg::kThreads;
           uint32_t lo = 0, hi = 0;
-          uint64_t acc = 0;
-          int64_t j = 0;
           if (mine) {
             const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
             lo = q[1]; hi = q[2];
-            acc = (uint64_t)corr[g] + (c_hi[m] - c_lo[m]);
-            j = qindex(own_q[m], g);
-            corr[g] = 0;
           }
-          finish_warp(mine, lo, hi, acc, j);
+          uint64_t corr_own = 0;
+          uint32_t owners = __ballot_sync(0xffffffffu, mine && hi > lo);
+          while (owners) {
+            const int src = __ffs(owners) - 1;
+            owners &= owners - 1;
+            const uint32_t l = __shfl_sync(0xffffffffu, lo, src), h = __shfl_sync(0xffffffffu, hi, src);
+            const int32_t ur = __shfl_sync(0xffffffffu, own_q[m], src);
+            const uint32_t a_lo = l > klo ? l : klo, a_hi = h < khi ? h : khi;
+            uint64_t d = 0;
+            if (s.n && a_lo < a_hi) {
+              const int32_t nev = (int32_t)(epre[(x.s + ur + 1) & M] - pe0);   // events of steps <= ur
+#pragma unroll 4
+              for (int32_t i = lane; i < nev; i += 32) {
+                const BwEvent e = eb[i];
+                if (e.key >= a_lo && e.key < a_hi) d += (em[i] & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
+              }
+            }
+            if constexpr (Cfg::kFlat) d += flat_range(l, h);
+#pragma unroll
+            for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+            if (lane == src) corr_own = d;
+          }
+          if (mine) {
+            const int64_t j = qindex(own_q[m], g);
+            int64_t* out = p.answers + j;
+            // (the ring refill below leaves the slots of x's steps alone)
+            if (hi <= lo) {
+              if (first) *out = 0;
+            } else if constexpr (Cfg::kFlat) {
+              const uint64_t a = corr_own + (c_hi[m] - c_lo[m]);
+              *out = first ? (int64_t)a : (int64_t)((uint64_t)*out + a);
+            } else {
+              finish(lo, hi, corr_own + (c_hi[m] - c_lo[m]), j);
+            }
+          }
         }
-        __syncthreads();   // probes done before this tile's updates
+        if (need >= filled) refill();
+        __syncthreads();   // probes done before this tile's updates; refilled ring visible
         if (s.n) {
 #pragma unroll
           for (int m = 0; m < Cfg::kEvPer; ++m) {
@@ -1499,7 +1514,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     };
 
     if constexpr (Cfg::kCoop) {
-      fill();
+      while (min(t0 + Cfg::kTileSteps, t1) + 1 > filled) fill();
       Tile cur = make_tile(t0);
       stage(cur, 0);
       int buf = 0;
@@ -1511,7 +1526,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         nxt.s = nxt.e = t1;
         nxt.qmask = 0;
         if (ns < t1) {
-          if (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
+          while (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
           nxt = make_tile(ns);
           stage(nxt, buf ^ 1);
         }
@@ -1521,7 +1536,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         buf ^= 1;
       }
     } else {
-      fill();
+      while (min(t0 + Cfg::kTileSteps, t1) + 1 > filled) fill();
       Tile cur = make_tile(t0);
       int32_t cur_e[Cfg::kEvPer], cur_q[Cfg::kQPer];
       stage_own(cur, 0, cur_e, cur_q);
@@ -1531,7 +1546,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         Tile nxt;
         int32_t nxt_e[Cfg::kEvPer], nxt_q[Cfg::kQPer];
         if (ns < t1) {
-          if (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
+          while (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
           nxt = make_tile(ns);
           stage_own(nxt, buf ^ 1, nxt_e, nxt_q);
         } else {
@@ -1540,7 +1555,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           cp_async_commit();
         }
         cp_async_wait<1>();   // this thread's copies of the current tile have landed
-        process_own(cur, buf, cur_e, cur_q);
+        process_own(cur, buf, cur_e, cur_q, nxt.e < t1 ? min(nxt.e + Cfg::kTileSteps, t1) : -1);
         if (ns >= t1) break;
         cur = nxt;
   #pragma unroll

@@ -51,7 +51,8 @@ constexpr int kOfflineQ = 128;                // and at most this many queries (
 
 // Sweep tile geometry: THREADS per CTA, EV events and QP queries staged per thread
 // per tile, at most STEPS steps per tile, a ring of RING step descriptors refilled
-// RING/2 at a time (the ring must hold two tiles plus a refill: RING >= 4 * STEPS).
+// RING/4 at a time (a refill during a tile's probes keeps the slots of that tile
+// and the next two: RING >= 3 * STEPS + RING/4, i.e. RING >= 4 * STEPS).
 // COOP: the tile is staged cooperatively and made visible by a barrier (suits many
 // small steps); otherwise every thread stages the items it will apply and probe
 // itself and waits for its own copies only (suits few large, query-heavy steps).
@@ -62,7 +63,7 @@ constexpr int kOfflineQ = 128;                // and at most this many queries (
 template <int EV, int QP, int STEPS, int RING, int THREADS, bool COOP, bool FLAT>
 struct TileCfg {
   static constexpr bool kCoop = COOP, kFlat = FLAT;
-  static constexpr int kEvPer = EV, kQPer = QP, kTileSteps = STEPS, kRing = RING, kRingFill = RING / 2;
+  static constexpr int kEvPer = EV, kQPer = QP, kTileSteps = STEPS, kRing = RING, kRingFill = RING / 4;
   static constexpr int kThreads = THREADS, kWarps = THREADS / 32, kMinBlocks = THREADS >= 512 ? 1 : 2;
   static constexpr int kTileEv = EV * THREADS, kTileQ = QP * THREADS;
   static_assert(RING >= 4 * STEPS && STEPS <= 64 && kRingFill % 32 == 0, "tile ring too small");
