@@ -837,11 +837,22 @@ __device__ __forceinline__ uint64_t slice_prefix2(const Node* fine, const unsign
 }
 
 // A tile: steps [s, e) whose events (up to kTileEv, in step order) and queries (up
-// to kTileQ) are staged together; bit i of qmask marks step s + i as a query step.
+// to kTileQ) are staged together; bit i of qm[i / 64] marks step s + i as a query
+// step (tiles span at most 128 steps).
 struct Tile {
   int32_t s, e;
-  uint64_t qmask;
+  uint64_t qm[2];
+  __device__ __forceinline__ bool any_query() const { return (qm[0] | qm[1]) != 0; }
+  __device__ __forceinline__ void clear() { qm[0] = qm[1] = 0; }
 };
+// Query steps of a tile in order: the next one's offset from the tile start (the
+// masks must not both be empty), and removing it.
+__device__ __forceinline__ int32_t next_query_step(const uint64_t* qm) {
+  return qm[0] ? __ffsll((long long)qm[0]) - 1 : 64 + __ffsll((long long)qm[1]) - 1;
+}
+__device__ __forceinline__ void pop_query_step(uint64_t* qm) {
+  if (qm[0]) qm[0] &= qm[0] - 1; else qm[1] &= qm[1] - 1;
+}
 
 template <typename Node, typename Cfg>
 __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLayout& L, unsigned char* smem,
@@ -852,6 +863,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
   Node* fine = reinterpret_cast<Node*>(smem + L.off_fine);
   Node* T = reinterpret_cast<Node*>(smem + L.off_T);   // chunk totals
   StepDesc* ring = reinterpret_cast<StepDesc*>(smem + L.off_ring);
+  StepDesc* pdesc = reinterpret_cast<StepDesc*>(smem + L.off_pdesc);   // [Cfg::kRingFill] next refill
   int64_t* epre = reinterpret_cast<int64_t*>(smem + L.off_epre);   // events before step, per ring slot
   int64_t* qpre = reinterpret_cast<int64_t*>(smem + L.off_qpre);   // queries before step, per ring slot
   BwEvent* evbuf = reinterpret_cast<BwEvent*>(smem + L.off_ev);     // [2][Cfg::kTileEv]
@@ -903,28 +915,38 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     int32_t filled = t0;
     int64_t run_e = 0, run_q = 0;
     constexpr int FW = Cfg::kWarps - 1;
-    // Warp FW keeps the descriptors of the next refill in registers (loaded one
-    // refill ahead), so a refill costs a scan and shared stores, not a global load.
+    // Warp FW copies the descriptors of the next refill into shared memory (cp.async,
+    // one refill ahead), so a refill costs a scan and shared stores, not a global load.
     constexpr int PER = Cfg::kRingFill / 32;
-    StepDesc pf[PER];
     auto prefetch = [&](int32_t from) {
-#pragma unroll
-      for (int j = 0; j < PER; ++j) {
-        const int32_t t = from + lane * PER + j;
-        pf[j].e0 = 0; pf[j].q0 = 0; pf[j].ne = 0; pf[j].nq = 0;
-        if (t < t1) pf[j] = p.desc[t];
+      for (int i = lane; i < Cfg::kRingFill; i += 32) {
+        const int32_t t = from + i;
+        if (t < t1) {
+          cp_async16(pdesc + i, p.desc + t);
+        } else {
+          StepDesc z;
+          z.e0 = 0; z.q0 = 0; z.ne = 0; z.nq = 0;
+          pdesc[i] = z;
+        }
       }
+      cp_async_commit();
     };
     if (warp == FW) prefetch(t0);
     // Warp FW's part of a refill (the caller keeps readers of the overwritten slots
     // and of the new ones on the right sides of barriers).
     auto refill = [&]() {
       if (warp == FW) {
+        cp_async_wait<0>();   // this warp's descriptor copies (and its own tile copies)
+        __syncwarp();
+        // lane takes descriptors [lane * PER, (lane + 1) * PER): sums, warp scan, then
+        // a second pass over the staged copies writes the ring slots and prefixes
+        const StepDesc* mine = pdesc + lane * PER;
         int64_t le = 0, lq = 0;
 #pragma unroll
         for (int j = 0; j < PER; ++j) {
-          le += pf[j].ne;
-          lq += pf[j].nq > 0 ? pf[j].nq : 0;
+          const int32_t ne = mine[j].ne, nq = mine[j].nq;
+          le += ne;
+          lq += nq > 0 ? nq : 0;
         }
         int64_t ie = le, iq = lq;
 #pragma unroll
@@ -933,17 +955,19 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           if (lane >= o) { ie += ye; iq += yq; }
         }
         int64_t xe = run_e + ie - le, xq = run_q + iq - lq;
-#pragma unroll
+#pragma unroll 2
         for (int j = 0; j < PER; ++j) {
+          const StepDesc d = mine[j];
           const int32_t sl = (filled + lane * PER + j) & M;
-          ring[sl] = pf[j];
+          ring[sl] = d;
           epre[sl] = xe;
           qpre[sl] = xq;
-          xe += pf[j].ne;
-          xq += pf[j].nq > 0 ? pf[j].nq : 0;
+          xe += d.ne;
+          xq += d.nq > 0 ? d.nq : 0;
         }
         run_e += __shfl_sync(0xffffffffu, ie, 31);
         run_q += __shfl_sync(0xffffffffu, iq, 31);
+        __syncwarp();   // every lane has read the staged descriptors
         prefetch(filled + Cfg::kRingFill);
       }
       filled += Cfg::kRingFill;
@@ -955,21 +979,29 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     };
     // Tile from step s: as many whole steps (<= kTileSteps) as fit kTileEv events and
     // kTileQ queries, at least one.  The fit is monotone in the end step, so each
-    // warp counts it with two ballots; every warp computes the same tile.
+    // warp counts it with one ballot per 32 candidate ends; every warp computes the
+    // same tile.
     auto make_tile = [&](int32_t st) -> Tile {
+      constexpr int NB = (Cfg::kTileSteps + 31) / 32;
       const int32_t emax = min(st + Cfg::kTileSteps, t1);
       const int64_t le = epre[st & M] + Cfg::kTileEv, lq = qpre[st & M] + Cfg::kTileQ;
-      const int32_t ea = st + 1 + lane, eb2 = st + 33 + lane;
-      const bool oka = ea <= emax && epre[ea & M] <= le && qpre[ea & M] <= lq;
-      const bool okb = eb2 <= emax && epre[eb2 & M] <= le && qpre[eb2 & M] <= lq;
-      int32_t e = st + __popc(__ballot_sync(0xffffffffu, oka)) + __popc(__ballot_sync(0xffffffffu, okb));
+      int32_t e = st;
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const int32_t ea = st + 1 + 32 * j + lane;
+        const bool ok = ea <= emax && epre[ea & M] <= le && qpre[ea & M] <= lq;
+        e += __popc(__ballot_sync(0xffffffffu, ok));
+      }
       if (e == st) e = st + 1;
       Tile x;
       x.s = st;
       x.e = e;
-      const bool qa = st + lane < x.e && ring[(st + lane) & M].nq > 0;
-      const bool qb = st + 32 + lane < x.e && ring[(st + 32 + lane) & M].nq > 0;
-      x.qmask = (uint64_t)__ballot_sync(0xffffffffu, qa) | ((uint64_t)__ballot_sync(0xffffffffu, qb) << 32);
+      x.clear();
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const bool q = st + 32 * j + lane < x.e && ring[(st + 32 * j + lane) & M].nq > 0;
+        x.qm[j >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, q) << (32 * (j & 1));
+      }
       return x;
     };
     // Stage a tile cooperatively: the first half of the warps copy (cp.async) the
@@ -1184,7 +1216,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         const int32_t u = x.s + urel;
         return (int64_t)ring[u & M].q0 + (pq0 + g - qpre[u & M]);
       };
-      if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
+      if (x.any_query() && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
         if (!Cfg::kFlat && dirty) {
           rebuild();
           dirty = false;
@@ -1249,10 +1281,10 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       }
       uint32_t done = 0;         // staged slots tid + 256 m applied so far
       int32_t a = x.s;           // first step of the current segment
-      uint64_t qm = x.qmask;
+      uint64_t qm[2] = {x.qm[0], x.qm[1]};
       for (;;) {
-        const bool has_q = qm != 0;
-        const int32_t u = has_q ? x.s + __ffsll((long long)qm) - 1 : x.e - 1;
+        const bool has_q = (qm[0] | qm[1]) != 0;
+        const int32_t u = has_q ? x.s + next_query_step(qm) : x.e - 1;
         const int32_t urel = u - x.s;
         if (s.n) {
 #pragma unroll
@@ -1309,7 +1341,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           }
         }
         __syncthreads();  // probes done before the next updates
-        qm &= qm - 1;
+        pop_query_step(qm);
         a = u + 1;
       }
     };
@@ -1381,7 +1413,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         const int32_t u = x.s + urel;
         return (int64_t)ring[u & M].q0 + (pq0 + g - qpre[u & M]);
       };
-      if (x.qmask != 0 && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
+      if (x.any_query() && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
         __syncthreads();   // earlier updates applied; this tile's staged events visible
         if (!Cfg::kFlat && dirty) {
           rebuild();
@@ -1453,10 +1485,10 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       }
       uint32_t done = 0;         // own staged events applied so far
       int32_t a = x.s;           // first step of the current segment
-      uint64_t qm = x.qmask;
+      uint64_t qm[2] = {x.qm[0], x.qm[1]};
       for (;;) {
-        const bool has_q = qm != 0;
-        const int32_t u = has_q ? x.s + __ffsll((long long)qm) - 1 : x.e - 1;
+        const bool has_q = (qm[0] | qm[1]) != 0;
+        const int32_t u = has_q ? x.s + next_query_step(qm) : x.e - 1;
         const int32_t urel = u - x.s;
         if (s.n) {
 #pragma unroll
@@ -1508,7 +1540,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           }
         }
         __syncthreads();  // probes done before the next updates
-        qm &= qm - 1;
+        pop_query_step(qm);
         a = u + 1;
       }
     };
@@ -1524,7 +1556,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         const int32_t ns = cur.e;
         Tile nxt;
         nxt.s = nxt.e = t1;
-        nxt.qmask = 0;
+        nxt.clear();
         if (ns < t1) {
           while (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
           nxt = make_tile(ns);
@@ -1551,7 +1583,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           stage_own(nxt, buf ^ 1, nxt_e, nxt_q);
         } else {
           nxt.s = nxt.e = t1;
-          nxt.qmask = 0;
+          nxt.clear();
           cp_async_commit();
         }
         cp_async_wait<1>();   // this thread's copies of the current tile have landed

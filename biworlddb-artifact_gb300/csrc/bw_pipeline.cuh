@@ -51,8 +51,8 @@ constexpr int kOfflineQ = 128;                // and at most this many queries (
 
 // Sweep tile geometry: THREADS per CTA, EV events and QP queries staged per thread
 // per tile, at most STEPS steps per tile, a ring of RING step descriptors refilled
-// RING/4 at a time (a refill during a tile's probes keeps the slots of that tile
-// and the next two: RING >= 3 * STEPS + RING/4, i.e. RING >= 4 * STEPS).
+// RING - 3 * STEPS (rounded down to whole warps) at a time: a refill during a tile's
+// probes keeps the slots of that tile and the next two.
 // COOP: the tile is staged cooperatively and made visible by a barrier (suits many
 // small steps); otherwise every thread stages the items it will apply and probe
 // itself and waits for its own copies only (suits few large, query-heavy steps).
@@ -63,14 +63,16 @@ constexpr int kOfflineQ = 128;                // and at most this many queries (
 template <int EV, int QP, int STEPS, int RING, int THREADS, bool COOP, bool FLAT>
 struct TileCfg {
   static constexpr bool kCoop = COOP, kFlat = FLAT;
-  static constexpr int kEvPer = EV, kQPer = QP, kTileSteps = STEPS, kRing = RING, kRingFill = RING / 4;
+  static constexpr int kEvPer = EV, kQPer = QP, kTileSteps = STEPS, kRing = RING,
+                       kRingFill = (RING - 3 * STEPS) / 32 * 32;
   static constexpr int kThreads = THREADS, kWarps = THREADS / 32, kMinBlocks = THREADS >= 512 ? 1 : 2;
   static constexpr int kTileEv = EV * THREADS, kTileQ = QP * THREADS;
-  static_assert(RING >= 4 * STEPS && STEPS <= 64 && kRingFill % 32 == 0, "tile ring too small");
+  static_assert((RING & (RING - 1)) == 0 && kRingFill >= STEPS && STEPS <= 128 && STEPS % 32 == 0,
+                "tile ring too small");
 };
 using TileNarrow = TileCfg<2, 2, 32, 128, 256, false, false>;      // query-heavy steps: small staging, Fenwick
 using TileWide = TileCfg<4, 1, 64, 256, 256, true, true>;          // event-heavy steps: deep staging, flat
-using TileNarrow512 = TileCfg<1, 1, 64, 256, 512, false, true>;    // 16 warps (one CTA per SM), own staging, flat
+using TileNarrow512 = TileCfg<1, 1, 64, 512, 512, false, true>;    // 16 warps (one CTA per SM), own staging, flat
 using TileWide512 = TileCfg<2, 1, 64, 256, 512, true, true>;
 enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4 };
 
@@ -120,14 +122,15 @@ struct SweepLayout {
   int32_t ww;
   int32_t nch32, nch64;
   uint32_t cap32, cap64;
-  size_t off_rl, off_fine, off_T, off_P, off_ring, off_epre, off_qpre, off_ev, off_emeta, off_q, off_qmeta, off_corr, bytes;
+  size_t off_rl, off_fine, off_T, off_P, off_ring, off_pdesc, off_epre, off_qpre, off_ev, off_emeta, off_q, off_qmeta,
+      off_corr, bytes;
 };
 template <typename Cfg>
 __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budget) {
   SweepLayout L;
   L.ww = nwords < kWinWords ? nwords : kWinWords;
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
-  const size_t staging = sizeof(StepDesc) * Cfg::kRing + 2 * 8 * (size_t)Cfg::kRing +
+  const size_t staging = sizeof(StepDesc) * (Cfg::kRing + Cfg::kRingFill) + 2 * 8 * (size_t)Cfg::kRing +
                          2 * (size_t)Cfg::kTileEv * 16 + al(2 * (size_t)Cfg::kTileEv) +
                          al(2 * (size_t)Cfg::kTileQ * 12) + al(2 * (size_t)Cfg::kTileQ) + (size_t)kOfflineQ * 8;
   // per-warp copies of the chunk-total prefix: Fenwick chunks only (flat chunks
@@ -147,6 +150,7 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   L.off_T = o;    o = al(o + (size_t)n32 * 8);
   L.off_P = o;    o = al(o + pcopies);
   L.off_ring = o; o = al(o + sizeof(StepDesc) * Cfg::kRing);
+  L.off_pdesc = o; o = al(o + sizeof(StepDesc) * Cfg::kRingFill);
   L.off_epre = o; o = al(o + 8 * (size_t)Cfg::kRing);
   L.off_qpre = o; o = al(o + 8 * (size_t)Cfg::kRing);
   L.off_ev = o;   o = al(o + 2 * (size_t)Cfg::kTileEv * 16);
