@@ -747,6 +747,8 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+// Commit this thread's uncommitted copies and wait for all of its copies.
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Point update of one chunk: the Fenwick nodes above local index l (l in
 // 1..kChunk, stopping below the chunk top, at most kChunkLevels nodes) and the
@@ -916,7 +918,8 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     int64_t run_e = 0, run_q = 0;
     constexpr int FW = Cfg::kWarps - 1;
     // Warp FW copies the descriptors of the next refill into shared memory (cp.async,
-    // one refill ahead), so a refill costs a scan and shared stores, not a global load.
+    // one refill ahead; the copies join the warp's next commit group), so a refill
+    // costs a scan and shared stores, not a global load.
     constexpr int PER = Cfg::kRingFill / 32;
     auto prefetch = [&](int32_t from) {
       for (int i = lane; i < Cfg::kRingFill; i += 32) {
@@ -929,14 +932,13 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           pdesc[i] = z;
         }
       }
-      cp_async_commit();
     };
     if (warp == FW) prefetch(t0);
     // Warp FW's part of a refill (the caller keeps readers of the overwritten slots
     // and of the new ones on the right sides of barriers).
     auto refill = [&]() {
       if (warp == FW) {
-        cp_async_wait<0>();   // this warp's descriptor copies (and its own tile copies)
+        cp_async_wait_all();   // this warp's descriptor copies (and its own tile copies)
         __syncwarp();
         // lane takes descriptors [lane * PER, (lane + 1) * PER): sums, warp scan, then
         // a second pass over the staged copies writes the ring slots and prefixes
@@ -969,6 +971,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         run_q += __shfl_sync(0xffffffffu, iq, 31);
         __syncwarp();   // every lane has read the staged descriptors
         prefetch(filled + Cfg::kRingFill);
+        __syncwarp();   // the new slots are visible to the warp's other lanes
       }
       filled += Cfg::kRingFill;
     };
@@ -986,10 +989,20 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       const int32_t emax = min(st + Cfg::kTileSteps, t1);
       const int64_t le = epre[st & M] + Cfg::kTileEv, lq = qpre[st & M] + Cfg::kTileQ;
       int32_t e = st;
+      int64_t qe[NB];   // query prefix after step st + 32 j + lane
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
         const int32_t ea = st + 1 + 32 * j + lane;
-        const bool ok = ea <= emax && epre[ea & M] <= le && qpre[ea & M] <= lq;
+        qe[j] = qpre[ea & M];
+        bool ok = ea <= emax && epre[ea & M] <= le && qe[j] <= lq;
+        if constexpr (Cfg::kFlat) {
+          // and within the single-probe limits (queries x events), so that a tile is
+          // replayed with one probe phase unless one step alone exceeds them
+          if (ok) {
+            const int64_t nqx = qpre[ea & M] - qpre[st & M], nex = epre[ea & M] - epre[st & M];
+            ok = nqx <= kOfflineQ && nqx * nex <= kOfflinePairs;
+          }
+        }
         e += __popc(__ballot_sync(0xffffffffu, ok));
       }
       if (e == st) e = st + 1;
@@ -997,9 +1010,14 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       x.s = st;
       x.e = e;
       x.clear();
+      // step u answers queries exactly when the query prefix grows across it
+      int64_t before = qpre[st & M];
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
-        const bool q = st + 32 * j + lane < x.e && ring[(st + 32 * j + lane) & M].nq > 0;
+        int64_t qb = __shfl_up_sync(0xffffffffu, qe[j], 1);
+        if (lane == 0) qb = before;
+        before = __shfl_sync(0xffffffffu, qe[j], 31);
+        const bool q = st + 32 * j + lane < x.e && qe[j] > qb;
         x.qm[j >> 1] |= (uint64_t)__ballot_sync(0xffffffffu, q) << (32 * (j & 1));
       }
       return x;
@@ -1083,6 +1101,81 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       }
       cp_async_commit();
     };
+    // Stage a tile with one warp (the staging warp of a specialised tile): events,
+    // then queries, 32 steps at a time; lane l decodes step l of the group, small
+    // steps are copied lane by lane, large ones by lanes taking consecutive flattened
+    // items.  The caller commits the copies.
+    auto stage_warp = [&](const Tile& x, int buf) {
+      BwEvent* eb = evbuf + (size_t)buf * Cfg::kTileEv;
+      uint8_t* em = emeta + (size_t)buf * Cfg::kTileEv;
+      unsigned char* qb = qbuf + (size_t)buf * Cfg::kTileQ * 12;
+      uint8_t* qmt = qmeta + (size_t)buf * Cfg::kTileQ;
+#pragma unroll 1
+      for (int pass = 0; pass < 2; ++pass) {
+        const bool evw = pass == 0;
+        const int64_t p0 = evw ? epre[x.s & M] : qpre[x.s & M];
+        const int64_t cap = evw ? Cfg::kTileEv : Cfg::kTileQ;
+        if ((evw ? epre[x.e & M] : qpre[x.e & M]) == p0) continue;   // nothing of this kind
+        for (int32_t c = x.s; c < x.e; c += 32) {
+          const int32_t st = c + lane;
+          int32_t cnt = 0;
+          int64_t src = 0, f = 0;
+          uint8_t meta = 0;
+          if (st < x.e) {
+            const StepDesc d = ring[st & M];
+            f = (evw ? epre[st & M] : qpre[st & M]) - p0;
+            const int64_t n = evw ? d.ne : (d.nq > 0 ? d.nq : 0);
+            cnt = (int32_t)imin64(n, cap - f > 0 ? cap - f : 0);
+            src = evw ? (int64_t)d.e0 : (int64_t)d.q0;
+            meta = evw ? (uint8_t)(((st - x.s) << 1) | (d.nq < 0 ? 1 : 0)) : (uint8_t)(st - x.s);
+          }
+          int32_t most = cnt;
+#pragma unroll
+          for (int o = 16; o; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
+          auto put = [&](int64_t fpos, int64_t from, uint8_t mt) {
+            if (evw) {
+              cp_async16(eb + fpos, p.ev + from);
+              em[fpos] = mt;
+            } else {
+              const uint32_t* q = reinterpret_cast<const uint32_t*>(p.qs + from);
+              unsigned char* dq = qb + (size_t)fpos * 12;
+              cp_async4(dq, q);
+              cp_async4(dq + 4, q + 1);
+              cp_async4(dq + 8, q + 2);
+              qmt[fpos] = mt;
+            }
+          };
+          if (most <= 16) {
+            for (int32_t i = 0; i < most; ++i)
+              if (i < cnt) put(f + i, src + i, meta);
+          } else {
+            int32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+              if (lane >= o) incl += y;
+            }
+            const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            for (int32_t g0 = 0; g0 < total; g0 += 32) {
+              const int32_t g = g0 + lane;
+              int32_t lo = 0, hi = 31;   // first lane whose inclusive count exceeds g
+#pragma unroll
+              for (int it = 0; it < 5; ++it) {
+                const int32_t mid = (lo + hi) >> 1;
+                if (__shfl_sync(0xffffffffu, incl, mid) > g) hi = mid; else lo = mid + 1;
+              }
+              const int32_t s_incl = __shfl_sync(0xffffffffu, incl, lo), s_cnt = __shfl_sync(0xffffffffu, cnt, lo);
+              const int64_t s_src = __shfl_sync(0xffffffffu, src, lo), s_f = __shfl_sync(0xffffffffu, f, lo);
+              const uint8_t s_meta = (uint8_t)__shfl_sync(0xffffffffu, (uint32_t)meta, lo);
+              if (g < total) {
+                const int32_t off = g - (s_incl - s_cnt);
+                put(s_f + off, s_src + off, s_meta);
+              }
+            }
+          }
+        }
+      }
+    };
     auto apply = [&](uint32_t k, uint64_t v, bool neg) {
       if (k >= klo && k < khi) {
         if (neg) v = (uint64_t)0 - v;
@@ -1139,22 +1232,35 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     auto key_rank = [&](uint32_t k) -> uint32_t {
       return k <= klo ? 0u : (k >= khi ? s.n : local_rank(sbits, srl, k - klo));
     };
-    auto flat_range = [&](uint32_t lo, uint32_t hi) -> uint64_t {
+    // Lane partial sums are kept in the node type: an int32 block's every partial
+    // sum fits int32 (its applied |delta| sum is below 2^31), so 32-bit wrapping
+    // arithmetic and one warp reduction give the exact value, sign-extended after.
+    auto flat_range = [&](uint32_t lo, uint32_t hi) -> Node {
       const uint32_t ra = key_rank(lo), rb = key_rank(hi);
       if (rb <= ra) return 0;
       const uint32_t ha = ra >> kChunkBits, hb = (rb - 1u) >> kChunkBits;
       const uint32_t ia = ra & (kChunk - 1u), ib = ((rb - 1u) & (kChunk - 1u)) + 1u;   // [ia, kChunk) of ha, [0, ib) of hb
       const Node* fa = fine + (size_t)ha * kChunkStride;
-      uint64_t v = 0;
+      Node v = 0;
       if (ha == hb) {
-        for (uint32_t i = ia + lane; i < ib; i += 32) v += node_value(fa[i]);
+        for (uint32_t i = ia + lane; i < ib; i += 32) v += fa[i];
       } else {
         const Node* fb = fine + (size_t)hb * kChunkStride;
-        for (uint32_t i = ia + lane; i < (uint32_t)kChunk; i += 32) v += node_value(fa[i]);
-        for (uint32_t c = ha + 1u + lane; c < hb; c += 32) v += node_value(T[c]);
-        for (uint32_t i = lane; i < ib; i += 32) v += node_value(fb[i]);
+        for (uint32_t i = ia + lane; i < (uint32_t)kChunk; i += 32) v += fa[i];
+        for (uint32_t c = ha + 1u + lane; c < hb; c += 32) v += T[c];
+        for (uint32_t i = lane; i < ib; i += 32) v += fb[i];
       }
       return v;
+    };
+    auto warp_sum = [&](Node v) -> uint64_t {
+      if constexpr (sizeof(Node) == 4) {
+        return (uint64_t)(int64_t)(int32_t)__reduce_add_sync(0xffffffffu, v);
+      } else {
+        uint64_t d = v;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        return d;
+      }
     };
     // Answer the queries of the lanes with `mine` (warp-uniform call): Fenwick chunks
     // let each owner finish alone; flat chunks sum the chunk's values with the warp.
@@ -1167,9 +1273,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           const int src = __ffs(owners) - 1;
           owners &= owners - 1;
           const uint32_t l = __shfl_sync(0xffffffffu, lo, src), h = __shfl_sync(0xffffffffu, hi, src);
-          uint64_t d = h > l ? flat_range(l, h) : 0ull;
-#pragma unroll
-          for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+          const uint64_t d = warp_sum(h > l ? flat_range(l, h) : Node(0));
           if (lane == src) {
             int64_t* out = p.answers + j;
             if (hi <= lo) {
@@ -1441,19 +1545,18 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
             const uint32_t l = __shfl_sync(0xffffffffu, lo, src), h = __shfl_sync(0xffffffffu, hi, src);
             const int32_t ur = __shfl_sync(0xffffffffu, own_q[m], src);
             const uint32_t a_lo = l > klo ? l : klo, a_hi = h < khi ? h : khi;
-            uint64_t d = 0;
+            Node d = 0;
             if (s.n && a_lo < a_hi) {
               const int32_t nev = (int32_t)(epre[(x.s + ur + 1) & M] - pe0);   // events of steps <= ur
 #pragma unroll 4
               for (int32_t i = lane; i < nev; i += 32) {
                 const BwEvent e = eb[i];
-                if (e.key >= a_lo && e.key < a_hi) d += (em[i] & 1) ? (uint64_t)0 - (uint64_t)e.delta : (uint64_t)e.delta;
+                if (e.key >= a_lo && e.key < a_hi) d += (em[i] & 1) ? Node(0) - (Node)e.delta : (Node)e.delta;
               }
             }
             if constexpr (Cfg::kFlat) d += flat_range(l, h);
-#pragma unroll
-            for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-            if (lane == src) corr_own = d;
+            const uint64_t dsum = warp_sum(d);
+            if (lane == src) corr_own = dsum;
           }
           if (mine) {
             const int64_t j = qindex(own_q[m], g);
@@ -1545,7 +1648,201 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       }
     };
 
-    if constexpr (Cfg::kCoop) {
+    // Specialised tiles: the consumer warps (all but the staging warp FW) replay a
+    // tile staged by FW; consumer-only barriers are named barrier 1.
+    constexpr int kCW = Cfg::kWarps - 1, kCons = kCW * 32;
+    constexpr int kEvPerC = (Cfg::kTileEv + kCons - 1) / kCons, kQPerC = (Cfg::kTileQ + kCons - 1) / kCons;
+    auto cbar = [&]() { asm volatile("bar.sync 1, %0;\n" ::"n"(kCons) : "memory"); };
+    auto process_spec = [&](const Tile& x, int buf) {
+      const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
+      const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
+      const int64_t ns_e = imin64(ne, Cfg::kTileEv), ns_q = imin64(nq, Cfg::kTileQ);
+      const BwEvent* eb = evbuf + (size_t)buf * Cfg::kTileEv;
+      const uint8_t* em = emeta + (size_t)buf * Cfg::kTileEv;
+      const unsigned char* qb = qbuf + (size_t)buf * Cfg::kTileQ * 12;
+      const uint8_t* qmt = qmeta + (size_t)buf * Cfg::kTileQ;
+      const int cslot = lane * kCW + warp;   // consecutive queries go to different warps
+      auto qindex = [&](int32_t urel, int64_t g) -> int64_t {
+        const int32_t u = x.s + urel;
+        return (int64_t)ring[u & M].q0 + (pq0 + g - qpre[u & M]);
+      };
+      if (x.any_query() && ne <= Cfg::kTileEv && nq <= kOfflineQ && nq * ne <= kOfflinePairs) {
+        // one probe phase on the state at the tile start: each query's owner warp sums
+        // the tile's events of the query's own and earlier steps inside [lo, hi) and
+        // the slice together with the probe's partial sums, in one warp reduction
+#pragma unroll
+        for (int m = 0; m < kQPerC; ++m) {
+          const int64_t g = cslot + m * kCons;
+          const bool mine = g < nq;
+          uint32_t lo = 0, hi = 0;
+          int32_t urel = 0;
+          uint64_t c_lo = 0, c_hi = 0;
+          if (mine) {
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
+            lo = q[1]; hi = q[2];
+            urel = qmt[g];
+            if (carried && hi > lo) {
+              c_lo = (uint64_t)__ldg(crow + lo);
+              c_hi = (uint64_t)__ldg(crow + hi);
+            }
+          }
+          uint64_t corr_own = 0;
+          uint32_t owners = __ballot_sync(0xffffffffu, mine && hi > lo);
+          while (owners) {
+            const int src = __ffs(owners) - 1;
+            owners &= owners - 1;
+            const uint32_t l = __shfl_sync(0xffffffffu, lo, src), h = __shfl_sync(0xffffffffu, hi, src);
+            const int32_t ur = __shfl_sync(0xffffffffu, urel, src);
+            const uint32_t a_lo = l > klo ? l : klo, a_hi = h < khi ? h : khi;
+            Node d = 0;
+            if (s.n && a_lo < a_hi) {
+              const int32_t nev = (int32_t)(epre[(x.s + ur + 1) & M] - pe0);   // events of steps <= ur
+#pragma unroll 4
+              for (int32_t i = lane; i < nev; i += 32) {
+                const BwEvent e = eb[i];
+                if (e.key >= a_lo && e.key < a_hi) d += (em[i] & 1) ? Node(0) - (Node)e.delta : (Node)e.delta;
+              }
+            }
+            d += flat_range(l, h);
+            const uint64_t dsum = warp_sum(d);
+            if (lane == src) corr_own = dsum;
+          }
+          if (mine) {
+            int64_t* out = p.answers + qindex(urel, g);
+            if (hi <= lo) {
+              if (first) *out = 0;
+            } else {
+              const uint64_t v = corr_own + (c_hi - c_lo);
+              *out = first ? (int64_t)v : (int64_t)((uint64_t)*out + v);
+            }
+          }
+        }
+        cbar();   // probes done before this tile's updates
+        if (s.n) {
+#pragma unroll
+          for (int m = 0; m < kEvPerC; ++m) {
+            const int64_t g = tid + m * kCons;
+            if (g < ne) {
+              const BwEvent e = eb[g];
+              apply(e.key, (uint64_t)e.delta, em[g] & 1);
+            }
+          }
+        }
+        return;
+      }
+      // Segments of steps ending at each query step: the updates of a segment, a
+      // barrier, the probes of its query step, a barrier (a tile with no query
+      // applies all of its events with no barrier).
+      uint32_t done = 0;
+      int32_t a = x.s;
+      uint64_t qm[2] = {x.qm[0], x.qm[1]};
+      for (;;) {
+        const bool has_q = (qm[0] | qm[1]) != 0;
+        const int32_t u = has_q ? x.s + next_query_step(qm) : x.e - 1;
+        const int32_t urel = u - x.s;
+        if (s.n) {
+#pragma unroll
+          for (int m = 0; m < kEvPerC; ++m) {
+            const int64_t g = tid + m * kCons;
+            if (!(done >> m & 1u) && g < ns_e) {
+              const uint8_t mt = em[g];
+              if ((int32_t)(mt >> 1) <= urel) {
+                const BwEvent e = eb[g];
+                apply(e.key, (uint64_t)e.delta, mt & 1);
+                done |= 1u << m;
+              }
+            }
+          }
+          if (ne > Cfg::kTileEv && a == x.s) {  // one step with more events than a tile stages
+            const StepDesc d = ring[x.s & M];
+            for (int64_t g = Cfg::kTileEv + tid; g < ne; g += kCons) {
+              const BwEvent e = p.ev[(int64_t)d.e0 + g];
+              apply(e.key, (uint64_t)e.delta, d.nq < 0);
+            }
+          }
+        }
+        if (!has_q) break;
+        cbar();  // every update of steps <= u is applied
+#pragma unroll
+        for (int m = 0; m < kQPerC; ++m) {
+          const int64_t g = cslot + m * kCons;
+          const bool mine = g < ns_q && (int32_t)qmt[g] == urel;
+          uint32_t lo = 0, hi = 0;
+          uint64_t acc = 0;
+          if (mine) {
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(qb + (size_t)g * 12);
+            lo = q[1]; hi = q[2];
+            if (carried && hi > lo) acc = (uint64_t)__ldg(crow + hi) - (uint64_t)__ldg(crow + lo);
+          }
+          finish_warp(mine, lo, hi, acc, mine ? qindex(urel, g) : 0);
+        }
+        if (nq > Cfg::kTileQ) {  // one step with more queries than a tile stages
+          const int64_t qbase = qindex(urel, 0);
+          for (int64_t g0 = Cfg::kTileQ + (tid & ~31); g0 < nq; g0 += kCons) {   // warp-uniform
+            const int64_t g = g0 + lane;
+            const bool mine = g < nq;
+            BwQuery qq;
+            qq.lo = qq.hi = 0;
+            uint64_t acc = 0;
+            if (mine) {
+              qq = p.qs[qbase + g];
+              if (carried && qq.hi > qq.lo) acc = (uint64_t)__ldg(crow + qq.hi) - (uint64_t)__ldg(crow + qq.lo);
+            }
+            finish_warp(mine, qq.lo, qq.hi, acc, qbase + g);
+          }
+        }
+        cbar();  // probes done before the next updates
+        pop_query_step(qm);
+        a = u + 1;
+      }
+    };
+
+    if constexpr (Cfg::kSpec) {
+      // Warp FW cuts and stages tile k + 2 while the consumers replay tile k; one CTA
+      // barrier per tile hands tile k over (FW has waited for its copies; the
+      // consumers have finished tile k - 1, whose buffer FW refills next).
+      Tile* tq = reinterpret_cast<Tile*>(smem + L.off_tiles);   // [3] tiles in flight
+      Tile last;
+      last.s = last.e = t1;
+      last.clear();
+      if (warp == FW) {
+        while (min(t0 + Cfg::kTileSteps, t1) + 1 > filled) refill();
+        const Tile a0 = make_tile(t0);
+        stage_warp(a0, 0);
+        cp_async_commit();
+        if (a0.e < t1) {
+          while (min(a0.e + Cfg::kTileSteps, t1) + 1 > filled) refill();
+          last = make_tile(a0.e);
+          stage_warp(last, 1);
+        }
+        cp_async_commit();
+        if (lane == 0) {
+          tq[0] = a0;
+          tq[1] = last;
+        }
+      }
+      for (int32_t k = 0;; ++k) {
+        if (warp == FW) cp_async_wait<1>();   // tile k's copies landed (tile k + 1's may be in flight)
+        __syncthreads();                       // tile k visible; tile k - 1 replayed
+        const Tile x = tq[k % 3];
+        if (x.s >= t1) break;
+        if (warp == FW) {
+          Tile n;
+          n.s = n.e = t1;
+          n.clear();
+          if (last.e < t1) {
+            while (min(last.e + Cfg::kTileSteps, t1) + 1 > filled) refill();
+            n = make_tile(last.e);
+            stage_warp(n, (k + 2) % 3);
+          }
+          cp_async_commit();
+          if (lane == 0) tq[(k + 2) % 3] = n;
+          last = n;
+        } else {
+          process_spec(x, k % 3);
+        }
+      }
+    } else if constexpr (Cfg::kCoop) {
       while (min(t0 + Cfg::kTileSteps, t1) + 1 > filled) fill();
       Tile cur = make_tile(t0);
       stage(cur, 0);
@@ -1625,7 +1922,7 @@ static inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 static size_t sweep_budget(int ctas_per_sm) { return (size_t)(kSmemPerSM / ctas_per_sm) - 3072; }
 
 static void finish_spec(PipeSpec& s, const Tuning& tune) {
-  s.tile = tune.tile >= kTileNarrowId && tune.tile <= kTileWide512Id ? tune.tile
+  s.tile = tune.tile >= kTileNarrowId && tune.tile <= kTileSpec512Id ? tune.tile
            : (s.Q * 8 >= s.E ? kTileNarrowId : kTileWideId);
   if (s.tile >= kTileNarrow512Id) s.ctas_per_sm = 1;   // a 512-thread CTA takes the SM's registers
   const int32_t nw = words_of(s.Cmax);
@@ -1634,6 +1931,7 @@ static void finish_spec(PipeSpec& s, const Tuning& tune) {
     case kTileWideId: s.SL = sweep_layout<TileWide>(nw, bud); break;
     case kTileNarrow512Id: s.SL = sweep_layout<TileNarrow512>(nw, bud); break;
     case kTileWide512Id: s.SL = sweep_layout<TileWide512>(nw, bud); break;
+    case kTileSpec512Id: s.SL = sweep_layout<TileSpec512>(nw, bud); break;
     default: s.SL = sweep_layout<TileNarrow>(nw, bud); break;
   }
   if (tune.slice_ranks > 0) {
@@ -1840,6 +2138,9 @@ static int ensure_attrs() {
   if ((rc = report(cudaFuncSetAttribute(k_sweep<TileNarrow512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         kSmemLimit - 1024), "smem attr")))
     return rc;
+  if ((rc = report(cudaFuncSetAttribute(k_sweep<TileSpec512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kSmemLimit - 1024), "smem attr")))
+    return rc;
   if ((rc = report(cudaFuncSetAttribute(k_sweep<TileWide512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         kSmemLimit - 1024), "smem attr")))
     return rc;
@@ -2007,6 +2308,7 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
         k_sweep<TileNarrow512><<<sgrid, TileNarrow512::kThreads, SL.bytes, st>>>(sp, SL);
         break;
       case kTileWide512Id: k_sweep<TileWide512><<<sgrid, TileWide512::kThreads, SL.bytes, st>>>(sp, SL); break;
+      case kTileSpec512Id: k_sweep<TileSpec512><<<sgrid, TileSpec512::kThreads, SL.bytes, st>>>(sp, SL); break;
       default: k_sweep<TileNarrow><<<sgrid, TileNarrow::kThreads, SL.bytes, st>>>(sp, SL); break;
     }
     if ((rc = chk("k_sweep"))) return rc;

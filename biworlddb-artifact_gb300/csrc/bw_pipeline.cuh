@@ -60,21 +60,28 @@ constexpr int kOfflineQ = 128;                // and at most this many queries (
 // atomics per update, probes summed by a warp: suits few queries per many events);
 // otherwise a Fenwick tree inside every chunk (<= 9 atomics per update, probes by one
 // thread: suits many queries).
-template <int EV, int QP, int STEPS, int RING, int THREADS, bool COOP, bool FLAT>
+// SPEC: warp-specialised: the last warp cuts and stages tiles (ring, tile cut,
+// cp.async of events and queries) two tiles ahead into three buffers while the
+// other warps replay, synchronised by one CTA barrier per tile and a consumer-only
+// named barrier (flat chunks only).
+template <int EV, int QP, int STEPS, int RING, int THREADS, bool COOP, bool FLAT, bool SPEC = false>
 struct TileCfg {
-  static constexpr bool kCoop = COOP, kFlat = FLAT;
+  static constexpr bool kCoop = COOP, kFlat = FLAT, kSpec = SPEC;
+  static constexpr int kBufs = SPEC ? 3 : 2;
   static constexpr int kEvPer = EV, kQPer = QP, kTileSteps = STEPS, kRing = RING,
                        kRingFill = (RING - 3 * STEPS) / 32 * 32;
   static constexpr int kThreads = THREADS, kWarps = THREADS / 32, kMinBlocks = THREADS >= 512 ? 1 : 2;
   static constexpr int kTileEv = EV * THREADS, kTileQ = QP * THREADS;
   static_assert((RING & (RING - 1)) == 0 && kRingFill >= STEPS && STEPS <= 128 && STEPS % 32 == 0,
                 "tile ring too small");
+  static_assert(!SPEC || (FLAT && !COOP && THREADS >= 128), "specialised tiles are flat, own staging");
 };
 using TileNarrow = TileCfg<2, 2, 32, 128, 256, false, false>;      // query-heavy steps: small staging, Fenwick
 using TileWide = TileCfg<4, 1, 64, 256, 256, true, true>;          // event-heavy steps: deep staging, flat
 using TileNarrow512 = TileCfg<1, 1, 64, 512, 512, false, true>;    // 16 warps (one CTA per SM), own staging, flat
 using TileWide512 = TileCfg<2, 1, 64, 256, 512, true, true>;
-enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4 };
+using TileSpec512 = TileCfg<1, 1, 64, 512, 512, false, true, true>;   // 15 replay warps + 1 staging warp
+enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4, kTileSpec512Id = 5 };
 
 // ------------------------------------------------------------------ records
 struct StepDesc {        // one Euler step, 16 bytes
@@ -123,7 +130,7 @@ struct SweepLayout {
   int32_t nch32, nch64;
   uint32_t cap32, cap64;
   size_t off_rl, off_fine, off_T, off_P, off_ring, off_pdesc, off_epre, off_qpre, off_ev, off_emeta, off_q, off_qmeta,
-      off_corr, bytes;
+      off_corr, off_tiles, bytes;
 };
 template <typename Cfg>
 __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budget) {
@@ -131,8 +138,9 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   L.ww = nwords < kWinWords ? nwords : kWinWords;
   auto al = [](size_t x) { return (x + 15) & ~size_t(15); };
   const size_t staging = sizeof(StepDesc) * (Cfg::kRing + Cfg::kRingFill) + 2 * 8 * (size_t)Cfg::kRing +
-                         2 * (size_t)Cfg::kTileEv * 16 + al(2 * (size_t)Cfg::kTileEv) +
-                         al(2 * (size_t)Cfg::kTileQ * 12) + al(2 * (size_t)Cfg::kTileQ) + (size_t)kOfflineQ * 8;
+                         Cfg::kBufs * (size_t)Cfg::kTileEv * 16 + al(Cfg::kBufs * (size_t)Cfg::kTileEv) +
+                         al(Cfg::kBufs * (size_t)Cfg::kTileQ * 12) + al(Cfg::kBufs * (size_t)Cfg::kTileQ) +
+                         (size_t)kOfflineQ * 8 + 3 * 32;
   // per-warp copies of the chunk-total prefix: Fenwick chunks only (flat chunks
   // probe the chunk totals directly)
   const size_t pcopies = Cfg::kFlat ? 0 : (size_t)Cfg::kWarps * (kMaxChunks + 1) * 8;
@@ -153,11 +161,12 @@ __host__ __device__ inline SweepLayout sweep_layout(int32_t nwords, size_t budge
   L.off_pdesc = o; o = al(o + sizeof(StepDesc) * Cfg::kRingFill);
   L.off_epre = o; o = al(o + 8 * (size_t)Cfg::kRing);
   L.off_qpre = o; o = al(o + 8 * (size_t)Cfg::kRing);
-  L.off_ev = o;   o = al(o + 2 * (size_t)Cfg::kTileEv * 16);
-  L.off_emeta = o; o = al(o + 2 * (size_t)Cfg::kTileEv);
-  L.off_q = o;    o = al(o + 2 * (size_t)Cfg::kTileQ * 12);
-  L.off_qmeta = o; o = al(o + 2 * (size_t)Cfg::kTileQ);
+  L.off_ev = o;   o = al(o + Cfg::kBufs * (size_t)Cfg::kTileEv * 16);
+  L.off_emeta = o; o = al(o + Cfg::kBufs * (size_t)Cfg::kTileEv);
+  L.off_q = o;    o = al(o + Cfg::kBufs * (size_t)Cfg::kTileQ * 12);
+  L.off_qmeta = o; o = al(o + Cfg::kBufs * (size_t)Cfg::kTileQ);
   L.off_corr = o; o = al(o + (size_t)kOfflineQ * 8);
+  L.off_tiles = o; o = al(o + 3 * 32);
   L.bytes = o;
   return L;
 }

@@ -205,7 +205,8 @@ typedef struct {
   int32_t tile;         /* sweep tile geometry: 1 narrow (256 threads, 2 events + 2 queries
                            staged per thread, 32 steps), 2 wide (256 threads, 4 events + 1
                            query, 64 steps), 3 and 4 the same tiles on 512 threads (one
-                           CTA per SM); 0 = by the query/event ratio */
+                           CTA per SM), 5 the 512-thread tile with one warp staging
+                           tiles for the other fifteen; 0 = by the query/event ratio */
   int32_t reserved;
 } BwForestTuning;
 

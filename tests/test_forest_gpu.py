@@ -47,6 +47,8 @@ def run_forest(bw, torch, F, tuning=None):
     (7, 50, {"tile": 2, "ctas_per_sm": 1}),              # wide sweep tiles, one CTA per SM
     (8, 40, {"tile": 3}),                                # narrow tiles on 512 threads
     (9, 40, {"tile": 4, "block_work": 65536}),           # wide tiles on 512 threads
+    (10, 40, {"tile": 5}),                               # one staging warp + 15 replay warps
+    (13, 60, {"tile": 5, "block_work": 65536, "slice_ranks": 512}),
 ])
 def test_forest_matches_oracle(bw, torch_cuda, oracle_mod, seed, T, tuning):
     rng = np.random.default_rng(seed)
@@ -56,10 +58,40 @@ def test_forest_matches_oracle(bw, torch_cuda, oracle_mod, seed, T, tuning):
     np.testing.assert_array_equal(got, want)
 
 
-def test_forest_wrapping_deltas(bw, torch_cuda, oracle_mod):
+@pytest.mark.parametrize("tile", [0, 5])
+def test_forest_wrapping_deltas(bw, torch_cuda, oracle_mod, tile):
     rng = np.random.default_rng(11)
     F = make_forest(rng, 30, max_states=800, big=True)
-    np.testing.assert_array_equal(run_forest(bw, torch_cuda, F, {"block_work": 40000}), oracle_mod.ev_forest(*F))
+    np.testing.assert_array_equal(run_forest(bw, torch_cuda, F, {"block_work": 40000, "tile": tile}),
+                                  oracle_mod.ev_forest(*F))
+
+
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
+def test_forest_heavy_states_all_tiles(bw, torch_cuda, oracle_mod, tile):
+    """States with more events and more queries than one sweep tile stages, in
+    query-dense and query-sparse trees, under every tile geometry (single-probe and
+    per-query-step replay, staged and direct reads)."""
+    rng = np.random.default_rng(31 + tile)
+    parents, events, queries, soff, eoff, qoff, keys = [], [], [], [0], [0], [0], []
+    for t in range(6):
+        S, C = int(rng.integers(200, 900)), int(rng.integers(500, 20000))
+        parents.append(evgen.make_tree(S, KINDS[t % len(KINDS)], rng, p_extend=0.9))
+        ecount = rng.poisson(4, S)
+        qcount = rng.poisson(3.0 if t % 2 else 0.2, S)
+        heavy = rng.choice(S, 4, replace=False)
+        ecount[heavy] = rng.integers(600, 3000, heavy.size)
+        qcount[heavy[:2]] = rng.integers(300, 1500, 2)
+        ev = evgen.make_events(S, C, int(ecount.sum()), rng, zipf=1.1)
+        ev["state"] = np.repeat(np.arange(S, dtype=np.uint32), ecount)
+        qs = evgen.make_queries(S, C, int(qcount.sum()), rng)
+        qs["state"] = np.repeat(np.arange(S, dtype=np.uint32), qcount)
+        events.append(ev); queries.append(qs); keys.append(C)
+        soff.append(soff[-1] + S); eoff.append(eoff[-1] + len(ev)); qoff.append(qoff[-1] + len(qs))
+    F = (np.array(soff, np.int64), np.array(eoff, np.int64), np.array(qoff, np.int64),
+         np.array(keys, np.uint32), np.concatenate(parents).astype(np.int32),
+         np.concatenate(events), np.concatenate(queries))
+    got = run_forest(bw, torch_cuda, F, {"tile": tile, "block_work": 30000})
+    np.testing.assert_array_equal(got, oracle_mod.ev_forest(*F))
 
 
 def test_forest_equals_plain_per_tree(bw, torch_cuda):
@@ -137,7 +169,7 @@ def test_forest_shape_errors(bw, torch_cuda):
         bw.Forest([0, 3], [0, 2], [0, 1], [0])           # empty key domain
 
 
-@pytest.mark.parametrize("tuning", [None, {"tile": 3}, {"tile": 4, "block_work": 200000}])
+@pytest.mark.parametrize("tuning", [None, {"tile": 3}, {"tile": 4, "block_work": 200000}, {"tile": 5}])
 def test_one_tree_forest_equals_plain(bw, torch_cuda, tuning):
     """A forest of one tree is the plain replay (its uploaded tables, not the
     plain path's per-launch ones)."""
