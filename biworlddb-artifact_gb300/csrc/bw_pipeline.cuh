@@ -78,7 +78,7 @@ struct TileCfg {
 };
 using TileNarrow = TileCfg<2, 2, 32, 128, 256, false, false>;      // query-heavy steps: small staging, Fenwick
 using TileWide = TileCfg<4, 1, 64, 256, 256, true, true>;          // event-heavy steps: deep staging, flat
-using TileNarrow512 = TileCfg<1, 1, 64, 512, 512, false, true>;    // 16 warps (one CTA per SM), own staging, flat
+using TileNarrow512 = TileCfg<2, 1, 128, 512, 512, false, true>;   // 16 warps (one CTA per SM), own staging, flat
 using TileWide512 = TileCfg<2, 1, 64, 256, 512, true, true>;
 using TileSpec512 = TileCfg<1, 1, 64, 512, 512, false, true, true>;   // 15 replay warps + 1 staging warp
 enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4, kTileSpec512Id = 5 };
