@@ -1241,14 +1241,26 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       const uint32_t ha = ra >> kChunkBits, hb = (rb - 1u) >> kChunkBits;
       const uint32_t ia = ra & (kChunk - 1u), ib = ((rb - 1u) & (kChunk - 1u)) + 1u;   // [ia, kChunk) of ha, [0, ib) of hb
       const Node* fa = fine + (size_t)ha * kChunkStride;
+      // fixed trip counts with predicated loads, so all of a lane's loads issue together
+      const uint32_t enda = ha == hb ? ib : (uint32_t)kChunk;
       Node v = 0;
-      if (ha == hb) {
-        for (uint32_t i = ia + lane; i < ib; i += 32) v += fa[i];
-      } else {
+#pragma unroll
+      for (int t = 0; t < kChunk / 32; ++t) {
+        const uint32_t i = ia + lane + 32u * t;
+        v += i < enda ? fa[i] : Node(0);
+      }
+      if (ha != hb) {
         const Node* fb = fine + (size_t)hb * kChunkStride;
-        for (uint32_t i = ia + lane; i < (uint32_t)kChunk; i += 32) v += fa[i];
-        for (uint32_t c = ha + 1u + lane; c < hb; c += 32) v += T[c];
-        for (uint32_t i = lane; i < ib; i += 32) v += fb[i];
+#pragma unroll
+        for (int t = 0; t < kChunk / 32; ++t) {
+          const uint32_t i = lane + 32u * t;
+          v += i < ib ? fb[i] : Node(0);
+        }
+#pragma unroll
+        for (int t = 0; t < kMaxChunks / 32; ++t) {
+          const uint32_t c = ha + 1u + lane + 32u * t;
+          v += c < hb ? T[c] : Node(0);
+        }
       }
       return v;
     };
@@ -1450,19 +1462,40 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       }
     };
 
+    // Each staged item's step: the last step of the tile starting at or before the
+    // item's flattened position, found for all of the thread's items at once by
+    // binary lifting over the low words of the prefixes (a position inside a tile
+    // is below 2^32, so 32-bit differences are exact).
     auto stage_own = [&](const Tile& x, int buf, int32_t* own_e, int32_t* own_q) {
       const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
       const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
+      const uint32_t* elo = reinterpret_cast<const uint32_t*>(epre);   // low word of slot i at 2 i
+      const uint32_t* qlo = reinterpret_cast<const uint32_t*>(qpre);
+      const uint32_t pe0l = (uint32_t)pe0, pq0l = (uint32_t)pq0;
+      int32_t se[Cfg::kEvPer], sq[Cfg::kQPer];
+#pragma unroll
+      for (int m = 0; m < Cfg::kEvPer; ++m) se[m] = x.s;
+#pragma unroll
+      for (int m = 0; m < Cfg::kQPer; ++m) sq[m] = x.s;
+#pragma unroll
+      for (int b = Cfg::kTileSteps / 2; b; b >>= 1) {
+#pragma unroll
+        for (int m = 0; m < Cfg::kEvPer; ++m) {
+          const int32_t c = se[m] + b;
+          if (c < x.e && elo[2 * (c & M)] - pe0l <= (uint32_t)(tid + m * Cfg::kThreads)) se[m] = c;
+        }
+#pragma unroll
+        for (int m = 0; m < Cfg::kQPer; ++m) {
+          const int32_t c = sq[m] + b;
+          if (c < x.e && qlo[2 * (c & M)] - pq0l <= (uint32_t)(qslot + m * Cfg::kThreads)) sq[m] = c;
+        }
+      }
 #pragma unroll
       for (int m = 0; m < Cfg::kEvPer; ++m) {
         const int64_t g = tid + m * Cfg::kThreads;
         own_e[m] = -1;
         if (g < ne) {
-          int32_t lo = x.s, hi = x.e - 1;
-          while (lo < hi) {
-            const int32_t mid = (lo + hi + 1) >> 1;
-            if (epre[mid & M] - pe0 <= g) lo = mid; else hi = mid - 1;
-          }
+          const int32_t lo = se[m];
           const StepDesc d = ring[lo & M];
           cp_async16(evbuf + (size_t)buf * Cfg::kTileEv + g, p.ev + (int64_t)d.e0 + (pe0 + g - epre[lo & M]));
           own_e[m] = ((lo - x.s) << 1) | (d.nq < 0 ? 1 : 0);
@@ -1474,11 +1507,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         const int64_t g = qslot + m * Cfg::kThreads;
         own_q[m] = -1;
         if (g < nq) {
-          int32_t lo = x.s, hi = x.e - 1;
-          while (lo < hi) {
-            const int32_t mid = (lo + hi + 1) >> 1;
-            if (qpre[mid & M] - pq0 <= g) lo = mid; else hi = mid - 1;
-          }
+          const int32_t lo = sq[m];
           const StepDesc d = ring[lo & M];
           const uint32_t* src = reinterpret_cast<const uint32_t*>(p.qs + (int64_t)d.q0 + (pq0 + g - qpre[lo & M]));
           unsigned char* dq = qbuf + ((size_t)buf * Cfg::kTileQ + g) * 12;
@@ -1494,7 +1523,13 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     // need: ring steps the next make_tile reads (filled must exceed it); the offline
     // path refills the ring between its two barriers (the overwritten slots hold
     // steps before x.s, which needs Cfg::kRing >= 3 * kTileSteps + kRingFill).
-    auto process_own = [&](const Tile& x, int buf, const int32_t* own_e, const int32_t* own_q, int32_t need) {
+    // An offline tile also cuts the tile that starts at `next_end` (the end of the
+    // tile staged next) in its probe phase (warp FW, after the refill) and hands it
+    // over through shared memory.
+    Tile* pre_tile = reinterpret_cast<Tile*>(smem + L.off_tiles);
+    bool have_pre = false;
+    auto process_own = [&](const Tile& x, int buf, const int32_t* own_e, const int32_t* own_q, int32_t next_end) {
+      const int32_t need = next_end < t1 ? min(next_end + Cfg::kTileSteps, t1) : -1;
       const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
       const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
       const BwEvent* eb = evbuf + (size_t)buf * Cfg::kTileEv;
@@ -1573,6 +1608,13 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           }
         }
         if (need >= filled) refill();
+        if (next_end < t1) {
+          if (warp == FW) {
+            const Tile nt = make_tile(next_end);
+            if (lane == 0) *pre_tile = nt;
+          }
+          have_pre = true;
+        }
         __syncthreads();   // probes done before this tile's updates; refilled ring visible
         if (s.n) {
 #pragma unroll
@@ -1876,7 +1918,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         int32_t nxt_e[Cfg::kEvPer], nxt_q[Cfg::kQPer];
         if (ns < t1) {
           while (min(ns + Cfg::kTileSteps, t1) + 1 > filled) fill();
-          nxt = make_tile(ns);
+          nxt = have_pre ? *pre_tile : make_tile(ns);
           stage_own(nxt, buf ^ 1, nxt_e, nxt_q);
         } else {
           nxt.s = nxt.e = t1;
@@ -1884,7 +1926,8 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           cp_async_commit();
         }
         cp_async_wait<1>();   // this thread's copies of the current tile have landed
-        process_own(cur, buf, cur_e, cur_q, nxt.e < t1 ? min(nxt.e + Cfg::kTileSteps, t1) : -1);
+        have_pre = false;
+        process_own(cur, buf, cur_e, cur_q, nxt.e);
         if (ns >= t1) break;
         cur = nxt;
   #pragma unroll
