@@ -1473,10 +1473,14 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       const uint32_t* qlo = reinterpret_cast<const uint32_t*>(qpre);
       const uint32_t pe0l = (uint32_t)pe0, pq0l = (uint32_t)pq0;
       int32_t se[Cfg::kEvPer], sq[Cfg::kQPer];
+      bool wq[Cfg::kQPer];   // this warp holds a query slot of the tile (few warps do)
 #pragma unroll
       for (int m = 0; m < Cfg::kEvPer; ++m) se[m] = x.s;
 #pragma unroll
-      for (int m = 0; m < Cfg::kQPer; ++m) sq[m] = x.s;
+      for (int m = 0; m < Cfg::kQPer; ++m) {
+        sq[m] = x.s;
+        wq[m] = __any_sync(0xffffffffu, (int64_t)(qslot + m * Cfg::kThreads) < nq);
+      }
 #pragma unroll
       for (int b = Cfg::kTileSteps / 2; b; b >>= 1) {
 #pragma unroll
@@ -1487,7 +1491,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
 #pragma unroll
         for (int m = 0; m < Cfg::kQPer; ++m) {
           const int32_t c = sq[m] + b;
-          if (c < x.e && qlo[2 * (c & M)] - pq0l <= (uint32_t)(qslot + m * Cfg::kThreads)) sq[m] = c;
+          if (wq[m] && c < x.e && qlo[2 * (c & M)] - pq0l <= (uint32_t)(qslot + m * Cfg::kThreads)) sq[m] = c;
         }
       }
 #pragma unroll
@@ -1499,7 +1503,6 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           const StepDesc d = ring[lo & M];
           cp_async16(evbuf + (size_t)buf * Cfg::kTileEv + g, p.ev + (int64_t)d.e0 + (pe0 + g - epre[lo & M]));
           own_e[m] = ((lo - x.s) << 1) | (d.nq < 0 ? 1 : 0);
-          emeta[(size_t)buf * Cfg::kTileEv + g] = (uint8_t)own_e[m];
         }
       }
 #pragma unroll
@@ -1533,8 +1536,19 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       const int64_t pe0 = epre[x.s & M], ne = epre[x.e & M] - pe0;
       const int64_t pq0 = qpre[x.s & M], nq = qpre[x.e & M] - pq0;
       const BwEvent* eb = evbuf + (size_t)buf * Cfg::kTileEv;
-      const uint8_t* em = emeta + (size_t)buf * Cfg::kTileEv;
       const unsigned char* qb = qbuf + (size_t)buf * Cfg::kTileQ * 12;
+      // Exit events are negated in place by their own stager once its copies have
+      // landed, so scans and updates read signed deltas (other threads read them only
+      // after the tile's first barrier).
+      {
+        BwEvent* ebw = evbuf + (size_t)buf * Cfg::kTileEv;
+#pragma unroll
+        for (int m = 0; m < Cfg::kEvPer; ++m)
+          if (own_e[m] >= 0 && (own_e[m] & 1)) {
+            int64_t* dp = &ebw[tid + m * Cfg::kThreads].delta;
+            *dp = (int64_t)((uint64_t)0 - (uint64_t)*dp);
+          }
+      }
       uint64_t c_lo[Cfg::kQPer], c_hi[Cfg::kQPer];
 #pragma unroll
       for (int m = 0; m < Cfg::kQPer; ++m) {
@@ -1585,8 +1599,8 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
               const int32_t nev = (int32_t)(epre[(x.s + ur + 1) & M] - pe0);   // events of steps <= ur
 #pragma unroll 4
               for (int32_t i = lane; i < nev; i += 32) {
-                const BwEvent e = eb[i];
-                if (e.key >= a_lo && e.key < a_hi) d += (em[i] & 1) ? Node(0) - (Node)e.delta : (Node)e.delta;
+                const BwEvent e = eb[i];   // signed (exits negated)
+                if (e.key >= a_lo && e.key < a_hi) d += (Node)e.delta;
               }
             }
             if constexpr (Cfg::kFlat) d += flat_range(l, h);
@@ -1621,7 +1635,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           for (int m = 0; m < Cfg::kEvPer; ++m) {
             if (own_e[m] >= 0) {
               const BwEvent e = eb[tid + m * Cfg::kThreads];
-              apply(e.key, (uint64_t)e.delta, own_e[m] & 1);
+              apply(e.key, (uint64_t)e.delta, false);
             }
           }
         }
@@ -1640,7 +1654,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           for (int m = 0; m < Cfg::kEvPer; ++m) {
             if (!(done >> m & 1u) && own_e[m] >= 0 && (own_e[m] >> 1) <= urel) {
               const BwEvent e = eb[tid + m * Cfg::kThreads];
-              apply(e.key, (uint64_t)e.delta, own_e[m] & 1);
+              apply(e.key, (uint64_t)e.delta, false);
               done |= 1u << m;
             }
           }
