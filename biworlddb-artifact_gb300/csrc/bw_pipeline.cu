@@ -119,11 +119,24 @@ __global__ void k_offsets(const void* items, int64_t n, TreeTabs tt, int32_t T, 
   int64_t lo, hi;
   warp_range(n, lo, hi);
   if (lo >= hi) return;
-  // global state of item i (-2: out of its tree, reported by its own lane)
-  auto gstate = [&](int32_t t, int64_t i) -> int64_t {
+  // global state of a tree-local state s of tree t (-2: out of its tree, reported by its own lane)
+  auto gstate_of = [&](int32_t t, uint32_t s) -> int64_t {
     const int32_t s0 = tt.soff[t], ns = tt.soff[t + 1] - s0;
-    const uint32_t s = kEvents ? ev[i].state : qs[i].state;
     return s < (uint32_t)ns ? (int64_t)s0 + s : -2;
+  };
+  auto gstate = [&](int32_t t, int64_t i) -> int64_t { return gstate_of(t, kEvents ? ev[i].state : qs[i].state); };
+  // an item's (state, key) or (state, lo, hi), loaded one iteration ahead so a
+  // warp keeps two record loads in flight
+  struct Rec { uint32_t s, a, b; };
+  auto load = [&](int64_t i) -> Rec {
+    Rec r;
+    if (kEvents) {
+      const uint2 v = __ldg(reinterpret_cast<const uint2*>(ev + i));   // state, key
+      r.s = v.x; r.a = v.y; r.b = 0;
+    } else {
+      r.s = qs[i].state; r.a = qs[i].lo; r.b = qs[i].hi;
+    }
+    return r;
   };
   int64_t gcarry = -1;   // global state of the item before this lane 0's item
   if (lo > 0) {
@@ -132,19 +145,22 @@ __global__ void k_offsets(const void* items, int64_t n, TreeTabs tt, int32_t T, 
     gcarry = __shfl_sync(0xffffffffu, gp, 0);
   }
   int32_t t = T > 1 ? find_tree(toff, T, imin64(lo + lane, n - 1)) : 0;
+  Rec nx = lo + lane < hi ? load(lo + lane) : Rec{0, 0, 0};
   for (int64_t i0 = lo; i0 < hi; i0 += 32) {
     const int64_t i = i0 + lane;
     const bool valid = i < hi;
+    const Rec rc = nx;
+    if (i + 32 < hi) nx = load(i + 32);
     int64_t g = -2;
     if (valid) {
       if (T > 1) t = tree_forward(toff, T, t, i);
       const uint32_t C = tt.C[t];
       if (kEvents) {
-        if (ev[i].key >= C) set_status(status, BW_STATUS_EVENT_KEY_RANGE);
+        if (rc.a >= C) set_status(status, BW_STATUS_EVENT_KEY_RANGE);
       } else {
-        if (qs[i].lo > C || qs[i].hi > C) set_status(status, BW_STATUS_QUERY_RANGE);
+        if (rc.a > C || rc.b > C) set_status(status, BW_STATUS_QUERY_RANGE);
       }
-      g = gstate(t, i);
+      g = gstate_of(t, rc.s);
       if (g == -2) set_status(status, BW_STATUS_STATE_RANGE);
     }
     int64_t gprev = __shfl_up_sync(0xffffffffu, g, 1);
@@ -900,6 +916,14 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
     const uint32_t klo = (uint32_t)s.word_lo << 6;
     const uint32_t khi = (uint32_t)imin64((int64_t)s.word_hi << 6, (int64_t)bt.C);
     const uint32_t nch = (s.n + kChunk - 1) / kChunk;
+    // Flat chunks keep R copies of each chunk total side by side (copy lane % R), so
+    // the lanes of a warp updating the same chunk of a small slice hit different
+    // words; R is the largest power of two <= 8 whose copies fit the totals' space.
+    uint32_t R = 1;
+    if constexpr (Cfg::kFlat) {
+      const uint32_t cap = (uint32_t)((size_t)L.nch32 * 8 / sizeof(Node));
+      while (R < 8 && nch > 0 && 2 * R * nch <= cap) R *= 2;
+    }
     const bool first = si == first_si;
     const bool carried = first && crow != nullptr;
     for (int i = tid; i < nwd; i += Cfg::kThreads) {
@@ -907,7 +931,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
       srl[i] = grl[s.word_lo + i] - s.rank_lo;
     }
     for (uint32_t i = tid; i < nch * kChunkStride; i += Cfg::kThreads) fine[i] = 0;
-    for (uint32_t i = tid; i < nch; i += Cfg::kThreads) T[i] = 0;
+    for (uint32_t i = tid; i < nch * R; i += Cfg::kThreads) T[i] = 0;
     for (int i = tid; i < kOfflineQ; i += Cfg::kThreads) corr[i] = 0;
 
     // Step ring: descriptors and event/query prefixes of steps [filled - Cfg::kRing, filled);
@@ -1181,7 +1205,7 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
         if (neg) v = (uint64_t)0 - v;
         const uint32_t r = local_rank(sbits, srl, k - klo);
         if constexpr (Cfg::kFlat)
-          flat_add<Node>(fine + (size_t)(r >> kChunkBits) * kChunkStride, T + (r >> kChunkBits),
+          flat_add<Node>(fine + (size_t)(r >> kChunkBits) * kChunkStride, T + (r >> kChunkBits) * R + (lane & (R - 1)),
                          r & (kChunk - 1u), v);
         else
           chunk_add<Node>(fine + (size_t)(r >> kChunkBits) * kChunkStride, T + (r >> kChunkBits),
@@ -1256,10 +1280,13 @@ __device__ __forceinline__ void sweep_block(const SweepParams& p, const SweepLay
           const uint32_t i = lane + 32u * t;
           v += i < ib ? fb[i] : Node(0);
         }
+        // the copies of the chunks strictly between: T[(ha + 1) R, hb R), at most
+        // the totals' space (2 kMaxChunks int32 words)
+        const uint32_t c1 = hb * R;
 #pragma unroll
-        for (int t = 0; t < kMaxChunks / 32; ++t) {
-          const uint32_t c = ha + 1u + lane + 32u * t;
-          v += c < hb ? T[c] : Node(0);
+        for (int t = 0; t < 2 * kMaxChunks / 32; ++t) {
+          const uint32_t c = (ha + 1u) * R + lane + 32u * t;
+          v += c < c1 ? T[c] : Node(0);
         }
       }
       return v;
