@@ -315,18 +315,30 @@ __global__ void k_lin_steps(const uint64_t* r, const int64_t* cnt, const int32_t
   int64_t lo, hi;
   warp_range(S, lo, hi);
   int32_t t = T > 1 && lo < hi ? find_tree(tt.soff, T, imin64(lo + (threadIdx.x & 31), S - 1)) : 0;
+  // the state's counters and ranges, loaded one iteration ahead
+  struct Pre { uint64_t c, cp; int64_t e0, e1, q0, q1; };
+  auto load = [&](int32_t v) -> Pre {
+    Pre x;
+    x.c = (uint64_t)cnt[v]; x.cp = v ? (uint64_t)cnt[v - 1] : 0ull;
+    x.e0 = eoff[v]; x.e1 = eoff[v + 1]; x.q0 = qoff[v]; x.q1 = qoff[v + 1];
+    return x;
+  };
+  Pre nx{0, 0, 0, 0, 0, 0};
+  if (lo + (threadIdx.x & 31) < hi) nx = load((int32_t)lo + (threadIdx.x & 31));
   for (int32_t v = (int32_t)lo + (threadIdx.x & 31); v < hi; v += 32) {
+    const Pre pr = nx;
+    if (v + 32 < hi) nx = load(v + 32);
     if (T > 1) t = tree_forward(tt.soff, T, t, v);
     const int32_t s0 = tt.soff[t], ns = tt.soff[t + 1] - s0;
     const int64_t base = 2 * (int64_t)s0 + 2 * (int64_t)ns;
-    const uint64_t c = (uint64_t)cnt[v], cp = v ? (uint64_t)cnt[v - 1] : 0ull;
+    const uint64_t c = pr.c, cp = pr.cp;
     const int64_t eid = (int64_t)(uint32_t)c - 1;
     const int64_t xh = (int64_t)(c >> 32) - (int64_t)(cp >> 32);
     const int64_t xid = (int64_t)(c >> 32) - xh;       // exit heads below v
     const int64_t pe = base - (int64_t)(uint32_t)r[eid] + (v - ehead[eid]);
     const int64_t px = base - (int64_t)(uint32_t)r[He + xid] + (xhead[xid] - v);
-    const int64_t e0 = eoff[v], q0 = qoff[v];
-    const int32_t ne = (int32_t)(eoff[v + 1] - e0), nq = (int32_t)(qoff[v + 1] - q0);
+    const int64_t e0 = pr.e0, q0 = pr.q0;
+    const int32_t ne = (int32_t)(pr.e1 - e0), nq = (int32_t)(pr.q1 - q0);
     partner[pe] = (int32_t)px;
     partner[px] = (int32_t)pe;
     StepDesc d;
@@ -413,15 +425,27 @@ struct PrepParams {
 template <typename F>
 __device__ __forceinline__ void for_block_events(const PrepParams& p, int32_t t0, int32_t t1, int mode, F&& f) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  // this lane's step of the next group, loaded one group ahead
+  StepDesc nd;
+  int32_t npt = 0;
+  nd.e0 = 0; nd.q0 = 0; nd.ne = 0; nd.nq = 0;
+  if (t0 + 32 * warp + lane < t1) {
+    nd = p.desc[t0 + 32 * warp + lane];
+    npt = p.partner[t0 + 32 * warp + lane];
+  }
   for (int32_t c = t0 + 32 * warp; c < t1; c += 32 * nw) {
     const int32_t t = c + lane;
+    const StepDesc d = nd;
+    const int32_t pt = npt;   // the node's other step (exit of an enter, enter of an exit)
+    if (t + 32 * nw < t1) {
+      nd = p.desc[t + 32 * nw];
+      npt = p.partner[t + 32 * nw];
+    }
     int32_t cnt = 0;
     uint32_t e0 = 0;
     bool neg = false, twice = false;
     if (t < t1) {
-      const StepDesc d = p.desc[t];
       neg = d.nq < 0;
-      const int32_t pt = p.partner[t];           // the node's other step (exit of an enter, enter of an exit)
       twice = !neg && pt < t1;
       bool keep = true;
       if (neg) keep = pt < t0;                   // entered in this block: keys known, deltas cancel
@@ -514,11 +538,16 @@ __device__ void prepare_block_a(const PrepParams& p, int32_t b, unsigned char* s
     }
     if (threadIdx.x == 0) {
       // greedy slices over the window's words: close a slice before it exceeds cap
+      // (its end: the last word boundary whose rank stays within cap of the slice
+      // start, by binary search over the nondecreasing rank table; at least one word)
       int32_t ns = s_nsl;
       int32_t lo = 0;
       while (lo < ww) {
-        int32_t hi = lo + 1;
-        while (hi < ww && srl[hi + 1] - srl[lo] <= cap) ++hi;
+        int32_t hi = lo + 1, top = ww;
+        while (hi < top) {
+          const int32_t mid = (hi + top + 1) >> 1;
+          if (srl[mid] - srl[lo] <= cap) hi = mid; else top = mid - 1;
+        }
         if (ns < kMaxSlices) {
           Slice s;
           s.word_lo = w0 + lo; s.word_hi = w0 + hi;
