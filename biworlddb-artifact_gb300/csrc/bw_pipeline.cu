@@ -2153,11 +2153,17 @@ int pipe_spec_forest(int32_t T, const int64_t* soff, const int64_t* eoff, const 
   s.gsum_words = gsum;
   if (s.h_units.size() >= (size_t)1 << 31) return BW_EINVAL;
   s.n_units = (int32_t)s.h_units.size();
-  // queue order: largest estimated block work first (longest-processing-time first)
+  // queue order: largest estimated block time first (longest-processing-time first).
+  // A block is swept once per rank slice, so its work counts once per slice its
+  // distinct keys are expected to need (at most its events, at most the domain).
   s.h_order.resize(s.B);
   std::vector<int64_t> bw(s.B);
-  for (int32_t t = 0; t < T; ++t)
-    for (int32_t i = 0; i < nb[t]; ++i) bw[s.h_boff[t] + i] = W[t] / nb[t];
+  const int64_t cap = std::max<int64_t>(1, (int64_t)s.SL.cap32);
+  for (int32_t t = 0; t < T; ++t) {
+    const int64_t keys = std::min<int64_t>((int64_t)C[t], (eoff[t + 1] - eoff[t]) / nb[t] + 1);
+    const int64_t slices = (keys + cap - 1) / cap;
+    for (int32_t i = 0; i < nb[t]; ++i) bw[s.h_boff[t] + i] = W[t] / nb[t] * slices;
+  }
   std::iota(s.h_order.begin(), s.h_order.end(), 0);
   std::stable_sort(s.h_order.begin(), s.h_order.end(), [&](int32_t a, int32_t b) { return bw[a] > bw[b]; });
   return 0;
