@@ -72,7 +72,7 @@ def parse():
     ap.add_argument("--full-check", action="store_true", help="check every answer against the oracle")
     ap.add_argument("--no-autotune", action="store_true", help="batched: use the default tuning")
     ap.add_argument("--tuning", default=None, help="batched: JSON tuning to use instead of the autotuner")
-    ap.add_argument("--e2e-chunks", type=int, default=4, help="batched: tree chunks of the host-buffer replay")
+    ap.add_argument("--e2e-chunks", type=int, default=6, help="batched: tree chunks of the host-buffer replay")
     ap.add_argument("--no-serving", action="store_true", help="batched: skip the served-store runs")
     ap.add_argument("--loads", default="1e6,5e6,2e7", help="serving: offered loads in requests/s")
     ap.add_argument("--hbm-cap-gb", type=float, default=120.0, help="serving: admission cap of the store")
@@ -416,7 +416,12 @@ def bench_batched(args):
         # step; the host-buffer form overlaps chunk copies with the replay of others
         e2e = None
         if not args.no_e2e:
-            hf = bw.HostForest(*shape, chunks=args.e2e_chunks, tuning=tuning, device=dev)
+            # each chunk holds a sixth of the trees: half the block work keeps its
+            # CTAs busy to the end of the chunk (measured: 18.7 vs 19.4 ms per step)
+            e2e_tuning = dict(tuning) if tuning else None
+            if e2e_tuning and e2e_tuning.get("block_work", 0) > 0 and args.e2e_chunks > 1:
+                e2e_tuning["block_work"] = max(65536, e2e_tuning["block_work"] // 2)
+            hf = bw.HostForest(*shape, chunks=args.e2e_chunks, tuning=e2e_tuning, device=dev)
             for _ in range(2):
                 hf.run(h_parent, h_events, h_queries, h_answers)
             torch.cuda.synchronize()
@@ -439,6 +444,7 @@ def bench_batched(args):
             e2e = {"value": ws * Q / (ems / 1e3), "unit": "answers/s",
                    "h2d_bytes_per_step": 4 * S + 16 * E + 12 * Q, "d2h_bytes_per_step": 8 * Q, "ms_per_step": ems,
                    "host_wall_ms_per_step": wall_ms, "chunks": len(hf.parts),
+                   "tuning": e2e_tuning,
                    "form": "HostForest: per-chunk plans, copies of chunk k+1 overlap the replay of chunk k"}
             del hf
 
