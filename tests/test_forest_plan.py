@@ -22,7 +22,7 @@ def test_every_tree_has_a_block(bw, forest):
     assert st["blocks"] == forest.n_trees and st["carry_bytes"] == 0
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
 @pytest.mark.parametrize("ctas", [1, 2])
 def test_block_work_monotone_and_carry_budget(bw, forest, tile, ctas):
     prev = None
@@ -39,6 +39,11 @@ def test_carry_budget_caps_huge_domains(bw):
     soff, eoff, qoff = np.array([0, 50000, 100000]), np.array([0, 800000, 1600000]), np.array([0, 100, 200])
     st = bw.forest_plan_stats(soff, eoff, qoff, np.array([1 << 28, 1 << 28], np.uint32), tuning={"block_work": 65536})
     assert st["carry_bytes"] <= 4e9 and st["blocks"] >= 2
+
+
+def test_unknown_tile_refused(bw, forest):
+    with pytest.raises(RuntimeError):
+        bw.forest_plan_stats(*args(forest), tuning={"tile": 6})
 
 
 def test_malformed_shapes_refused(bw):
