@@ -766,21 +766,24 @@ struct SweepParams {
 };
 
 // The sweep keeps the block-local prefix structure in shared memory as chunks of
-// kChunk ranks: a Fenwick tree inside every chunk (levels below the chunk top),
-// the chunk totals T[h], and per-warp copies of the exclusive prefix of the chunk
-// totals, rebuilt by each warp before every probe phase.  An update touches only
-// its own chunk; a probe reads the prefix copy plus <= kChunkLevels nodes.
+// kChunk ranks with chunk totals T[h], in one of two forms.  Fenwick chunks (a tree
+// inside every chunk, per-warp copies of the exclusive prefix of the totals rebuilt
+// before a probe phase): an update touches <= kChunkLevels nodes of its chunk, a probe
+// is one thread.  Flat chunks (each rank's own value, totals in up to 8 side-by-side
+// copies): an update is two atomics, a probe is one warp summing the partial chunks at
+// both ends of its range and the totals between them.
 //
-// Steps are replayed in tiles: the events of up to Cfg::kTileSteps consecutive
-// steps are flattened in step order and thread i stages, with cp.async, flattened
-// events i + 256 m and queries i + 256 m of the next tile into its own double-buffered
-// slots while it replays the current tile, waiting only for its own copies, so
-// staging needs no barrier.  Barriers only order the Fenwick: after the updates
-// that precede a query step (its probes must see them) and after its probes (the
-// next updates must not run under them).  The events of the steps between two
-// query steps (exits of a tree walk, states without queries) are applied as one
-// flat batch by all threads.  Step descriptors and their event/query prefix sums
-// come from a shared ring refilled Cfg::kRingFill steps at a time.
+// Steps are replayed in tiles of up to Cfg::kTileSteps consecutive steps whose events
+// and queries, flattened in step order, fit the tile's staging slots.  Own-slot tiles:
+// thread i stages, with cp.async, flattened events i + kThreads m and its query slots
+// of the next tile while it replays the current one and waits only for its own copies.
+// Cooperative tiles: warps copy 32-step groups and a barrier publishes the tile.
+// Specialised tiles: one warp cuts and stages tiles two ahead for the others.  A tile
+// within the single-probe limits is replayed offline (one barrier, every query probed
+// on the state at the tile start plus its correction over the tile's earlier events,
+// a barrier, the tile's updates); otherwise per query step (its updates, a barrier,
+// its probes, a barrier).  Step descriptors and their event/query prefix sums come
+// from a shared ring refilled Cfg::kRingFill steps at a time.
 __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");

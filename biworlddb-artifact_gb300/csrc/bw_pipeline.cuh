@@ -38,8 +38,6 @@ __host__ __device__ inline int64_t est_work(int64_t S, int64_t E, int64_t Q) {
 }
 
 // Sweep geometry (see bw_pipeline.cu).
-constexpr int kSweepThreads = 256;
-constexpr int kSweepWarps = kSweepThreads / 32;
 constexpr int kChunk = 256;
 constexpr int kChunkBits = 8;
 constexpr int kChunkLevels = 8;
