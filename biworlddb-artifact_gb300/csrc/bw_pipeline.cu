@@ -16,15 +16,16 @@
 //                                blocks (batch_engine_v7.hpp:707-722 cuts equal
 //                                state counts of one chain; here the cut follows
 //                                events + queries and never spans two trees)
-//   4. prepare   k_prepare       per block: key bitmap + popcount rank table
+//   4. prepare   k_prepare<0>    per block: key bitmap + popcount rank table
 //                                (the CSR rank-LUT of sparse_engine.hpp:70-102),
-//                                smem-sized key slices, and, unless the block ends
-//                                its tree, its net key deltas as a dense row
+//                                smem-sized key slices and the node width;
+//                k_prepare<1>    unless the block ends its tree, its net key deltas
+//                                as a dense key-prefix row
 //   5. carry     k_carry_*       inclusive column scan of each tree's rows: the
 //                                key prefix at every block start
 //                                (batch_engine_v7.hpp:936-945, on the device)
 //   6. sweep     k_sweep         persistent CTAs take blocks from a queue and
-//                                replay each from a zero local Fenwick tree in
+//                                replay each from a zero local prefix structure in
 //                                shared memory; answer = carry(hi) - carry(lo) +
 //                                local(hi) - local(lo) (batch_engine_v7.hpp:849-961)
 //
