@@ -559,7 +559,8 @@ class BwNativeWorkload(C.Structure):
 
 
 HOST_SYMBOLS = ["bw_fixture_open", "bw_fixture_from_memory", "bw_fixture_close", "bw_fixture_rows",
-                "bw_native_build", "bw_native_free", "bw_sha256_hex", "bw_fnv1a"]
+                "bw_native_build", "bw_native_free", "bw_native_build_declared", "bw_v7_plan_build",
+                "bw_v7_plan_build_declared", "bw_v7_plan_free", "bw_sha256_hex", "bw_fnv1a"]
 
 _host = None
 
@@ -600,11 +601,31 @@ def fnv1a(buf) -> int:
     return int(host_lib().bw_fnv1a(a.ctypes.data if a.size else None, a.size))
 
 
-def native_workload(fixture: bytes, n_states: int, topology: int, seed: int, factor_period: int,
-                    q: int, per_state: bool = True, factor_pct: int = -1) -> "workloads.Workload":
-    """Compile a reference-native case (BWBASE02 image + declared edits) into the
-    event model: class-delta events by state and class-interval queries in the
-    reference's answer order (v = 1..S-1, k = 0..q-1)."""
+class BwDeclared(C.Structure):
+    _fields_ = [("n_states", C.c_int32), ("q", C.c_int32), ("per_state", C.c_int32), ("parent", C.c_void_p),
+                ("op", C.c_void_p), ("g", C.c_void_p), ("id", C.c_void_p), ("val", C.c_void_p), ("t", C.c_void_p),
+                ("qlo", C.c_void_p), ("qhi", C.c_void_p), ("n_inserted", C.c_int64), ("ins_t", C.c_void_p),
+                ("ins_g", C.c_void_p)]
+
+
+def _declared(decl):
+    """A BwDeclared over numpy copies of ``decl``'s arrays (kept alive with it)."""
+    import numpy as np
+    keep = {"parent": np.ascontiguousarray(decl.parent, np.int32), "op": np.ascontiguousarray(decl.op, np.uint8),
+            "g": np.ascontiguousarray(decl.g, np.int32), "id": np.ascontiguousarray(decl.id, np.int64),
+            "val": np.ascontiguousarray(decl.val, np.int64), "t": np.ascontiguousarray(decl.t, np.int64),
+            "qlo": np.ascontiguousarray(decl.qlo, np.int64), "qhi": np.ascontiguousarray(decl.qhi, np.int64),
+            "ins_t": np.ascontiguousarray(decl.ins_t, np.int64).reshape(-1),
+            "ins_g": np.ascontiguousarray(decl.ins_g, np.int32).reshape(-1)}
+    d = BwDeclared()
+    d.n_states, d.q, d.per_state = int(keep["parent"].size), int(decl.q), int(bool(decl.per_state))
+    d.n_inserted = int(keep["ins_t"].size)
+    for k, a in keep.items():
+        setattr(d, k, a.ctypes.data if a.size else None)
+    return d, keep
+
+
+def _with_fixture(fixture: bytes, fn):
     import numpy as np
     L = host_lib()
     img = np.frombuffer(fixture, dtype=np.uint8)
@@ -613,25 +634,59 @@ def native_workload(fixture: bytes, n_states: int, topology: int, seed: int, fac
     if rc:
         raise ValueError(f"malformed BWBASE02 fixture (rc={rc})")
     try:
+        return fn(L, fx)
+    finally:
+        L.bw_fixture_close(fx)
+
+
+def _native_result(L, out, name: str, chain: bool) -> "workloads.Workload":
+    import numpy as np
+    try:
+        w = out.contents
+        S, E, Q = w.n_states, w.n_events, w.n_queries
+        parent = np.ctypeslib.as_array(C.cast(w.parent, C.POINTER(C.c_int32)), (S,)).copy()
+        ev = np.frombuffer(C.string_at(w.events, 16 * E), dtype=workloads.EVENT_DTYPE).copy() \
+            if E else np.empty(0, dtype=workloads.EVENT_DTYPE)
+        qs = np.frombuffer(C.string_at(w.queries, 12 * Q), dtype=workloads.QUERY_DTYPE).copy() \
+            if Q else np.empty(0, dtype=workloads.QUERY_DTYPE)
+        return workloads.Workload(name, parent, int(w.n_keys), ev, qs, chain)
+    finally:
+        L.bw_native_free(out)
+
+
+def native_workload(fixture: bytes, n_states: int, topology: int, seed: int, factor_period: int,
+                    q: int, per_state: bool = True, factor_pct: int = -1) -> "workloads.Workload":
+    """Compile a reference-native case (BWBASE02 image + declared edits) into the
+    event model: class-delta events by state and class-interval queries in the
+    reference's answer order (v = 1..S-1, k = 0..q-1)."""
+    def run(L, fx):
         spec = BwNativeSpec(n_states, topology, seed, factor_period, q, int(per_state), factor_pct)
         out = C.POINTER(BwNativeWorkload)()
         rc = L.bw_native_build(fx, C.byref(spec), C.byref(out))
         if rc:
             raise ValueError(f"native workload rejected (rc={rc})")
-        try:
-            w = out.contents
-            S, E, Q = w.n_states, w.n_events, w.n_queries
-            parent = np.ctypeslib.as_array(C.cast(w.parent, C.POINTER(C.c_int32)), (S,)).copy()
-            ev = np.frombuffer(C.string_at(w.events, 16 * E), dtype=workloads.EVENT_DTYPE).copy() \
-                if E else np.empty(0, dtype=workloads.EVENT_DTYPE)
-            qs = np.frombuffer(C.string_at(w.queries, 12 * Q), dtype=workloads.QUERY_DTYPE).copy() \
-                if Q else np.empty(0, dtype=workloads.QUERY_DTYPE)
-            name = f"native_S{n_states}_t{topology}_s{seed}_f{factor_period}_q{q}"
-            return workloads.Workload(name, parent, int(w.n_keys), ev, qs, topology == 0)
-        finally:
-            L.bw_native_free(out)
-    finally:
-        L.bw_fixture_close(fx)
+        return _native_result(L, out, f"native_S{n_states}_t{topology}_s{seed}_f{factor_period}_q{q}", topology == 0)
+    return _with_fixture(fixture, run)
+
+
+def native_workload_declared(fixture: bytes, decl, name: str = "declared") -> "workloads.Workload":
+    """The event model of an explicit declared workload (bw_native_build_declared):
+    ``decl`` carries n-state arrays parent/op/g/id/val/t, declared ranges qlo/qhi,
+    inserted rows ins_t/ins_g, q and per_state (the reference fuzz's Workload)."""
+    import numpy as np
+
+    def run(L, fx):
+        L.bw_native_build_declared.argtypes = [C.c_void_p, C.POINTER(BwDeclared),
+                                               C.POINTER(C.POINTER(BwNativeWorkload))]
+        d, _keep = _declared(decl)
+        out = C.POINTER(BwNativeWorkload)()
+        rc = L.bw_native_build_declared(fx, C.byref(d), C.byref(out))
+        if rc:
+            raise ValueError(f"declared workload rejected (rc={rc})")
+        par = np.asarray(decl.parent)
+        chain = bool(np.all(par[1:] == np.arange(par.size - 1)))
+        return _native_result(L, out, name, chain)
+    return _with_fixture(fixture, run)
 
 
 class BwV7Plan(C.Structure):
@@ -652,47 +707,58 @@ def _node_dtype():
                      ("ex_old", "u1"), ("ex_new", "u1"), ("pad", "u1", (6,))])
 
 
+def _v7_result(L, out) -> dict:
+    import numpy as np
+    try:
+        p = out.contents
+        B, G, Cp, S, na = p.B, p.G, p.Cpfx, p.n_states, p.n_active
+
+        def arr(ptr, dtype, n):
+            dt = np.dtype(dtype)
+            return np.frombuffer(C.string_at(ptr, dt.itemsize * n), dtype=dt).copy() if n else np.zeros(0, dt)
+        ms_off = arr(p.ms_off, "<i4", na + 1)
+        nms = int(ms_off[-1])
+        return {"B": B, "G": G, "Cpfx": Cp, "ncls": p.ncls, "q": p.q, "n_states": S,
+                "nodes": arr(p.nodes, _node_dtype(), S), "block_v0": arr(p.block_v0, "<i4", B),
+                "block_v1": arr(p.block_v1, "<i4", B), "fac_start": arr(p.fac_start, "<i8", B * G),
+                "g2row": arr(p.g2row, "<i4", G), "ms_off": ms_off, "ms_cls": arr(p.ms_cls, "<i8", nms),
+                "ms_base": arr(p.ms_base, "<i8", nms), "ms_dev": arr(p.ms_dev, "<i4", nms),
+                "devbuf": arr(p.devbuf, "<i8", max(1, p.n_devbuf)), "need_off": arr(p.need_off, "<i8", B * G),
+                "qlb": arr(p.qlb, "<i4", S * p.q), "qhb": arr(p.qhb, "<i4", S * p.q),
+                "bidx": arr(p.bidx, "<i4", S), "vbase": arr(p.vbase, "<i8", Cp)}
+    finally:
+        L.bw_v7_plan_free(out)
+
+
 def v7_plan(fixture: bytes, n_states: int, seed: int, factor_period: int, q: int, blocks: int,
             per_state: bool = True, factor_pct: int = -1) -> dict:
     """The reference's v7 chain plan for gpu_v7_launch, as numpy arrays."""
-    import numpy as np
-    L = host_lib()
-    L.bw_v7_plan_build.argtypes = [C.c_void_p, C.POINTER(BwNativeSpec), C.c_int32,
-                                   C.POINTER(C.POINTER(BwV7Plan))]
-    L.bw_v7_plan_free.argtypes = [C.POINTER(BwV7Plan)]
-    img = np.frombuffer(fixture, dtype=np.uint8)
-    fx = C.c_void_p()
-    rc = L.bw_fixture_from_memory(img.ctypes.data, img.size, C.byref(fx))
-    if rc:
-        raise ValueError(f"malformed BWBASE02 fixture (rc={rc})")
-    try:
+    def run(L, fx):
+        L.bw_v7_plan_build.argtypes = [C.c_void_p, C.POINTER(BwNativeSpec), C.c_int32,
+                                       C.POINTER(C.POINTER(BwV7Plan))]
+        L.bw_v7_plan_free.argtypes = [C.POINTER(BwV7Plan)]
         spec = BwNativeSpec(n_states, 0, seed, factor_period, q, int(per_state), factor_pct)
         out = C.POINTER(BwV7Plan)()
         rc = L.bw_v7_plan_build(fx, C.byref(spec), blocks, C.byref(out))
         if rc:
             raise ValueError(f"v7 plan rejected (rc={rc})")
-        try:
-            p = out.contents
-            B, G, Cp, S, na = p.B, p.G, p.Cpfx, p.n_states, p.n_active
-            nms = None
+        return _v7_result(L, out)
+    return _with_fixture(fixture, run)
 
-            def arr(ptr, dtype, n):
-                dt = np.dtype(dtype)
-                return np.frombuffer(C.string_at(ptr, dt.itemsize * n), dtype=dt).copy() if n else np.zeros(0, dt)
-            ms_off = arr(p.ms_off, "<i4", na + 1)
-            nms = int(ms_off[-1])
-            return {"B": B, "G": G, "Cpfx": Cp, "ncls": p.ncls, "q": p.q, "n_states": S,
-                    "nodes": arr(p.nodes, _node_dtype(), S), "block_v0": arr(p.block_v0, "<i4", B),
-                    "block_v1": arr(p.block_v1, "<i4", B), "fac_start": arr(p.fac_start, "<i8", B * G),
-                    "g2row": arr(p.g2row, "<i4", G), "ms_off": ms_off, "ms_cls": arr(p.ms_cls, "<i8", nms),
-                    "ms_base": arr(p.ms_base, "<i8", nms), "ms_dev": arr(p.ms_dev, "<i4", nms),
-                    "devbuf": arr(p.devbuf, "<i8", max(1, p.n_devbuf)), "need_off": arr(p.need_off, "<i8", B * G),
-                    "qlb": arr(p.qlb, "<i4", S * p.q), "qhb": arr(p.qhb, "<i4", S * p.q),
-                    "bidx": arr(p.bidx, "<i4", S), "vbase": arr(p.vbase, "<i8", Cp)}
-        finally:
-            L.bw_v7_plan_free(out)
-    finally:
-        L.bw_fixture_close(fx)
+
+def v7_plan_declared(fixture: bytes, decl, blocks: int) -> dict:
+    """The v7 chain plan of an explicit declared chain workload (bw_v7_plan_build_declared)."""
+    def run(L, fx):
+        L.bw_v7_plan_build_declared.argtypes = [C.c_void_p, C.POINTER(BwDeclared), C.c_int32,
+                                                C.POINTER(C.POINTER(BwV7Plan))]
+        L.bw_v7_plan_free.argtypes = [C.POINTER(BwV7Plan)]
+        d, _keep = _declared(decl)
+        out = C.POINTER(BwV7Plan)()
+        rc = L.bw_v7_plan_build_declared(fx, C.byref(d), blocks, C.byref(out))
+        if rc:
+            raise ValueError(f"v7 plan rejected (rc={rc})")
+        return _v7_result(L, out)
+    return _with_fixture(fixture, run)
 
 
 class GpuV7Args(C.Structure):

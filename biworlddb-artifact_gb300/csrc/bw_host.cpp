@@ -174,15 +174,6 @@ void declare(const BwFixture& f, const BwNativeSpec& sp, Declared& w) {
       e.val = f.row_amt(e.id) + rng.range(-100000, 100000);
     }
   }
-  w.endpoints.reserve((size_t)(S - 1) * q * 2);
-  for (int32_t v = 1; v < S; ++v)
-    for (int32_t k = 0; k < q; ++k) {
-      const size_t qi = sp.per_state ? (size_t)v * q + k : (size_t)k;
-      w.endpoints.push_back(w.qlo[qi]);
-      w.endpoints.push_back(w.qhi[qi]);
-    }
-  std::sort(w.endpoints.begin(), w.endpoints.end());
-  w.endpoints.erase(std::unique(w.endpoints.begin(), w.endpoints.end()), w.endpoints.end());
 }
 
 // Per-group support: every class a row of the group can occupy (base rows of the
@@ -239,13 +230,65 @@ extern "C" int bw_fixture_from_memory(const void* image, size_t len, BwFixture**
 extern "C" void bw_fixture_close(BwFixture* f) { delete f; }
 extern "C" int64_t bw_fixture_rows(const BwFixture* f) { return f ? f->n : 0; }
 
-extern "C" int bw_native_build(const BwFixture* fx, const BwNativeSpec* sp, BwNativeWorkload** out) {
-  if (!fx || !sp || !out || sp->n_states < 2 || sp->q < 1 || sp->topology < 0 || sp->topology > 2)
+namespace {
+
+// Edits must name existing rows and groups, parents must precede their children
+// (the reference aborts on the same conditions, oracle.cpp:268-275, 325-328).
+int validate(const BwFixture& f, const Declared& w, int32_t S) {
+  const int64_t M = f.n + (int64_t)w.ins_t.size();
+  if ((int32_t)w.parent.size() != S || w.parent[0] != -1) return 2;
+  for (int32_t v = 1; v < S; ++v) {
+    if (w.parent[v] < 0 || w.parent[v] >= v) return 2;
+    const Edit& e = w.edit[v];
+    if (e.op > OP_FACTOR) return 2;
+    if (e.op == OP_FACTOR || e.op == OP_INSERT || e.op == OP_MOVE)
+      if (e.g < 0 || e.g >= f.G) return 2;
+    if (e.op != OP_FACTOR && (e.id < 0 || e.id >= M)) return 2;
+  }
+  for (int32_t g : w.ins_g)
+    if (g < 0 || g >= f.G) return 2;
+  return 0;
+}
+
+// Sorted distinct declared bounds (batch_engine_v7.hpp:362-442 dedupe).
+void collect_endpoints(Declared& w, int32_t S, int32_t q, bool per_state) {
+  w.endpoints.clear();
+  w.endpoints.reserve((size_t)(S - 1) * q * 2);
+  for (int32_t v = 1; v < S; ++v)
+    for (int32_t k = 0; k < q; ++k) {
+      const size_t qi = per_state ? (size_t)v * q + k : (size_t)k;
+      w.endpoints.push_back(w.qlo[qi]);
+      w.endpoints.push_back(w.qhi[qi]);
+    }
+  std::sort(w.endpoints.begin(), w.endpoints.end());
+  w.endpoints.erase(std::unique(w.endpoints.begin(), w.endpoints.end()), w.endpoints.end());
+}
+
+// Copy of a caller's explicit workload into the builder's form.
+int from_declared(const BwFixture& f, const BwDeclared* d, Declared& w) {
+  if (!d || d->n_states < 2 || d->q < 1 || !d->parent || !d->op || !d->g || !d->id || !d->val || !d->t ||
+      !d->qlo || !d->qhi || d->n_inserted < 0 || (d->n_inserted && (!d->ins_t || !d->ins_g)))
     return 2;
-  const BwFixture& f = *fx;
-  Declared w;
-  declare(f, *sp, w);
-  const int32_t S = sp->n_states, q = sp->q, G = f.G;
+  const int32_t S = d->n_states, q = d->q;
+  w.parent.assign(d->parent, d->parent + S);
+  w.edit.assign(S, Edit{});
+  for (int32_t v = 1; v < S; ++v) {
+    Edit& e = w.edit[v];
+    e.op = d->op[v]; e.g = d->g[v]; e.id = d->id[v]; e.val = d->val[v]; e.t = d->t[v];
+  }
+  const size_t nq = d->per_state ? (size_t)S * q : (size_t)q;
+  w.qlo.assign(d->qlo, d->qlo + nq);
+  w.qhi.assign(d->qhi, d->qhi + nq);
+  w.ins_t.assign(d->ins_t, d->ins_t + d->n_inserted);
+  w.ins_g.assign(d->ins_g, d->ins_g + d->n_inserted);
+  collect_endpoints(w, S, q, d->per_state != 0);
+  return validate(f, w, S);
+}
+
+// The event model of a declared workload (see the file comment).
+int build_events(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bool per_state,
+                 BwNativeWorkload** out) {
+  const int32_t G = f.G;
   const int64_t N = f.n, M = N + (int64_t)w.ins_t.size();
   const std::vector<int64_t>& ep = w.endpoints;
   auto class_of = [&](int64_t t) {
@@ -378,12 +421,31 @@ extern "C" int bw_native_build(const BwFixture* fx, const BwNativeSpec* sp, BwNa
   o->queries = new BwQuery[o->n_queries ? o->n_queries : 1];
   for (int32_t v = 1; v < S; ++v)
     for (int32_t k = 0; k < q; ++k) {
-      const size_t qi = sp->per_state ? (size_t)v * q + k : (size_t)k;
+      const size_t qi = per_state ? (size_t)v * q + k : (size_t)k;
       o->queries[(size_t)(v - 1) * q + k] = {(uint32_t)v, (uint32_t)class_of(w.qlo[qi]),
                                              (uint32_t)class_of(w.qhi[qi])};
     }
   *out = o;
   return 0;
+}
+
+}  // namespace
+
+extern "C" int bw_native_build(const BwFixture* fx, const BwNativeSpec* sp, BwNativeWorkload** out) {
+  if (!fx || !sp || !out || sp->n_states < 2 || sp->q < 1 || sp->topology < 0 || sp->topology > 2)
+    return 2;
+  Declared w;
+  declare(*fx, *sp, w);
+  collect_endpoints(w, sp->n_states, sp->q, sp->per_state != 0);
+  const int rc = validate(*fx, w, sp->n_states);
+  return rc ? rc : build_events(*fx, w, sp->n_states, sp->q, sp->per_state != 0, out);
+}
+
+extern "C" int bw_native_build_declared(const BwFixture* fx, const BwDeclared* d, BwNativeWorkload** out) {
+  if (!fx || !out) return 2;
+  Declared w;
+  const int rc = from_declared(*fx, d, w);
+  return rc ? rc : build_events(*fx, w, d->n_states, d->q, d->per_state != 0, out);
 }
 
 extern "C" void bw_native_free(BwNativeWorkload* w) {
@@ -481,12 +543,12 @@ extern "C" uint64_t bw_fnv1a(const void* data, size_t n) {
 // touched-class coordinates per group (1234-1308), factor plan (1311-1340), base
 // leaf and base mass (1350-1415), merged support (1578-1629), equal state blocks,
 // block-start factors and deviation snapshots (707-830).
-extern "C" int bw_v7_plan_build(const BwFixture* fx, const BwNativeSpec* sp, int32_t blocks, BwV7Plan** out) {
-  if (!fx || !sp || !out || sp->n_states < 3 || sp->q < 1 || sp->topology != 0) return 2;
-  const BwFixture& f = *fx;
-  Declared w;
-  declare(f, *sp, w);
-  const int32_t S = sp->n_states, q = sp->q, G = f.G, VS = S - 1;
+namespace {
+int build_v7(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bool per_state, int32_t blocks,
+             BwV7Plan** out) {
+  for (int32_t v = 1; v < S; ++v)
+    if (w.parent[v] != v - 1) return 2;   // the block path takes chains only (batch_engine_v7.hpp:708)
+  const int32_t G = f.G, VS = S - 1;
   const int64_t N = f.n;
   const std::vector<int64_t>& ep = w.endpoints;
   auto class_of = [&](int64_t t) {
@@ -632,7 +694,7 @@ extern "C" int bw_v7_plan_build(const BwFixture* fx, const BwNativeSpec* sp, int
   std::vector<int32_t> qlb((size_t)S * q, 0), qhb((size_t)S * q, 0);
   for (int32_t v = 1; v < S; ++v)
     for (int32_t k = 0; k < q; ++k) {
-      const size_t qi = sp->per_state ? (size_t)v * q + k : (size_t)k;
+      const size_t qi = per_state ? (size_t)v * q + k : (size_t)k;
       qlb[(size_t)v * q + k] = class_of(w.qlo[qi]);
       qhb[(size_t)v * q + k] = class_of(w.qhi[qi]);
     }
@@ -652,6 +714,23 @@ extern "C" int bw_v7_plan_build(const BwFixture* fx, const BwNativeSpec* sp, int
   o->qlb = dup(qlb); o->qhb = dup(qhb); o->bidx = dup(bidx); o->vbase = dup(vbase);
   *out = o;
   return 0;
+}
+}  // namespace
+
+extern "C" int bw_v7_plan_build(const BwFixture* fx, const BwNativeSpec* sp, int32_t blocks, BwV7Plan** out) {
+  if (!fx || !sp || !out || sp->n_states < 3 || sp->q < 1 || sp->topology != 0) return 2;
+  Declared w;
+  declare(*fx, *sp, w);
+  collect_endpoints(w, sp->n_states, sp->q, sp->per_state != 0);
+  const int rc = validate(*fx, w, sp->n_states);
+  return rc ? rc : build_v7(*fx, w, sp->n_states, sp->q, sp->per_state != 0, blocks, out);
+}
+
+extern "C" int bw_v7_plan_build_declared(const BwFixture* fx, const BwDeclared* d, int32_t blocks, BwV7Plan** out) {
+  if (!fx || !out || !d || d->n_states < 3) return 2;
+  Declared w;
+  const int rc = from_declared(*fx, d, w);
+  return rc ? rc : build_v7(*fx, w, d->n_states, d->q, d->per_state != 0, blocks, out);
 }
 
 extern "C" void bw_v7_plan_free(BwV7Plan* p) {

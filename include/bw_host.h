@@ -64,6 +64,39 @@ typedef struct {          /* host arrays owned by the library */
 int bw_native_build(const BwFixture* f, const BwNativeSpec* spec, BwNativeWorkload** out);
 void bw_native_free(BwNativeWorkload* w);
 
+/* An explicit declared workload: the reference's Workload (common.hpp:177-212) as a
+ * caller fills it directly, e.g. the reference's randomized branching fuzz
+ * (fuzz_fullpath.cpp:196-283), instead of drawing it from (topology, seed, factor
+ * period).  Row ids: base rows 0..n-1, inserted rows n..n+n_inserted-1 (row n+k is
+ * the k-th insert, initially absent at ins_t[k] in group ins_g[k]).  Edit v >= 1:
+ * op BW_OP_*; REPLACE sets row id's amount to val (and makes it present), INSERT and
+ * MOVE set its (t, g, amount) to (t, g, val), DELETE removes it, FACTOR sets group
+ * g's factor to val (any int64, zero and negative included).  Endpoint classes are
+ * the sorted distinct declared bounds (batch_engine_v7.hpp:559-572). */
+enum { BW_OP_REPLACE = 0, BW_OP_INSERT = 1, BW_OP_DELETE = 2, BW_OP_MOVE = 3, BW_OP_FACTOR = 4 };
+
+typedef struct {
+  int32_t n_states;       /* states 0..n_states-1 (state 0 = the fixture, no edit) */
+  int32_t q;              /* ranges per state */
+  int32_t per_state;      /* 1: qlo/qhi hold n_states*q entries (v*q+k); 0: q shared entries */
+  const int32_t* parent;  /* n_states; parent[0] = -1, 0 <= parent[v] < v */
+  const uint8_t* op;      /* n_states (index 0 unused) */
+  const int32_t* g;       /* n_states: group of INSERT/MOVE/FACTOR */
+  const int64_t* id;      /* n_states: row of REPLACE/INSERT/DELETE/MOVE */
+  const int64_t* val;     /* n_states: amount or factor */
+  const int64_t* t;       /* n_states: timestamp of INSERT/MOVE */
+  const int64_t* qlo;     /* declared ranges [qlo, qhi) */
+  const int64_t* qhi;
+  int64_t n_inserted;
+  const int64_t* ins_t;   /* n_inserted */
+  const int32_t* ins_g;   /* n_inserted */
+} BwDeclared;
+
+/* Same output as bw_native_build for an explicit workload (answer order v = 1..S-1,
+ * k = 0..q-1).  Returns 2 for malformed edits (unknown op, row or group out of
+ * range, bad parent), 3 for an unusable fixture. */
+int bw_native_build_declared(const BwFixture* f, const BwDeclared* w, BwNativeWorkload** out);
+
 /* The reference's v7 chain plan (batch_engine_v7.hpp:576-830) in the argument
  * layout of gpu_v7_launch / gpu_combine_launch, built on the host: node plans,
  * equal state blocks, block-start factor vectors, block-start deviation
@@ -91,6 +124,8 @@ typedef struct {
 } BwV7Plan;
 
 int bw_v7_plan_build(const BwFixture* f, const BwNativeSpec* spec, int32_t blocks, BwV7Plan** out);
+/* The same plan for an explicit chain workload (parent[v] == v-1, else 2). */
+int bw_v7_plan_build_declared(const BwFixture* f, const BwDeclared* w, int32_t blocks, BwV7Plan** out);
 void bw_v7_plan_free(BwV7Plan* p);
 
 /* Lowercase hex SHA-256 (64 chars + NUL) and the reference's FNV-1a. */

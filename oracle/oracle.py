@@ -130,6 +130,34 @@ def direct_scan(fx: Fixture, n_states: int, topology: int, seed: int, factor_per
         lib().bwo_workload_free(C.byref(w))
 
 
+def direct_scan_declared(fx: Fixture, decl) -> np.ndarray:
+    """Direct-scan oracle answers of an explicit declared workload: ``decl`` has
+    n-state arrays parent/op/g/id/val/t, ranges qlo/qhi (n_states*q per state or q
+    shared), ins_t/ins_g of the inserted rows, q and per_state (the reference fuzz's
+    Workload, fuzz_fullpath.cpp:196-283)."""
+    S, q = int(decl.parent.size), int(decl.q)
+    keep = {
+        "parent": np.ascontiguousarray(decl.parent, np.int32), "op": np.ascontiguousarray(decl.op, np.uint8),
+        "eg": np.ascontiguousarray(decl.g, np.int32), "eid": np.ascontiguousarray(decl.id, np.int64),
+        "eval": np.ascontiguousarray(decl.val, np.int64), "et": np.ascontiguousarray(decl.t, np.int64),
+        "qlo": np.ascontiguousarray(decl.qlo, np.int64), "qhi": np.ascontiguousarray(decl.qhi, np.int64),
+        "ins_t": np.ascontiguousarray(decl.ins_t, np.int64).reshape(-1),
+        "ins_g": np.ascontiguousarray(decl.ins_g, np.int32).reshape(-1)}
+    w = _Workload()
+    w.n_states, w.q, w.per_state = S, q, int(bool(decl.per_state))
+    w.n_base, w.groups, w.n_inserted = fx.s.n, fx.s.groups, int(keep["ins_t"].size)
+    w.t_min, w.t_max = fx.s.t_min, fx.s.t_max
+    for k, a in keep.items():
+        setattr(w, k, _ptr(a) if a.size else None)
+    ans = np.zeros((S - 1) * q, dtype=np.int64)
+    rc = lib().bwo_direct_scan(C.byref(fx.s), C.byref(w), _ptr(ans))
+    if rc == 6:
+        raise OverflowError("an exact answer does not fit int64")
+    if rc:
+        raise RuntimeError(f"direct scan failed rc={rc}")
+    return ans
+
+
 def _ev_arrays(parent, events, queries):
     parent = np.ascontiguousarray(parent, dtype=np.int32)
     events = np.ascontiguousarray(events, dtype=EVENT_DTYPE)

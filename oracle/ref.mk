@@ -12,6 +12,10 @@ CC ?= gcc
 
 all: $(OUT)/oracle_$(STATES) $(OUT)/compiled_$(STATES) $(OUT)/csr_ref
 
+# The reference's randomized branching fuzz case builder and its "rf" oracle arm
+# (fuzz_fullpath.cpp) behind a harness that prints per-case golden hashes.
+fuzz: $(OUT)/fuzz_ref_$(STATES)
+
 $(OUT)/sha_shim.o: oracle/ref_shim/sha256_shim.c oracle/bw_oracle.c
 	mkdir -p $(OUT)
 	$(CC) -O2 -c -o $(OUT)/sha_shim.o oracle/ref_shim/sha256_shim.c
@@ -30,4 +34,8 @@ $(OUT)/csr_ref: oracle/ref_csr.cpp
 	mkdir -p $(OUT)
 	$(CXX) -std=c++17 -O2 -fopenmp -Ioracle/ref_shim -I$(REF)/src oracle/ref_csr.cpp -o $@
 
-.PHONY: all
+$(OUT)/fuzz_ref_$(STATES): oracle/ref_fuzz.cpp $(OUT)/sha_shim.o
+	$(CXX) -std=c++17 -O2 -DNDEBUG -DBWH_STATES=$(STATES) -DBWH_MAXQ=$(MAXQ) -Ioracle/ref_shim -I$(REF)/src \
+	  oracle/ref_fuzz.cpp $(OUT)/bwo.o -o $@
+
+.PHONY: all fuzz

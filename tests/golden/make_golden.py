@@ -57,6 +57,12 @@ CASES = [
 ] + [("check", 2049, topo, 7, fp, 2, None) for topo in (0, 1, 2) for fp in (4, 37)] + [
     ("check", 2049, topo, 11, 4, 8, None) for topo in (0, 1, 2)]
 
+# Shared-range cases (BWH_RANGE_SCOPE unset: one set of q nested ranges for every
+# state, common.hpp:296-306), pinned by the reference oracle run without the
+# per_state scope.
+SHARED_CASES = [("check", 2049, topo, 7, 37, 2, None) for topo in (0, 1, 2)] + [
+    ("check", 2049, 0, 11, 4, 8, None), ("real3_100k", 2049, 1, 20261291, 59, 4, None)]
+
 
 # Large reference-native cases, too slow for the direct-scan oracle (about five
 # minutes each); pinned by the reference's own v7 worker (panel_batch_v7fix.cpp,
@@ -95,12 +101,13 @@ def main() -> int:
             raise SystemExit(f"fixture {name}: sha {got} != reference tool {want}")
         (HERE / f"{name}.bin.z").write_bytes(zlib.compress(img, 9))
     out = {"fixtures": {k: v[4] for k, v in FIXTURES.items()}, "cases": []}
-    for fx_name, states, topo, seed, fp, q, published in CASES:
+    for (fx_name, states, topo, seed, fp, q, published), per_state in (
+            [(c, True) for c in CASES] + [(c, False) for c in SHARED_CASES]):
         img = fixture_bytes(fx_name)
-        ans = oracle.direct_scan(oracle.Fixture(img), states, topo, seed, fp, q, True)
+        ans = oracle.direct_scan(oracle.Fixture(img), states, topo, seed, fp, q, per_state)
         sha = oracle.sha256_hex(ans.tobytes())
         rec = {"fixture": fx_name, "states": states, "topology": topo, "seed": seed,
-               "factor_period": fp, "q": q, "per_state": True, "oracle": sha,
+               "factor_period": fp, "q": q, "per_state": per_state, "oracle": sha,
                "fnv1a": f"{oracle.fnv1a(ans.tobytes()):016x}", "n_answers": int(ans.size)}
         if published:
             rec["published"] = published
@@ -109,7 +116,9 @@ def main() -> int:
             tmp = ROOT / "_work" / "golden_fixture.bin"
             tmp.parent.mkdir(exist_ok=True)
             tmp.write_bytes(img)
-            env = dict(os.environ, BWH_RANGE_SCOPE="per_state")
+            env = {k: v for k, v in os.environ.items() if k != "BWH_RANGE_SCOPE"}
+            if per_state:
+                env["BWH_RANGE_SCOPE"] = "per_state"
             p = subprocess.run([str(ref), "--fixture", str(tmp), "--topology", str(topo),
                                 "--seed", str(seed), "--factor-period", str(fp), "--q", str(q),
                                 "--out", str(tmp) + ".ans"], capture_output=True, text=True,

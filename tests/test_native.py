@@ -26,7 +26,8 @@ def fixture(name: str) -> bytes:
 
 
 def cid(c):
-    return f"{c['fixture']}-S{c['states']}-t{c['topology']}-s{c['seed']}-f{c['factor_period']}-q{c['q']}"
+    scope = "" if c.get("per_state", True) else "-shared"
+    return f"{c['fixture']}-S{c['states']}-t{c['topology']}-s{c['seed']}-f{c['factor_period']}-q{c['q']}{scope}"
 
 
 def expected(c):
@@ -46,7 +47,7 @@ def test_front_end_events_reproduce_golden(bw, oracle_mod, case):
 @pytest.mark.parametrize("case", [c for c in CASES if c["topology"] == 0 and c["q"] == 2], ids=cid)
 def test_v7_plan_reproduces_golden(bw, case):
     plan = bw.v7_plan(fixture(case["fixture"]), case["states"], case["seed"], case["factor_period"],
-                      case["q"], blocks=7)
+                      case["q"], blocks=7, per_state=case["per_state"])
     ans, _, _ = v7_emul.run(plan)
     assert bw.sha256_hex(ans.tobytes()) == expected(case)
 
@@ -94,10 +95,10 @@ def test_gpu_replay_large_reference_case(bw, torch_cuda, case):
 @pytest.mark.parametrize("blocks", [1, 9, 64])
 def test_gpu_v7_dropin_reproduces_golden(bw, torch_cuda, case, blocks):
     plan = bw.v7_plan(fixture(case["fixture"]), case["states"], case["seed"], case["factor_period"],
-                      case["q"], blocks=blocks)
+                      case["q"], blocks=blocks, per_state=case["per_state"])
     ans, dV, lvals = bw.run_v7_plan(plan)
     assert bw.sha256_hex(ans.tobytes()) == expected(case)
-    if case["q"] == 2 and blocks == 9:
+    if case["q"] in (2, 8) and blocks == 9:
         # intermediate outputs of gpu_v7_launch equal the reference block executor's
         e_ans, e_dV, e_lvals = v7_emul.run(plan)
         np.testing.assert_array_equal(dV.reshape(e_dV.shape), e_dV)
