@@ -1,38 +1,48 @@
 #!/usr/bin/env python3
-"""Benchmark: bit-exact range-sum answers/s on GB300, batched vs plain.
+"""Benchmark: bit-exact range-sum answers/s on GB300, batched vs plain, every config.
 
-Default workload (``--workload batched_trees``): 4,096 independent version trees
-of uneven size (lognormal state counts, median 2,000, about 30M states, 240M
-events, 4.1M queries; see biworlddb-artifact_gb300/workloads.py).  One step = one
-replay of the whole batch as a single autotuned pipeline replayed from a CUDA
-graph.  The same line reports the plain form -- 4,096 sequential bw_replay_launch
-calls, one per tree -- and its answers/s, with answers compared bit for bit.
+Default (``--workload batched_trees``): 4,096 independent version trees of uneven
+size (lognormal state counts, median 2,000, about 27.5M states, 220M events, 4.1M
+queries; biworlddb-artifact_gb300/workloads.py).  One step = one replay of the whole
+batch as a single autotuned pipeline replayed from a CUDA graph.  Every batched
+answer is checked against the oracle (all trees).  The same line reports the plain
+form (4,096 sequential bw_replay_launch calls) and, as sub-records with their own
+roofline, e2e and CPU baseline:
 
-Single-tree workload (``--workload trip_tree``): the trip-log-shaped single tree -- 300,000 states (extend
-with p=0.9, fork from a uniform earlier state otherwise), 40,000,000 int64 delta
-events with Zipf s=1.2 keys over 65,536 cells, 50,000,000 range-sum queries at
-uniform states with uniform intervals; seeded synthetic data (see
-biworlddb-artifact_gb300/workloads.py).  One step = one full replay of that
-workload: ingest, tree linearisation, block plan, carry scan and block sweep.
+* ``plain_chain``: the plain chain replay (20,000 states, 1M events, 10k queries,
+  4,096 keys) and ``plain_chain_x100`` (the same generator at 100x: 2M states,
+  100M events, 1M queries), both on the single-pass chain path;
+* ``trip_tree``: the trip-log-shaped tree (300k states, 40M events, 50M queries,
+  65,536 keys) on the general pipeline;
+* ``csr_lut``: the sparse-key CSR rank-LUT (10M u64 keys, 100M point and range
+  lookups, LUT budgets 64/256/1024 MiB);
+* ``reference_chain``: the reference's own published GPU workload -- a 300,000-state
+  chain, seed 7, factor period 37, q=2, per-state ranges, on the synthetic 100k-row
+  fixture -- through the worker binary (both arms: the event replay and the
+  gpu_v7.h drop-in), beside the reference's published RTX 4090 numbers;
+* ``served``: the served store (config 5) at 1M/5M/20M requests/s.
+
+Other workloads: ``--workload plain_chain|trip_tree|csr_lut|serving`` prints that
+record as the line (``--scale`` multiplies the sizes).
 
 * value: answers/s with inputs resident in HBM (CUDA events around K steps).
-* e2e:   the same through the public API with pinned host buffers: every step
+  Inputs smaller than twice L2 are timed one replay at a time with a 256 MiB write
+  between replays (L2 flushed); larger ones need no flush.
+* e2e: the same through the public API with pinned host buffers: every step
   copies parent/events/queries host->device and the answers device->host.
-* roofline: the dominant kernel (the block sweep) -- algorithmic bytes per launch
-  (16 B per event record + 12 B per query record + 8 B per answer) over its mean
-  launch time, measured with CUDA events on the launch stream over the timed
-  region, against the measured HBM copy bandwidth.
-* cpu_baseline: the oracle's preorder apply/undo replay (the reference's tree
-  path, batch_engine_v7.hpp:1021-1059, ported) on the first states of the same
-  workload, 1 thread.
+* roofline: the dominant kernel -- the chain sweep (k_chain_sweep) on chains, the
+  tree sweep (k_sweep) otherwise -- with its algorithmic bytes (16 per event
+  record, 12 per query record, 8 per answer) over its mean launch time (CUDA
+  events on the launch stream), against the measured HBM copy bandwidth.
+* cpu_baseline: the oracle's restatement of the reference's CPU path on the box's
+  host cores: the block-parallel chain executor (batch_engine_v7.hpp:832-968) on
+  every thread for chains, the preorder apply/undo replay
+  (batch_engine_v7.hpp:1021-1059) on one thread for trees.
 
-Inputs (1.24 GB) exceed L2 (129 MB), so no explicit L2 flush is done between steps.
-
---impl reference times the reference's CPU implementation of the path (the
-ported preorder replay; the reference's block-parallel executor only supports
-chains, batch_engine_v7.hpp:708) on a bounded sample and prints the same line.
-Under torchrun with N>1 every rank runs an independent replica (weak scaling);
-rank 0 prints.
+--impl reference times the reference's CPU algorithm for the default workload on
+every host thread, all 4,096 trees per step (the same configuration).  Under
+torchrun with N>1 every rank runs an independent replica (weak scaling); rank 0
+prints.
 """
 from __future__ import annotations
 
@@ -44,6 +54,7 @@ import subprocess
 import sys
 import tempfile
 import time
+import zlib
 from pathlib import Path
 
 import numpy as np
@@ -53,6 +64,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "bit-exact range-sum answers/s (plain version-tree replay)"
 BATCHED_METRIC = "bit-exact range-sum answers/s (batched uneven trees: one autotuned CUDA-graph launch)"
+L2_BYTES = 129 << 20
 
 
 def parse():
@@ -65,16 +77,20 @@ def parse():
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--blocks", type=int, default=0)
+    ap.add_argument("--path", default="auto", choices=["auto", "chain", "general"],
+                    help="plain workloads: force the chain path or the general pipeline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU sample duration")
     ap.add_argument("--plain-steps", type=int, default=2, help="steps of the sequential plain form")
-    ap.add_argument("--full-check", action="store_true", help="check every answer against the oracle")
+    ap.add_argument("--sample-check", action="store_true", help="batched: check 65 trees instead of all")
     ap.add_argument("--no-autotune", action="store_true", help="batched: use the default tuning")
     ap.add_argument("--tuning", default=None, help="batched: JSON tuning to use instead of the autotuner")
     ap.add_argument("--e2e-chunks", type=int, default=6, help="batched: tree chunks of the host-buffer replay")
     ap.add_argument("--no-serving", action="store_true", help="batched: skip the served-store runs")
-    ap.add_argument("--loads", default="1e6,5e6,2e7", help="serving: offered loads in requests/s")
+    ap.add_argument("--no-subrecords", action="store_true", help="batched: skip the per-config sub-records")
+    ap.add_argument("--sub-steps", type=int, default=10, help="timed steps of each sub-record")
+    ap.add_argument("--loads", default="1e6,5e6,2e7,4e7,8e7", help="serving: offered loads in requests/s")
     ap.add_argument("--hbm-cap-gb", type=float, default=120.0, help="serving: admission cap of the store")
     return ap.parse_args()
 
@@ -151,9 +167,9 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(workload: str):
-    """DRAM bytes per sweep launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / f"k_sweep_{workload}.txt"
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / f"{kernel}_{workload}.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -165,10 +181,21 @@ def profiled_traffic(workload: str):
     return None
 
 
-def cpu_baseline(w, seconds: float):
-    """Oracle preorder replay over the first Euler steps of the workload, timed alone."""
+def oracle_mod():
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
+    return oracle
+
+
+def load_pkg():
+    import __graft_entry__ as g
+    return g.package()
+
+
+# ----------------------------------------------------------------------------- CPU legs
+def cpu_tree_sample(w, seconds: float):
+    """Oracle preorder replay over the first Euler steps of the workload, one thread."""
+    oracle = oracle_mod()
     S = len(w.parent)
     probe = max(1, min(S, 2000))
     _, done, secs = oracle.ev_sweep_prefix(w.parent, w.n_keys, w.events, w.queries, probe)
@@ -180,13 +207,41 @@ def cpu_baseline(w, seconds: float):
                       f"{done} answers, {secs:.1f} s)"}
 
 
-def forest_cpu_sample(w, seconds: float, threads: int = 1, seed: int = 5):
+def cpu_chain_sample(w, seconds: float):
+    """Oracle block-parallel chain executor (run_blocks, batch_engine_v7.hpp:832-968)
+    on every host thread, whole workload per run, repeated for about `seconds`."""
+    oracle = oracle_mod()
+    threads = oracle.max_threads()
+    runs, t0 = 0, time.perf_counter()
+    while True:
+        oracle.ev_blocks(w.parent, w.n_keys, w.events, w.queries, blocks=threads, threads=threads)
+        runs += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or runs >= 200:
+            break
+    return {"value": runs * len(w.queries) / el, "unit": "answers/s", "cores": threads, "kind": "port",
+            "sample": f"block-parallel chain executor over the whole workload, {runs} runs in {el:.1f} s "
+                      f"({len(w.events)} events, {len(w.queries)} queries)"}
+
+
+def cpu_sample(w, seconds: float):
+    return cpu_chain_sample(w, seconds) if w.chain else cpu_tree_sample(w, seconds)
+
+
+def oracle_answers(w):
+    oracle = oracle_mod()
+    if w.chain:
+        t = oracle.max_threads()
+        return oracle.ev_blocks(w.parent, w.n_keys, w.events, w.queries, blocks=t, threads=t)
+    return oracle.ev_sweep(w.parent, w.n_keys, w.events, w.queries)
+
+
+def forest_cpu_sample(w, seconds: float, threads: int = 1, seed: int = 5, all_trees: bool = False):
     """Oracle preorder replay (the reference's tree path, batch_engine_v7.hpp:1021-1059,
-    ported) of whole trees in a seeded random order until `seconds` of work; trees run
-    on `threads` host threads (the oracle call releases the GIL)."""
+    ported) of whole trees in a seeded random order until `seconds` of work (or all
+    trees); trees run on `threads` host threads (the oracle call releases the GIL)."""
     from concurrent.futures import ThreadPoolExecutor
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
+    oracle = oracle_mod()
     order = np.random.default_rng(seed).permutation(w.n_trees)
 
     def one(t):
@@ -198,7 +253,7 @@ def forest_cpu_sample(w, seconds: float, threads: int = 1, seed: int = 5):
     t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as pool:
         i = 0
-        while i < len(order) and time.perf_counter() - t0 < seconds:
+        while i < len(order) and (all_trees or time.perf_counter() - t0 < seconds):
             batch = order[i:i + 4 * threads]
             for a, st in pool.map(one, batch):
                 answers += a
@@ -208,7 +263,24 @@ def forest_cpu_sample(w, seconds: float, threads: int = 1, seed: int = 5):
     secs = time.perf_counter() - t0
     return {"value": answers / max(secs, 1e-9), "unit": "answers/s", "cores": threads, "kind": "port",
             "sample": f"preorder replay of {trees} of {w.n_trees} trees in a seeded random order "
-                      f"({states} states, {answers} answers, {secs:.1f} s)"}
+                      f"({states} states, {answers} answers, {secs:.1f} s)", "trees": trees}
+
+
+def forest_check_all(w, ans, threads: int) -> int:
+    """Every tree's batched answers against the oracle's preorder replay (parallel)."""
+    from concurrent.futures import ThreadPoolExecutor
+    oracle = oracle_mod()
+
+    def one(t):
+        tr = w.tree(int(t))
+        q0, q1 = int(w.query_off[t]), int(w.query_off[t + 1])
+        return bool(np.array_equal(ans[q0:q1], oracle.ev_sweep(tr.parent, tr.n_keys, tr.events, tr.queries)))
+
+    with ThreadPoolExecutor(max_workers=threads) as pool:
+        bad = [t for t, ok in zip(range(w.n_trees), pool.map(one, range(w.n_trees))) if not ok]
+    if bad:
+        raise SystemExit(f"batched answers of {len(bad)} trees differ from the oracle (first: tree {bad[0]})")
+    return w.n_trees
 
 
 def reference_arm(args):
@@ -216,48 +288,172 @@ def reference_arm(args):
     if rank != 0:
         return 0
     w = load_pkg().workloads.make(args.workload, args.seed, args.scale)
+    threads = os.cpu_count() or 1
     if args.workload == "batched_trees":
-        threads = os.cpu_count() or 1
-        vals = [forest_cpu_sample(w, max(1.0, args.cpu_seconds / max(1, args.steps)), threads, seed=5 + i)
+        # every step replays all trees (the same configuration as the GPU arm)
+        vals = [forest_cpu_sample(w, 0.0, threads, seed=5 + i, all_trees=True)
                 for i in range(args.warmup + args.steps)][args.warmup:]
         v = statistics.median([x["value"] for x in vals])
         line = {"impl": "reference", "metric": BATCHED_METRIC, "value": v, "unit": "answers/s",
-                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
-                "data": "synthetic", "config": dict(w.describe(), l2="inputs larger than L2"),
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * len(w.queries) / v, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+                "config": dict(w.describe(), l2="inputs larger than L2"), "same_config": True,
                 "cpu_baseline": {"value": v, "unit": "answers/s", "cores": threads, "kind": "port",
                                  "sample": vals[-1]["sample"]},
                 "e2e": {"value": v, "unit": "answers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return 0
+    if args.workload == "csr_lut":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the version-chain "
+                          "replay workloads; csr_lut has no reference CPU arm here"}), flush=True)
+        return 0
+    steps = args.steps if w.chain else min(args.steps, 3)
     vals = []
-    for _ in range(args.warmup):
-        cpu_baseline(w, min(3.0, args.cpu_seconds / 4))
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(w, max(1.0, args.cpu_seconds / max(1, args.steps))))
+    for i in range(args.warmup + steps):
+        if w.chain:
+            s = cpu_chain_sample(w, 0.0)
+        else:
+            t0 = time.perf_counter()
+            oracle_mod().ev_sweep(w.parent, w.n_keys, w.events, w.queries)
+            el = time.perf_counter() - t0
+            s = {"value": len(w.queries) / el, "cores": 1,
+                 "sample": f"preorder replay of the whole workload in {el:.1f} s"}
+        if i >= args.warmup:
+            vals.append(s)
     v = statistics.median([x["value"] for x in vals])
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "answers/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
-            "config": dict(w.describe(), l2="inputs larger than L2"),
-            "cpu_baseline": {"value": v, "unit": "answers/s", "cores": 1, "kind": "port",
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * len(w.queries) / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic", "config": dict(w.describe(), l2="inputs larger than L2"), "same_config": True,
+            "cpu_baseline": {"value": v, "unit": "answers/s", "cores": vals[-1]["cores"], "kind": "port",
                              "sample": vals[-1]["sample"]},
             "e2e": {"value": v, "unit": "answers/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def bench_csr(args):
-    """Sparse-key rank index (10M distinct u64 keys, 20M events, 100M point and 100M
-    range lookups): build time and lookup throughput at LUT budgets 64/256/1024 MiB.
-    Prints one JSON line (headline: point lookups/s at the 64 MiB budget)."""
+# ----------------------------------------------------------------------------- GPU records
+def timed_replays(torch, plan, stream, d_parent, d_events, d_queries, d_answers, steps: int, flush: bool):
+    """Mean ms of `steps` replays (CUDA events on the launch stream).  With `flush`,
+    every replay is timed alone after a 256 MiB write that evicts L2."""
+    buf = torch.empty(256 << 20, dtype=torch.uint8, device=d_parent.device) if flush else None
+    plan.timing_reset()
+    torch.cuda.synchronize()
+    if not flush:
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(steps):
+            plan.launch(d_parent, d_events, d_queries, d_answers)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / steps
+    pairs = []
+    for i in range(steps):
+        buf.fill_(i & 255)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        plan.launch(d_parent, d_events, d_queries, d_answers)
+        b.record(stream)
+        pairs.append((a, b))
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in pairs) / steps
+
+
+def plain_record(args, bw, dev, name: str, scale: float, steps: int, warmup: int, cpu_seconds: float,
+                 ws: int = 1, clocks: bool = False) -> dict:
+    """One plain workload (one tree): correctness against the oracle, device-resident
+    replays, the host-buffer e2e form, the roofline of the dominant kernel and the CPU
+    baseline.  Returns the record (the bench line's fields without the boilerplate)."""
     import torch
-    ws, rank, local = dist_env()
-    torch.cuda.set_device(local)
-    dev = torch.device(f"cuda:{local}")
-    bw = load_pkg()
-    bw.build()
-    w = bw.workloads.make("csr_lut", args.seed, args.scale)
+    t_gen = time.perf_counter()
+    w = bw.workloads.make(name, args.seed, scale)
+    gen_s = time.perf_counter() - t_gen
+    S, E, Q = len(w.parent), len(w.events), len(w.queries)
+    h_parent = torch.from_numpy(w.parent).pin_memory()
+    h_events = torch.from_numpy(w.events.view(np.int64).reshape(-1, 2)).pin_memory()
+    h_queries = torch.from_numpy(w.queries.view(np.int32).reshape(-1, 3)).pin_memory()
+    h_answers = torch.empty(Q, dtype=torch.int64).pin_memory()
+    d_parent, d_events, d_queries = h_parent.to(dev), h_events.to(dev), h_queries.to(dev)
+    d_answers = torch.empty(Q, dtype=torch.int64, device=dev)
+    plan = bw.Replay(d_parent, w.n_keys, E, Q, blocks=args.blocks, chain=w.chain, timing=True, path=args.path)
+    chain_path = plan.chain_path(d_events)
+    stream = torch.cuda.current_stream(dev)
+    for i in range(max(1, warmup)):
+        plan.launch(d_parent, d_events, d_queries, d_answers)
+        if i == 0:
+            st = plan.status()
+            if st:
+                raise SystemExit(f"{name}: device rejected the workload: {bw.STATUS_NAMES.get(st, st)}")
+    torch.cuda.synchronize()
+    ans0 = d_answers.cpu().numpy()
+    if not np.array_equal(ans0, oracle_answers(w)):
+        raise SystemExit(f"{name}: GPU answers differ from the oracle")
+    digest = oracle_mod().sha256_hex(ans0.tobytes())
+    in_bytes = 4 * S + 16 * E + 12 * Q
+    flush = in_bytes < 2 * L2_BYTES
+    kernels, blocks = plan.info()
+    clk_s = ClockSampler(int(dev.index or 0)) if clocks else None
+    if clk_s:
+        clk_s.start()
+    ms = timed_replays(torch, plan, stream, d_parent, d_events, d_queries, d_answers, steps, flush)
+    clk = clk_s.stop() if clk_s else None
+    stage_ms, n_timed = plan.stage_times()
+    stage_mean = {k: v / max(1, n_timed) for k, v in stage_ms.items()}
+    ms = max_over_ranks(ms, dev)
+    if not np.array_equal(d_answers.cpu().numpy(), ans0):
+        raise SystemExit(f"{name}: answers changed between steps")
+    e2e = None
+    if not args.no_e2e:
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            d_parent.copy_(h_parent, non_blocking=True)
+            d_events.copy_(h_events, non_blocking=True)
+            d_queries.copy_(h_queries, non_blocking=True)
+            plan.launch(d_parent, d_events, d_queries, d_answers)
+            h_answers.copy_(d_answers, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = max_over_ranks(e0.elapsed_time(e1) / steps, dev)
+        if not np.array_equal(h_answers.numpy(), ans0):
+            raise SystemExit(f"{name}: e2e answers differ")
+        e2e = {"value": ws * Q / (ems / 1e3), "unit": "answers/s", "h2d_bytes_per_step": in_bytes,
+               "d2h_bytes_per_step": 8 * Q, "ms_per_step": ems}
+    peak, peak_kind = measured_peaks()
+    kernel = "k_chain_sweep" if chain_path else "k_sweep"
+    sweep_bytes = 16 * E + 20 * Q
+    sweep_ms = stage_mean["sweep"]
+    achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9
+    tag = name if scale == 1.0 else f"{name}_x{scale:g}"
+    rec = {
+        "value": ws * Q / (ms / 1e3), "unit": "answers/s", "ms_per_step": ms, "steps": steps,
+        "config": dict(w.describe(), scale=scale, blocks=blocks, path="chain" if chain_path else "general",
+                       l2=("inputs fit in L2: 256 MiB written between timed replays" if flush
+                           else "inputs larger than L2 (no flush needed)"), answers_sha256=digest),
+        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": profiled_traffic(kernel, tag),
+                     "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": sweep_ms},
+        "pipeline": {"stages_ms": stage_mean, "whole_step_gbs": w.algorithmic_bytes / (ms / 1e3) / 1e9,
+                     "whole_step_frac": w.algorithmic_bytes / (ms / 1e3) / 1e9 / peak,
+                     "kernels_per_step": kernels},
+        "gpu_launches": kernels * steps, "exact": True, "setup": {"generate_s": gen_s}}
+    if clk is not None:
+        rec["clocks"] = clk
+    if e2e:
+        rec["e2e"] = e2e
+    if cpu_seconds > 0:
+        rec["cpu_baseline"] = cpu_sample(w, cpu_seconds)
+    return rec
+
+
+def csr_record(args, bw, dev, steps: int, warmup: int, scale: float = 1.0) -> dict:
+    """Sparse-key rank index (10M distinct u64 keys, 20M events, 100M point and 100M
+    range lookups): build time and lookup throughput at LUT budgets 64/256/1024 MiB."""
+    import torch
+    oracle = oracle_mod()
+    w = bw.workloads.make("csr_lut", args.seed, scale)
     L = len(w.point)
     d_keys = torch.from_numpy(w.keys.view(np.int64)).to(dev)
     d_amt = torch.from_numpy(w.amounts).to(dev)
@@ -266,32 +462,28 @@ def bench_csr(args):
     out_p = torch.empty(L, dtype=torch.int64, device=dev)
     out_r = torch.empty((L, 2), dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream(dev)
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
     peak, peak_kind = measured_peaks()
 
-    def timed(fn, steps):
-        for _ in range(args.warmup):
+    def timed(fn, n):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        for _ in range(steps):
+        for _ in range(n):
             fn()
         b.record(stream)
         torch.cuda.synchronize()
-        return a.elapsed_time(b) / steps
+        return a.elapsed_time(b) / n
 
     budgets = {}
-    clocks = ClockSampler(local)
-    clocks.start()
     rng = np.random.default_rng(7)
     sample = rng.integers(0, L, 200_000)
     for mib in (64, 256, 1024):
         idx = bw.CsrIndex(d_keys, d_amt, key_bits=w.key_bits, lut_budget_bytes=mib << 20)
-        build_ms = timed(idx.rebuild, args.steps)
-        p_ms = timed(lambda: idx.point(d_point, out_p), args.steps)
-        r_ms = timed(lambda: idx.range(d_ranges, out_r), args.steps)
+        build_ms = timed(idx.rebuild, steps)
+        p_ms = timed(lambda: idx.point(d_point, out_p), steps)
+        r_ms = timed(lambda: idx.range(d_ranges, out_r), steps)
         uk, pre = idx.arrays()
         uk = uk.cpu().numpy().view(np.uint64)
         pre = pre.cpu().numpy()
@@ -299,27 +491,99 @@ def bench_csr(args):
                 np.array_equal(out_r.cpu().numpy()[sample], oracle.csr_range(uk, pre, w.ranges[sample]))):
             raise SystemExit(f"CSR lookups differ from the oracle at budget {mib} MiB")
         budgets[f"{mib}MiB"] = {
-            "shift": idx.shift, "buckets": idx.n_buckets, "distinct_keys": idx.count(),
-            "build_ms": build_ms,
-            "point_lookups_per_s": L / (p_ms / 1e3), "point_ms": p_ms,
-            "point_gbs": 16 * L / (p_ms / 1e3) / 1e9,
-            "range_lookups_per_s": L / (r_ms / 1e3), "range_ms": r_ms,
-            "range_gbs": 32 * L / (r_ms / 1e3) / 1e9}
+            "shift": idx.shift, "buckets": idx.n_buckets, "distinct_keys": idx.count(), "build_ms": build_ms,
+            "point_lookups_per_s": L / (p_ms / 1e3), "point_ms": p_ms, "point_gbs": 16 * L / (p_ms / 1e3) / 1e9,
+            "range_lookups_per_s": L / (r_ms / 1e3), "range_ms": r_ms, "range_gbs": 32 * L / (r_ms / 1e3) / 1e9}
         del idx
-    clk = clocks.stop()
     head = budgets["64MiB"]
-    line = {
-        "metric": "exact sparse-key rank lookups/s (CSR rank-LUT, point)", "value": head["point_lookups_per_s"],
-        "unit": "lookups/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": head["point_ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "u64", "data": "synthetic",
-        "config": dict(w.describe(), l2="lookup arrays larger than L2 (no flush needed)"),
-        "roofline": {"bound": "hbm", "kernel": "k_csr_point", "achieved": head["point_gbs"], "peak": peak,
-                     "unit": "GB/s", "frac": head["point_gbs"] / peak, "peak_kind": peak_kind,
-                     "traffic": None, "algorithmic_bytes_per_launch": 16 * L},
-        "budgets": budgets, "gpu_launches": None, "clocks": clk}
-    print(json.dumps(line), flush=True)
-    return 0
+    return {"value": head["point_lookups_per_s"], "unit": "lookups/s", "ms_per_step": head["point_ms"],
+            "config": dict(w.describe(), l2="lookup arrays larger than L2 (no flush needed)"),
+            "roofline": {"bound": "hbm", "kernel": "k_csr_point", "achieved": head["point_gbs"], "peak": peak,
+                         "unit": "GB/s", "frac": head["point_gbs"] / peak, "peak_kind": peak_kind,
+                         "traffic": profiled_traffic("k_csr_point", "csr_lut"),
+                         "algorithmic_bytes_per_launch": 16 * L},
+            "budgets": budgets, "exact": "200,000 sampled lookups per budget against the oracle",
+            "gpu_launches": 3 * 3 * steps}
+
+
+# the reference's published GPU numbers for its own workload (300,000-state chain,
+# seed 7, factor period 37, q=2, per-state ranges; RTX 4090 + EPYC 9554)
+REFERENCE_PUBLISHED = {
+    "hardware": "RTX 4090 + EPYC 9554 (intel / taxi2024 fixtures)",
+    "gpu_v7_kernel_ms": {"B32": [11.375, 9.533], "B64": [6.522, 4.600], "B128": [3.505, 2.279]},
+    "gpu_v7_full_ms": {"B32": [169.1, 184.7], "B64": [192.0, 181.5], "B128": [233.5, 183.5]},
+    "gpu_snapshot_full_ms": {"B32": [129.0, 144.3], "B64": [134.8, 139.1]},
+    "best_kernel_answers_per_s": 599998 / 2.279e-3,
+    "source": "results/batch_gpu_20261031/summary.json:3-90, results/batch_gpu3_20261031/summary.json:3-78"}
+
+
+def reference_chain_record(args, bw, dev, steps: int) -> dict:
+    """The reference's own GPU workload through the worker binary, one process per
+    measurement as the reference measures it (both arms: the event replay and the
+    gpu_v7.h drop-in with B=128), plus the warm chain-path replay timed in-process."""
+    import torch
+    gold = json.loads((ROOT / "tests" / "golden" / "golden.json").read_text())
+    case = next(c for c in gold["large_cases"] if c["fixture"] == "survey_100k")
+    img = zlib.decompress((ROOT / "tests" / "golden" / "survey_100k.bin.z").read_bytes())
+    out = {"workload": "300,000-state chain, seed 7, factor period 37, q=2, per-state ranges, "
+                       "synthetic 100k-row 64-group fixture (the reference's 300k survey run)",
+           "want_sha256": case["reference"], "published": REFERENCE_PUBLISHED, "worker": {}}
+    with tempfile.TemporaryDirectory() as tmp:
+        fx = Path(tmp) / "survey_100k.bin"
+        fx.write_bytes(img)
+        env = dict(os.environ, BWH_RANGE_SCOPE="per_state")
+        for arm in ("gb300", "gpu_v7"):
+            recs = []
+            for r in range(3):
+                js = Path(tmp) / f"{arm}{r}.json"
+                p = subprocess.run([str(bw._build.WORKER), "--fixture", str(fx), "--base-id", "survey_100k",
+                                    "--topology", "0", "--seed", "7", "--factor-period", "37", "--q", "2",
+                                    "--repeat", str(r), "--states", "300000", "--arm", arm, "--blocks",
+                                    "128" if arm == "gpu_v7" else "0", "--answers", str(Path(tmp) / "a.bin"),
+                                    "--json", str(js)], capture_output=True, text=True, env=env)
+                if p.returncode:
+                    raise SystemExit(f"worker {arm} failed rc={p.returncode}: {p.stderr[-400:]}")
+                recs.append(json.loads(js.read_text()))
+            if any(x["answers_sha256"] != case["reference"] for x in recs):
+                raise SystemExit(f"worker {arm}: answers differ from the reference SHA-256")
+            med = sorted(recs, key=lambda x: x["full_ns"])[1]
+            out["worker"][arm] = {"full_ms": med["full_ns"] / 1e6,
+                                  "phases_ms": {k: v / 1e6 for k, v in med["phases_ns"].items()},
+                                  "kernel_ms": (med["gpu"]["kernel_ns"] + med["gpu"]["carry_ns"]
+                                                + med["gpu"]["combine_ns"]) / 1e6,
+                                  "upload_ms": med["gpu"]["upload_ns"] / 1e6,
+                                  "download_ms": med["gpu"]["download_ns"] / 1e6,
+                                  "blocks": med["gpu"]["blocks"], "kernels": med["gpu"]["kernels"],
+                                  "answers_sha256": med["answers_sha256"], "runs": len(recs)}
+    # warm, device-resident replay of the same workload
+    w = bw.native_workload(img, 300000, 0, 7, 37, 2, True)
+    S, E, Q = len(w.parent), len(w.events), len(w.queries)
+    d_parent = torch.from_numpy(w.parent).to(dev)
+    d_events = torch.from_numpy(w.events.view(np.int64).reshape(-1, 2)).to(dev)
+    d_queries = torch.from_numpy(w.queries.view(np.int32).reshape(-1, 3)).to(dev)
+    d_answers = torch.empty(Q, dtype=torch.int64, device=dev)
+    plan = bw.Replay(d_parent, w.n_keys, E, Q, chain=True, timing=True)
+    chain_path = plan.chain_path(d_events)
+    for _ in range(3):
+        plan.launch(d_parent, d_events, d_queries, d_answers)
+    torch.cuda.synchronize()
+    if bw.sha256_hex(d_answers.cpu().numpy().tobytes()) != case["reference"]:
+        raise SystemExit("reference chain: warm replay answers differ from the reference SHA-256")
+    stream = torch.cuda.current_stream(dev)
+    ms = timed_replays(torch, plan, stream, d_parent, d_events, d_queries, d_answers, steps,
+                       4 * S + 16 * E + 12 * Q < 2 * L2_BYTES)
+    stage_ms, n = plan.stage_times()
+    peak, peak_kind = measured_peaks()
+    sweep = stage_ms["sweep"] / max(1, n)
+    out["warm_replay"] = {"path": "chain" if chain_path else "general", "ms": ms, "answers_per_s": Q / (ms / 1e3),
+                          "sweep_ms": sweep, "events": E, "queries": Q, "keys": int(w.n_keys),
+                          "sweep_frac_of_peak": (16 * E + 20 * Q) / (sweep / 1e3) / 1e9 / peak,
+                          "vs_best_published_kernel": (Q / (ms / 1e3)) / REFERENCE_PUBLISHED[
+                              "best_kernel_answers_per_s"]}
+    best_full = min(min(v) for v in REFERENCE_PUBLISHED["gpu_snapshot_full_ms"].values())
+    out["worker_full_vs_best_published_full"] = best_full / out["worker"]["gb300"]["full_ms"]
+    out["exact"] = True
+    return out
 
 
 def bench_batched(args):
@@ -349,8 +613,8 @@ def bench_batched(args):
     d_parent, d_events, d_queries = h_parent.to(dev), h_events.to(dev), h_queries.to(dev)
     d_answers = torch.empty(Q, dtype=torch.int64, device=dev)
     stream = torch.cuda.Stream(dev)
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
+    oracle = oracle_mod()
+    threads = os.cpu_count() or 1
 
     def ev_timer():
         return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -371,18 +635,21 @@ def bench_batched(args):
         if st:
             raise SystemExit(f"device rejected the workload: {bw.STATUS_NAMES.get(st, st)}")
         ans0 = d_answers.cpu().numpy()
-        # parity: every tree when asked, else the largest tree and a seeded sample
-        if args.full_check:
-            check = np.arange(T)
-        else:
+        # parity: every tree against the oracle (or, when asked, the largest and 64 seeded)
+        t_chk = time.perf_counter()
+        if args.sample_check:
             rng = np.random.default_rng(123)
             check = np.unique(np.concatenate([[int(np.argmax(np.diff(w.state_off)))],
                                               rng.choice(T, size=min(T, 64), replace=False)]))
-        for t in check:
-            tr = w.tree(int(t))
-            q0, q1 = int(w.query_off[t]), int(w.query_off[t + 1])
-            if not np.array_equal(ans0[q0:q1], oracle.ev_sweep(tr.parent, tr.n_keys, tr.events, tr.queries)):
-                raise SystemExit(f"batched answers of tree {t} differ from the oracle")
+            for t in check:
+                tr = w.tree(int(t))
+                q0, q1 = int(w.query_off[t]), int(w.query_off[t + 1])
+                if not np.array_equal(ans0[q0:q1], oracle.ev_sweep(tr.parent, tr.n_keys, tr.events, tr.queries)):
+                    raise SystemExit(f"batched answers of tree {t} differ from the oracle")
+            checked = len(check)
+        else:
+            checked = forest_check_all(w, ans0, threads)
+        check_s = time.perf_counter() - t_chk
         digest = oracle.sha256_hex(ans0.tobytes())
         stages = [f.launch_timed(d_parent, d_events, d_queries, d_answers, stream) for _ in range(3)]
         stage_ms = {k: statistics.median([x[k] for x in stages]) for k in stages[0]}
@@ -506,12 +773,14 @@ def bench_batched(args):
         "config": dict(w.describe(), blocks=info["blocks"], tuning=info["tuning"],
                        l2="inputs (3.9 GB) larger than L2 (no flush needed)", answers_sha256=digest,
                        parallelism=f"tree-sharded x{ws} (a batch per rank, no exchange)" if ws > 1 else "single"),
+        "full_check": checked == T, "checked_trees": int(checked), "check_s": check_s,
         "plain": {"value": plain_value, "unit": "answers/s", "ms_per_step": plain_ms,
                   "launches_per_step": T, "kernels_per_step": plain_kernels // max(1, args.plain_steps),
                   "form": "one bw_replay_launch per tree, sequential on one stream"},
         "batched_vs_plain": value / plain_value if plain_value else None,
         "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": profiled_traffic(w.name),
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": profiled_traffic("k_sweep", w.name),
                      "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": stage_ms["sweep"]},
         "pipeline": {"stages_ms": stage_ms, "dominant_stage": top,
                      "whole_step_gbs": w.algorithmic_bytes / (ms / 1e3) / 1e9,
@@ -525,9 +794,28 @@ def bench_batched(args):
         line["e2e"] = e2e
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = forest_cpu_sample(w, args.cpu_seconds, 1)
-    if not args.no_serving:
-        del d_events, d_queries, d_parent, d_answers, f, pws
+    del d_events, d_queries, d_parent, d_answers, f, pws, h_events, h_queries, h_parent, h_answers
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.no_subrecords:
+        sub_cpu = 0.0 if args.no_cpu_baseline else min(8.0, args.cpu_seconds)
+        subs = {}
+        for key, name, scale in (("plain_chain", "plain_chain", 1.0), ("plain_chain_x100", "plain_chain", 100.0),
+                                 ("trip_tree", "trip_tree", 1.0)):
+            t_sub = time.perf_counter()
+            subs[key] = plain_record(args, bw, dev, name, scale, args.sub_steps, 3, sub_cpu)
+            subs[key]["wall_s"] = time.perf_counter() - t_sub
+            torch.cuda.empty_cache()
+        t_sub = time.perf_counter()
+        subs["csr_lut"] = csr_record(args, bw, dev, args.sub_steps, 3)
+        subs["csr_lut"]["wall_s"] = time.perf_counter() - t_sub
         torch.cuda.empty_cache()
+        t_sub = time.perf_counter()
+        subs["reference_chain"] = reference_chain_record(args, bw, dev, args.sub_steps)
+        subs["reference_chain"]["wall_s"] = time.perf_counter() - t_sub
+        torch.cuda.empty_cache()
+        line.update(subs)
+        line["gpu_launches"] += sum(int(s.get("gpu_launches") or 0) for s in subs.values())
+    if not args.no_serving:
         line["served"] = run_serving(args, bw, args.seed, args.scale)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -539,9 +827,9 @@ def bench_batched(args):
 def run_serving(args, bw, seed: int, scale: float):
     """Served store on the trip-log tree: the request log at each offered load (open
     loop, Poisson arrivals), every answer checked against the oracle's replay of the
-    final tree.  Returns a dict of per-load latency percentiles and rates."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
+    final tree.  Returns a dict of per-load latency percentiles and rates; the
+    highest loads show where achieved falls below offered (saturation)."""
+    oracle = oracle_mod()
     t = time.perf_counter()
     log = bw.workloads.serving(seed, scale)
     gen_s = time.perf_counter() - t
@@ -556,12 +844,14 @@ def run_serving(args, bw, seed: int, scale: float):
     want[order] = oracle.ev_sweep(par, b.n_keys, ev, qs)
     q = log.requests["kind"] == 0
     loads = []
-    for rate in [float(x) for x in args.loads.split(",") if x]:
+    for rate in [float(x) for x in args.loads.split(",") if x] + [None]:
         srv.reset()
-        ans, lat, st = srv.run(log.requests, log.commit_events, log.arrival / rate, max_inflight=1 << 16)
+        arr = None if rate is None else log.arrival / rate
+        ans, lat, st = srv.run(log.requests, log.commit_events, arr, max_inflight=1 << 16)
         if not np.array_equal(ans[q], want[q]):
-            raise SystemExit(f"served answers differ from the oracle at {rate:g} requests/s")
-        loads.append({"offered_rps": rate, "achieved_rps": st["requests"] / st["wall_s"],
+            raise SystemExit(f"served answers differ from the oracle at {rate} requests/s")
+        loads.append({"offered_rps": rate if rate is not None else "all at once",
+                      "achieved_rps": st["requests"] / st["wall_s"],
                       "answers_per_s": st["queries"] / st["wall_s"],
                       "p50_us": float(np.percentile(lat, 50)), "p99_us": float(np.percentile(lat, 99)),
                       "p50_query_us": float(np.percentile(lat[q], 50)),
@@ -572,7 +862,8 @@ def run_serving(args, bw, seed: int, scale: float):
                                                 "store_gb": info["store_bytes"] / 1e9,
                                                 "cap_gb": args.hbm_cap_gb,
                                                 "loop_warps": info["warps"]},
-            "loads": loads, "exact": True, "answers_sha256": oracle.sha256_hex(want[q].tobytes()),
+            "loads": loads, "saturated_answers_per_s": max(x["answers_per_s"] for x in loads),
+            "exact": True, "answers_sha256": oracle.sha256_hex(want[q].tobytes()),
             "setup_s": {"generate": gen_s, "store_build": build_s}}
 
 
@@ -586,7 +877,7 @@ def bench_serving(args):
     clocks.start()
     res = run_serving(args, bw, args.seed, args.scale)
     clk = clocks.stop()
-    top = res["loads"][-1]
+    top = [x for x in res["loads"] if x["offered_rps"] != "all at once"][-1]
     line = {"metric": "served range-sum answers/s (persistent request loop, open-loop Poisson arrivals)",
             "value": top["answers_per_s"], "unit": "answers/s", "n_gpus": 1, "steps": len(res["loads"]),
             "warmup": 0, "ms_per_step": top["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -599,9 +890,54 @@ def bench_serving(args):
     return 0
 
 
-def load_pkg():
-    import __graft_entry__ as g
-    return g.package()
+def bench_plain(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    bw = load_pkg()
+    bw.build()
+    if ws > 1:
+        torch.distributed.barrier()
+    cpu = 0.0 if (args.no_cpu_baseline or rank != 0 or ws > 1) else args.cpu_seconds
+    rec = plain_record(args, bw, dev, args.workload, args.scale, args.steps, args.warmup, cpu, ws=ws, clocks=True)
+    line = {"metric": METRIC, "value": rec.pop("value"), "unit": rec.pop("unit"), "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": rec.pop("ms_per_step"),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic"}
+    cfg = rec.pop("config")
+    cfg["parallelism"] = f"replicas{ws}" if ws > 1 else "single"
+    line["config"] = cfg
+    line.update(rec)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def bench_csr(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    bw = load_pkg()
+    bw.build()
+    clocks = ClockSampler(local)
+    clocks.start()
+    rec = csr_record(args, bw, dev, args.steps, args.warmup, args.scale)
+    clk = clocks.stop()
+    line = {"metric": "exact sparse-key rank lookups/s (CSR rank-LUT, point)", "value": rec.pop("value"),
+            "unit": rec.pop("unit"), "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": rec.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic", "clocks": clk}
+    line.update(rec)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
 
 
 def main():
@@ -614,132 +950,7 @@ def main():
         return bench_batched(args)
     if args.workload == "serving":
         return bench_serving(args)
-    import torch
-    ws, rank, local = dist_env()
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device(f"cuda:{local}"))
-    torch.cuda.set_device(local)
-    dev = torch.device(f"cuda:{local}")
-    bw = load_pkg()
-    bw.build()
-    w = bw.workloads.make(args.workload, args.seed, args.scale)
-    S, E, Q = len(w.parent), len(w.events), len(w.queries)
-
-    h_parent = torch.from_numpy(w.parent).pin_memory()
-    h_events = torch.from_numpy(w.events.view(np.int64).reshape(-1, 2)).pin_memory()
-    h_queries = torch.from_numpy(w.queries.view(np.int32).reshape(-1, 3)).pin_memory()
-    h_answers = torch.empty(Q, dtype=torch.int64).pin_memory()
-    d_parent = h_parent.to(dev)
-    d_events = h_events.to(dev)
-    d_queries = h_queries.to(dev)
-    d_answers = torch.empty(Q, dtype=torch.int64, device=dev)
-    plan = bw.Replay(d_parent, w.n_keys, E, Q, blocks=args.blocks, chain=w.chain, timing=True)
-    stream = torch.cuda.current_stream(dev)
-
-    # warm-up + correctness check (every answer against the oracle)
-    for i in range(args.warmup):
-        plan.launch(d_parent, d_events, d_queries, d_answers)
-        if i == 0:
-            st = plan.status()
-            if st:
-                raise SystemExit(f"device rejected the workload: {bw.STATUS_NAMES.get(st, st)}")
-    torch.cuda.synchronize()
-    ans0 = d_answers.cpu().numpy()
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-    # every answer against the oracle's preorder replay (linear in events + queries;
-    # an ancestor walk per sampled query is quadratic on long chains)
-    want = oracle.ev_sweep(w.parent, w.n_keys, w.events, w.queries)
-    if not np.array_equal(ans0, want):
-        raise SystemExit("GPU answers differ from the oracle")
-    digest = oracle.sha256_hex(ans0.tobytes())
-
-    # ---- timed region (device-resident inputs)
-    clocks = ClockSampler(local)
-    kernels, blocks = plan.info()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    plan.timing_reset()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
-    for _ in range(args.steps):
-        plan.launch(d_parent, d_events, d_queries, d_answers)
-    t1.record(stream)
-    torch.cuda.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    clk = clocks.stop()
-    ms = t0.elapsed_time(t1) / args.steps
-    stage_ms, n_timed = plan.stage_times()
-    stage_mean = {k: v / max(1, n_timed) for k, v in stage_ms.items()}
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    if not np.array_equal(d_answers.cpu().numpy(), ans0):
-        raise SystemExit("answers changed between steps")
-    value = ws * Q / (ms / 1e3)
-
-    # ---- e2e through the public API with host buffers
-    e2e = None
-    if not args.no_e2e:
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            d_parent.copy_(h_parent, non_blocking=True)
-            d_events.copy_(h_events, non_blocking=True)
-            d_queries.copy_(h_queries, non_blocking=True)
-            plan.launch(d_parent, d_events, d_queries, d_answers)
-            h_answers.copy_(d_answers, non_blocking=True)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ems = e0.elapsed_time(e1) / args.steps
-        if ws > 1:
-            t = torch.tensor([ems], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ems = float(t.item())
-        if not np.array_equal(h_answers.numpy(), ans0):
-            raise SystemExit("e2e answers differ")
-        e2e = {"value": ws * Q / (ems / 1e3), "unit": "answers/s",
-               "h2d_bytes_per_step": 4 * S + 16 * E + 12 * Q, "d2h_bytes_per_step": 8 * Q,
-               "ms_per_step": ems}
-
-    peak, peak_kind = measured_peaks()
-    sweep_bytes = 16 * E + 20 * Q
-    sweep_ms = stage_mean["sweep"]
-    achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9
-    traffic = profiled_traffic(w.name)
-    line = {
-        "metric": METRIC, "value": value, "unit": "answers/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int64", "data": "synthetic",
-        "config": dict(w.describe(), blocks=blocks, l2="inputs larger than L2 (no flush needed)",
-                       answers_sha256=digest, parallelism=f"replicas{ws}" if ws > 1 else "single"),
-        "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": sweep_bytes,
-                     "mean_launch_ms": sweep_ms},
-        "pipeline": {"stages_ms": stage_mean,
-                     "whole_step_gbs": w.algorithmic_bytes / (ms / 1e3) / 1e9,
-                     "whole_step_frac": w.algorithmic_bytes / (ms / 1e3) / 1e9 / peak},
-        "gpu_launches": kernels * args.steps,
-        "clocks": clk,
-    }
-    if e2e:
-        line["e2e"] = e2e
-    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if ws > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+    return bench_plain(args)
 
 
 if __name__ == "__main__":

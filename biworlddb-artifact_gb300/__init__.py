@@ -30,11 +30,14 @@ PKG = _build.PKG
 BW_EINVAL = 1001
 BW_REPLAY_CHAIN_HINT = 1
 BW_REPLAY_TIMING = 2
+BW_REPLAY_CHAIN_KERNEL = 4
+BW_REPLAY_GENERAL = 8
+PATH_FLAGS = {"auto": 0, "chain": BW_REPLAY_CHAIN_KERNEL, "general": BW_REPLAY_GENERAL}
 STAGES = ["ingest", "linearise", "blocks", "prepare", "carry", "sweep"]
 STATUS_NAMES = {0: "ok", 1: "events not grouped by state", 2: "event key out of range",
                 3: "queries not grouped by state", 4: "query bound out of range",
                 5: "bad parent array", 6: "too many key slices in a block",
-                7: "state id out of range"}
+                7: "state id out of range", 8: "a bounded device wait gave up"}
 
 
 class BwReplayArgs(C.Structure):
@@ -68,7 +71,7 @@ class BwForestTuning(C.Structure):
 class BwServeConfig(C.Structure):
     _fields_ = [("n_states", C.c_int32), ("parent", C.c_void_p), ("n_keys", C.c_uint32), ("n_events", C.c_int64),
                 ("events", C.c_void_p), ("max_versions", C.c_int32), ("max_events", C.c_int64),
-                ("hbm_cap_bytes", C.c_size_t), ("chain_limit", C.c_int32)]
+                ("hbm_cap_bytes", C.c_size_t), ("chain_limit", C.c_int32), ("spin_limit", C.c_uint32)]
 
 
 class BwServeStats(C.Structure):
@@ -81,9 +84,11 @@ class BwServeStats(C.Structure):
                 for k, _ in self._fields_ if k != "reserved"}
 
 
-GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch",
+GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch", "gpu_v7b_snap_launch",
+               "gpu_v7b_launch", "gpu_v7b_combine_launch", "gpu_sess_reset_launch", "gpu_sess_run_launch",
+               "gpu_sess_snap_launch", "gpu_sess_combine_launch",
                "bw_replay_workspace_size", "bw_replay_launch", "bw_replay_status",
-               "bw_replay_last_info", "bw_replay_timing_reset", "bw_replay_stage_times",
+               "bw_replay_last_info", "bw_replay_path", "bw_replay_timing_reset", "bw_replay_stage_times",
                "bw_device_info", "bw_replay_launch_noalloc",
                "bw_csr_workspace_size", "bw_csr_build", "bw_csr_point", "bw_csr_range", "bw_csr_status",
                "bw_forest_create", "bw_forest_workspace_size", "bw_forest_bind", "bw_forest_launch",
@@ -115,6 +120,7 @@ def gpu_lib(build_if_missing: bool = True):
         L.bw_replay_status.argtypes = [C.POINTER(BwReplayArgs), C.POINTER(C.c_int32)]
         L.bw_replay_last_info.argtypes = [C.POINTER(BwReplayArgs), C.POINTER(C.c_int32),
                                           C.POINTER(C.c_int32)]
+        L.bw_replay_path.argtypes = [C.POINTER(BwReplayArgs), C.POINTER(C.c_int32)]
         L.bw_device_info.argtypes = [C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.bw_replay_stage_times.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_int32)]
         L.bw_v7_carry_launch.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -169,7 +175,7 @@ class Replay:
     """Reusable replay plan: holds the device workspace for one input shape."""
 
     def __init__(self, parent, n_keys: int, n_events: int, n_queries: int, *, blocks: int = 0,
-                 chain: bool = False, timing: bool = False, device=None):
+                 chain: bool = False, timing: bool = False, path: str = "auto", device=None):
         torch = _torch()
         self.lib = gpu_lib()
         self.device = device or parent.device
@@ -180,7 +186,7 @@ class Replay:
         a.n_events = int(n_events)
         a.n_queries = int(n_queries)
         a.blocks = int(blocks)
-        a.flags = (BW_REPLAY_CHAIN_HINT if chain else 0) | (BW_REPLAY_TIMING if timing else 0)
+        a.flags = (BW_REPLAY_CHAIN_HINT if chain else 0) | (BW_REPLAY_TIMING if timing else 0) | PATH_FLAGS[path]
         nbytes = C.c_size_t(0)
         _check(self.lib.bw_replay_workspace_size(C.byref(a), C.byref(nbytes)), "workspace size")
         self.workspace = torch.empty(max(int(nbytes.value), 256), dtype=torch.uint8, device=self.device)
@@ -227,12 +233,24 @@ class Replay:
         self.lib.bw_replay_last_info(C.byref(self.args), C.byref(k), C.byref(b))
         return int(k.value), int(b.value)
 
+    def chain_path(self, events=None) -> bool:
+        """Whether these arguments take the single-pass chain path (host decision)."""
+        a = self.args
+        if events is not None:
+            a.events = events.data_ptr() if a.n_events else None
+        out = C.c_int32(0)
+        _check(self.lib.bw_replay_path(C.byref(a), C.byref(out)), "bw_replay_path")
+        return bool(out.value)
+
 
 def replay(parent, n_keys: int, events, queries, *, blocks: int = 0, chain: bool = False,
-           check: bool = True):
-    """One replay on the current CUDA stream; returns int64 answers on the device."""
+           check: bool = True, path: str = "auto"):
+    """One replay on the current CUDA stream; returns int64 answers on the device.
+    ``path``: "auto" (the chain path for event-heavy chains with small key domains,
+    else the general pipeline), "chain" or "general" to force one (chain needs
+    ``chain=True``)."""
     torch = _torch()
-    r = Replay(parent, n_keys, events.shape[0], queries.shape[0], blocks=blocks, chain=chain)
+    r = Replay(parent, n_keys, events.shape[0], queries.shape[0], blocks=blocks, chain=chain, path=path)
     answers = torch.empty(queries.shape[0], dtype=torch.int64, device=parent.device)
     r.launch(parent, events, queries, answers)
     if check:
@@ -480,7 +498,7 @@ class Server:
     records served with open-loop arrival times."""
 
     def __init__(self, parent, n_keys: int, events, *, max_versions: int, max_events: int,
-                 hbm_cap_bytes: int, chain_limit: int = 0):
+                 hbm_cap_bytes: int, chain_limit: int = 0, spin_limit: int = 0):
         import numpy as np
         _torch()
         self.lib = gpu_lib()
@@ -490,7 +508,7 @@ class Server:
             raise TypeError("events must be workloads.EVENT_DTYPE records")
         cfg = BwServeConfig(int(par.size), par.ctypes.data, int(n_keys), int(ev.size),
                             ev.ctypes.data if ev.size else None, int(max_versions), int(max_events),
-                            int(hbm_cap_bytes), int(chain_limit))
+                            int(hbm_cap_bytes), int(chain_limit), int(spin_limit))
         self.handle = C.c_void_p()
         _check(self.lib.bw_serve_create(C.byref(cfg), C.byref(self.handle)), "bw_serve_create")
         self.n_keys = int(n_keys)
@@ -806,6 +824,117 @@ def run_v7_plan(plan: dict):
     _check(L.gpu_combine_launch(C.byref(ca)), "gpu_combine_launch")
     torch.cuda.synchronize()
     return answers.cpu().numpy(), dV.cpu().numpy(), lvals.cpu().numpy()
+
+
+class GpuV7bArgs(C.Structure):
+    _fields_ = [("B", C.c_int), ("G", C.c_int), ("Cpfx", C.c_int), ("ncls", C.c_int), ("q", C.c_int),
+                ("nodes", C.c_void_p), ("bv0", C.c_void_p), ("bv1", C.c_void_p), ("fac_start", C.c_void_p),
+                ("g2row", C.c_void_p), ("ms_off", C.c_void_p), ("ms_cls", C.c_void_p), ("ms_base", C.c_void_p),
+                ("ms_dev", C.c_void_p), ("devbuf", C.c_void_p), ("need_off", C.c_void_p), ("qlb", C.c_void_p),
+                ("qhb", C.c_void_p), ("lvals", C.c_void_p), ("dV", C.c_void_p), ("threads", C.c_int),
+                ("shared_bytes", C.c_int)]
+
+
+class GpuSessRunArgs(C.Structure):
+    _fields_ = GpuV7bArgs._fields_[:-2] + [("fen", C.c_void_p), ("leaf", C.c_void_p), ("threads", C.c_int)]
+
+
+class GpuV7bSnapArgs(C.Structure):
+    _fields_ = [("nstates", C.c_int), ("nodes", C.c_void_p), ("bidx", C.c_void_p), ("gb_off", C.c_void_p),
+                ("gb_block", C.c_void_p), ("gb_reg", C.c_void_p), ("devbuf", C.c_void_p)]
+
+
+class GpuSessResetArgs(C.Structure):
+    _fields_ = [("B", C.c_int), ("Cpfx", C.c_int), ("fen", C.c_void_p), ("leaf", C.c_void_p)]
+
+
+def compact_plan(plan: dict) -> dict:
+    """The v7b / session form of a v7 plan (gpu_v7b.h:6-21): 40-byte nodes (kind bits
+    1 row, 2 factor, 4 ex_old, 8 ex_new; a, b = amt_old, amt_new or fac_val, fac_prev)
+    and the (group, block) occurrence tables of the device snapshot entry."""
+    import numpy as np
+    n = plan["nodes"]
+    dt = np.dtype([("kind", "u1"), ("pad0", "u1"), ("g_old", "<i2"), ("g_new", "<i2"), ("pad1", "u1", (2,)),
+                   ("c_old", "<i4"), ("c_new", "<i4"), ("ti_old", "<i4"), ("ti_new", "<i4"),
+                   ("a", "<i8"), ("b", "<i8")])
+    assert dt.itemsize == 40
+    cn = np.zeros(n.size, dtype=dt)
+    row, fac = n["kind"] == 1, n["kind"] == 2
+    cn["kind"] = n["kind"] | (n["ex_old"].astype(np.int32) << 2) | (n["ex_new"].astype(np.int32) << 3)
+    cn["g_old"], cn["g_new"] = n["g_old"], n["g_new"]
+    cn["c_old"], cn["c_new"], cn["ti_old"], cn["ti_new"] = n["c_old"], n["c_new"], n["ti_old"], n["ti_new"]
+    cn["a"] = np.where(row, n["amt_old"], np.where(fac, n["fac_val"], 0))
+    cn["b"] = np.where(row, n["amt_new"], np.where(fac, n["fac_prev"], 0))
+    B, G = plan["B"], plan["G"]
+    need = plan["need_off"].reshape(B, G)
+    gb_off, gb_block, gb_reg = [0], [], []
+    for g in range(G):
+        bs = np.nonzero(need[:, g] >= 0)[0]
+        gb_block += bs.tolist()
+        gb_reg += need[bs, g].tolist()
+        gb_off.append(len(gb_block))
+    return {"nodes": cn, "gb_off": np.array(gb_off, np.int32), "gb_block": np.array(gb_block or [0], np.int32),
+            "gb_reg": np.array(gb_reg or [0], np.int64)}
+
+
+def run_v7b_plan(plan: dict, session: bool = False, batches: int = 1):
+    """Drive the compact drop-in ABI as the reference's snapshot worker (gpu_v7b.h,
+    panel_batch_gpu2.cpp:193-244) or session worker (gpu_session.h,
+    panel_gpu_session.cpp:110-137) do: device snapshots into a zeroed devbuf, block
+    replay (session: reset + run per batch, prefix structure in global memory), carry,
+    combine.  Returns (answers, devbuf after the snapshot entry)."""
+    import numpy as np
+    torch = _torch()
+    L = gpu_lib()
+    dev = torch.device("cuda")
+    cp = compact_plan(plan)
+
+    def up(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8)).to(dev)
+    d = {k: up(plan[k]) for k in ("block_v0", "block_v1", "fac_start", "g2row", "ms_off", "ms_cls", "ms_base",
+                                  "ms_dev", "need_off", "qlb", "qhb", "bidx", "vbase")}
+    d.update({k: up(cp[k]) for k in ("nodes", "gb_off", "gb_block", "gb_reg")})
+    B, Cp, q, S, G = plan["B"], plan["Cpfx"], plan["q"], plan["n_states"], plan["G"]
+    devbuf = torch.zeros(max(1, plan["devbuf"].size), dtype=torch.int64, device=dev)
+    lvals = torch.empty((S - 1) * 2 * q, dtype=torch.int64, device=dev)
+    dV = torch.empty(B * Cp, dtype=torch.int64, device=dev)
+    carry = torch.empty(B * Cp, dtype=torch.int64, device=dev)
+    answers = torch.empty((S - 1) * q, dtype=torch.int64, device=dev)
+    torch.cuda.synchronize()
+    sa = GpuV7bSnapArgs(S, d["nodes"].data_ptr(), d["bidx"].data_ptr(), d["gb_off"].data_ptr(),
+                        d["gb_block"].data_ptr(), d["gb_reg"].data_ptr(), devbuf.data_ptr())
+    for name in ("gpu_v7b_snap_launch", "gpu_sess_snap_launch", "gpu_v7b_launch", "gpu_sess_run_launch",
+                 "gpu_sess_reset_launch", "gpu_v7b_combine_launch", "gpu_sess_combine_launch"):
+        getattr(L, name).argtypes = [C.c_void_p]
+    _check((L.gpu_sess_snap_launch if session else L.gpu_v7b_snap_launch)(C.byref(sa)), "snapshot entry")
+    torch.cuda.synchronize()
+    snap = devbuf.cpu().numpy().copy()
+    common = (B, G, Cp, plan["ncls"], q, d["nodes"].data_ptr(), d["block_v0"].data_ptr(), d["block_v1"].data_ptr(),
+              d["fac_start"].data_ptr(), d["g2row"].data_ptr(), d["ms_off"].data_ptr(), d["ms_cls"].data_ptr(),
+              d["ms_base"].data_ptr(), d["ms_dev"].data_ptr(), devbuf.data_ptr(), d["need_off"].data_ptr(),
+              d["qlb"].data_ptr(), d["qhb"].data_ptr(), lvals.data_ptr(), dV.data_ptr())
+    ca = GpuV7CombineArgs(S - 1, q, Cp, d["qlb"].data_ptr(), d["qhb"].data_ptr(), carry.data_ptr(),
+                          d["bidx"].data_ptr(), lvals.data_ptr(), answers.data_ptr())
+    if session:
+        fen = torch.empty(B * Cp, dtype=torch.int64, device=dev)
+        leaf = torch.empty(B * Cp, dtype=torch.int64, device=dev)
+        ra = GpuSessRunArgs(*common, fen.data_ptr(), leaf.data_ptr(), 256)
+        snap_dev = devbuf.clone()   # each batch replays from the snapshots (panel_gpu_session.cpp:111-131)
+        for _ in range(max(1, batches)):
+            devbuf.copy_(snap_dev)
+            _check(L.gpu_sess_reset_launch(C.byref(GpuSessResetArgs(B, Cp, fen.data_ptr(), leaf.data_ptr()))),
+                   "gpu_sess_reset_launch")
+            _check(L.gpu_sess_run_launch(C.byref(ra)), "gpu_sess_run_launch")
+            _check(L.bw_v7_carry_launch(B, Cp, d["vbase"].data_ptr(), dV.data_ptr(), carry.data_ptr(), None),
+                   "bw_v7_carry_launch")
+            _check(L.gpu_sess_combine_launch(C.byref(ca)), "gpu_sess_combine_launch")
+    else:
+        _check(L.gpu_v7b_launch(C.byref(GpuV7bArgs(*common, 256, 0))), "gpu_v7b_launch")
+        _check(L.bw_v7_carry_launch(B, Cp, d["vbase"].data_ptr(), dV.data_ptr(), carry.data_ptr(), None),
+               "bw_v7_carry_launch")
+        _check(L.gpu_v7b_combine_launch(C.byref(ca)), "gpu_v7b_combine_launch")
+    torch.cuda.synchronize()
+    return answers.cpu().numpy(), snap
 
 
 def replay_noalloc(parent, n_keys: int, events, queries, *, blocks: int = 0, chain: bool = False):

@@ -92,10 +92,8 @@ def build(force: bool = False, verbose: bool = False) -> None:
     if host_objs:
         subprocess.run(["g++", "-shared", "-fopenmp", "-o", str(HOST_LIB), *map(str, host_objs)],
                        check=True)
-        wsrc = CSRC / "worker_main.cpp"
-        if wsrc.exists():
-            subprocess.run([nvcc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fopenmp,-ffp-contract=off",
-                            "-I", str(INCLUDE), "-I", str(CSRC), str(wsrc), *map(str, host_objs),
-                            *map(str, sorted(objdir.glob("*.o"))[:0]), "-L", str(PKG),
-                            "-lbwgpu", "-lgomp", f"-Xlinker=-rpath,{PKG}", "-o", str(WORKER)],
-                           check=True)
+        # the worker: host objects linked in, the CUDA library by rpath
+        subprocess.run([nvcc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fopenmp,-ffp-contract=off",
+                        "-I", str(INCLUDE), "-I", str(CSRC), str(CSRC / "worker_main.cpp"), *map(str, host_objs),
+                        "-L", str(PKG), "-lbwgpu", "-lgomp", f"-Xlinker=-rpath,{PKG}", "-o", str(WORKER)],
+                       check=True)

@@ -1,0 +1,665 @@
+// bw_chain.cu -- single-pass replay of a linear version chain (see bw_chain.cuh).
+//
+// Sweep (k_chain_sweep, one CTA per state block, 512 threads):
+//   * the block's events [e0, e1) stream through a ring of kChainStages tiles of
+//     kChainTile events, each tile one cp.async.bulk copy from global memory into
+//     shared memory completed on the stage's mbarrier (bounded waits);
+//   * the running key histogram of the block lives in shared memory as exact
+//     int32 window accumulators H[key] plus lane-replicated chunk totals T[chunk]
+//     (each lane of a warp adds into its own copy, so chunk updates never collide).
+//     A window holds events whose absolute sum stays below 2^28 + 2^29, so every
+//     partial sum of it is exact in int32; before it can grow past that it is
+//     flushed into the block's int64 row in global memory (plus int64 chunk
+//     totals in shared memory).  Tiles with a large delta (a thread's two events
+//     summing to >= 2^20 in magnitude) bypass the window: they add straight into
+//     the int64 row with 64-bit global atomics;
+//   * a tile owns the queries whose position (number of events at or before their
+//     state) falls inside it: state < state of the tile's last event.  Their local
+//     answer = the window + row probe over [lo, hi) before the tile is applied,
+//     plus the tile's events at or before the query's state inside [lo, hi);
+//     one warp per query, int32 lane sums reduced with redux.sync;
+//   * one warp (the last) finds the next tile's queries while the others apply
+//     the current tile: its query states are prefetched into registers one tile
+//     ahead, its records copied into shared memory.
+// Carry (k_chain_colsum, k_chain_colfix): exclusive column scan over the block
+// rows in two passes (segment sums, then segment-local prefixes), in place.
+// Fix-up (k_chain_fixup): each block's carry row is scanned over keys in place and
+// every query of the block adds row[hi] - row[lo].
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <mutex>
+
+#include "bw_gpu.h"
+#include "bw_common.cuh"
+#include "bw_chain.cuh"
+
+namespace bw {
+namespace {
+
+constexpr int NT = kChainThreads;
+constexpr int NW = NT / 32;
+constexpr int QW = NW - 1;                       // the query warp
+constexpr int TE = kChainTile;
+constexpr int NS = kChainStages;
+constexpr int QB = kChainQBuf;
+constexpr uint32_t kWaitLimit = 1u << 22;        // mbarrier polls before a stage is declared lost
+constexpr uint64_t kBigThread = 1ull << 20;      // a thread's |delta| sum below which its tile is int32-safe
+constexpr uint32_t kFlushAt = 1u << 28;          // window |delta| sum that triggers a flush
+
+struct ChainParams {
+  const uint4* ev;        // events as 16-byte records (state, key, delta lo, delta hi)
+  const BwQuery* qs;
+  int64_t* ans;
+  const int32_t* parent;
+  int64_t E, Q;
+  int32_t S;
+  uint32_t C;
+  int32_t B;
+  int32_t chs, nch, nseg;
+  int64_t* rows;          // B rows of C+1 int64
+  int64_t* btab;          // B x (first query, end query)
+  int64_t* seg;           // nseg rows of C+1 uint64
+  int32_t* status;
+};
+
+// Shared words written in one tile and read in the next are double-buffered by
+// tile parity: a fast warp may already write the next tile's copy while a slow one
+// still reads this tile's.
+struct Misc {
+  uint32_t wsum[2][NW];   // per-warp |delta| sum of a tile's window updates
+  int64_t tq[2][2];       // queries [tq0, tq1) of a tile
+  uint32_t prev_state[2]; // state of the event before a tile
+  int64_t tail_q0;
+};
+
+// Dynamic shared memory of the sweep, every region 16-byte aligned.
+struct SweepSmem {
+  size_t ring, H, T, T64, qbuf, bar, misc, bytes;
+};
+__host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
+__host__ __device__ inline SweepSmem sweep_smem(uint32_t C, int nch) {
+  SweepSmem L;
+  size_t o = 0;
+  L.ring = o;  o = al16(o + (size_t)NS * TE * 16);
+  L.H = o;     o = al16(o + (size_t)C * 4);
+  L.T = o;     o = al16(o + (size_t)nch * 32 * 4);
+  L.T64 = o;   o = al16(o + (size_t)nch * 8);
+  L.qbuf = o;  o = al16(o + (size_t)QB * 12);
+  L.bar = o;   o = al16(o + (size_t)NS * 8);
+  L.misc = o;  o = al16(o + sizeof(Misc));
+  L.bytes = o;
+  return L;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Bounded wait for phase `parity` of a stage barrier; false when it never completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void set_status(int32_t* st, int32_t code) {
+  if (*reinterpret_cast<volatile int32_t*>(st) == 0) atomicCAS(st, 0, code);
+}
+
+__device__ __forceinline__ uint64_t uabs64(uint64_t d) {
+  return (int64_t)d < 0 ? (uint64_t)0 - d : d;
+}
+
+__device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Lane share of the window sum over keys [lo, hi): partial chunks from H, whole
+// chunks from the lane's own chunk-total copy.
+__device__ __forceinline__ int32_t probe32(const int32_t* H, const int32_t* T, uint32_t lo, uint32_t hi, int chs,
+                                           int lane) {
+  const uint32_t clo = (lo + (1u << chs) - 1) >> chs, chi = hi >> chs;
+  int32_t s = 0;
+  if (clo >= chi) {
+    for (uint32_t k = lo + lane; k < hi; k += 32) s += H[k];
+    return s;
+  }
+  for (uint32_t k = lo + lane; k < (clo << chs); k += 32) s += H[k];
+  for (uint32_t c = clo; c < chi; ++c) s += T[c * 32 + lane];
+  for (uint32_t k = (chi << chs) + lane; k < hi; k += 32) s += H[k];
+  return s;
+}
+
+// Lane share of the int64 row over [lo, hi): partial chunks from the row, whole
+// chunks from the int64 chunk totals.  Row words are read from L2 (__ldcg): wide
+// tiles update them with global atomics, which do not update L1.
+__device__ __forceinline__ uint64_t probe64(const int64_t* row, const unsigned long long* T64, uint32_t lo,
+                                            uint32_t hi, int chs, int lane) {
+  const uint32_t clo = (lo + (1u << chs) - 1) >> chs, chi = hi >> chs;
+  uint64_t s = 0;
+  if (clo >= chi) {
+    for (uint32_t k = lo + lane; k < hi; k += 32) s += (uint64_t)__ldcg(row + k);
+    return s;
+  }
+  for (uint32_t k = lo + lane; k < (clo << chs); k += 32) s += (uint64_t)__ldcg(row + k);
+  for (uint32_t c = clo + lane; c < chi; c += 32) s += T64[c];
+  for (uint32_t k = (chi << chs) + lane; k < hi; k += 32) s += (uint64_t)__ldcg(row + k);
+  return s;
+}
+
+// Lane share of the tile's events at or before state qst with key in [lo, hi).
+template <bool WIDE>
+__device__ __forceinline__ uint64_t tile_corr(const uint4* tile, int n, uint32_t qst, uint32_t lo, uint32_t hi,
+                                              int lane) {
+  uint64_t s = 0;
+  int32_t s32 = 0;
+  for (int base = 0; base < n; base += 32) {
+    const int j = base + lane;
+    bool le = false;
+    if (j < n) {
+      const uint4 e = tile[j];
+      le = e.x <= qst;
+      if (le && e.y >= lo && e.y < hi) {
+        if (WIDE) s += ((uint64_t)e.w << 32) | e.z;
+        else s32 += (int32_t)e.z;
+      }
+    }
+    if (!__all_sync(0xffffffffu, le)) break;
+  }
+  return WIDE ? s : (uint64_t)(uint32_t)s32;
+}
+
+// First query index in [0, Q) whose state is >= x (Q when none), found by the
+// whole CTA in rounds of NT probes.
+__device__ int64_t first_query_at_or_after(const BwQuery* qs, int64_t Q, uint32_t x) {
+  int64_t lo = 0, hi = Q;
+  while (true) {
+    const int64_t n = hi - lo;
+    if (n <= 0) return lo;
+    const int64_t step = (n + NT - 1) / NT;
+    const int64_t pos = lo + (int64_t)threadIdx.x * step;
+    const bool lt = pos < hi && qs[pos].state < x;
+    const int cnt = __syncthreads_count(lt);
+    if (step == 1) return lo + cnt;
+    const int64_t nlo = cnt ? lo + (int64_t)(cnt - 1) * step + 1 : lo;
+    hi = min(hi, lo + (int64_t)cnt * step);
+    lo = nlo;
+  }
+}
+
+// The query warp's prefetched window of 32 query records.
+struct QCache {
+  int64_t base;
+  uint32_t st, lo, hi;
+};
+
+__device__ __forceinline__ void qcache_fetch(QCache& c, const BwQuery* qs, int64_t Q, int64_t base, int lane) {
+  c.base = base;
+  const int64_t i = base + lane;
+  if (i < Q) {
+    const uint32_t* r = reinterpret_cast<const uint32_t*>(qs + i);
+    c.st = r[0];
+    c.lo = r[1];
+    c.hi = r[2];
+  } else {
+    c.st = 0xffffffffu;
+    c.lo = c.hi = 0;
+  }
+}
+
+// Query warp: the queries of the tile whose last event has state x are those from
+// qcur on with state < x.  Their records go to qbuf (the first QB), their range to
+// tq; qcur advances past them.
+__device__ void find_tile_queries(const ChainParams& p, QCache& c, int64_t& qcur, uint32_t x, uint32_t* qbuf,
+                                  int64_t* tq, int lane) {
+  const int64_t tq0 = qcur;
+  while (true) {
+    if (c.base != qcur) qcache_fetch(c, p.qs, p.Q, qcur, lane);
+    const bool valid = qcur + lane < p.Q;
+    const uint32_t ball = __ballot_sync(0xffffffffu, valid && c.st < x);
+    const int n = ball == 0xffffffffu ? 32 : __ffs(~ball) - 1;
+    if (lane < n) {
+      const int64_t slot = qcur - tq0 + lane;
+      if (slot < QB) {
+        qbuf[3 * slot] = c.st;
+        qbuf[3 * slot + 1] = c.lo;
+        qbuf[3 * slot + 2] = c.hi;
+      }
+    }
+    qcur += n;
+    if (n < 32) break;
+    qcache_fetch(c, p.qs, p.Q, qcur, lane);
+  }
+  if (lane == 0) {
+    tq[0] = tq0;
+    tq[1] = qcur;
+  }
+  qcache_fetch(c, p.qs, p.Q, qcur, lane);   // consumed at the next tile
+}
+
+// Answer of one query by one warp: window + row probe, plus the tile correction
+// (tile == nullptr: no correction).
+__device__ __forceinline__ int64_t answer_one(const ChainParams& p, const int32_t* H, const int32_t* T,
+                                              const unsigned long long* T64, const int64_t* row, bool rows_live,
+                                              bool wide_tile, const uint4* tile, int n, uint32_t qst, uint32_t lo,
+                                              uint32_t hi, int lane) {
+  lo = min(lo, p.C);
+  hi = min(hi, p.C);
+  if (lo >= hi) return 0;
+  int32_t part = probe32(H, T, lo, hi, p.chs, lane);
+  uint64_t wide = 0;
+  if (tile) {
+    if (wide_tile) wide = tile_corr<true>(tile, n, qst, lo, hi, lane);
+    else part += (int32_t)(uint32_t)tile_corr<false>(tile, n, qst, lo, hi, lane);
+  }
+  int64_t total = (int64_t)(int32_t)__reduce_add_sync(0xffffffffu, (uint32_t)part);
+  if (rows_live || wide_tile) {
+    if (rows_live) wide += probe64(row, T64, lo, hi, p.chs, lane);
+    total = (int64_t)((uint64_t)total + warp_sum_u64(wide));
+  }
+  return total;
+}
+
+__global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const uint32_t C = p.C;
+  const SweepSmem SL = sweep_smem(C, p.nch);
+  uint4* ring = reinterpret_cast<uint4*>(sm + SL.ring);
+  int32_t* H = reinterpret_cast<int32_t*>(sm + SL.H);
+  int32_t* T = reinterpret_cast<int32_t*>(sm + SL.T);
+  unsigned long long* T64 = reinterpret_cast<unsigned long long*>(sm + SL.T64);
+  uint32_t* qbuf = reinterpret_cast<uint32_t*>(sm + SL.qbuf);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + SL.bar);
+  Misc* m = reinterpret_cast<Misc*>(sm + SL.misc);
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int b = blockIdx.x;
+  const int64_t e0 = (int64_t)b * p.E / p.B, e1 = (int64_t)(b + 1) * p.E / p.B;
+  const int64_t ne = e1 - e0;
+  const int ntiles = (int)((ne + TE - 1) / TE);
+  int64_t* row = p.rows + (int64_t)b * (C + 1);
+  auto tile_n = [&](int t) { return (int)min((int64_t)TE, ne - (int64_t)t * TE); };
+
+  for (uint32_t i = tid; i < C; i += NT) H[i] = 0;
+  for (int i = tid; i < p.nch * 32; i += NT) T[i] = 0;
+  for (int i = tid; i < p.nch; i += NT) T64[i] = 0;
+  if (tid == 0) {
+    for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    m->prev_state[0] = b > 0 ? p.ev[e0 - 1].x : 0u;
+  }
+  __syncthreads();
+  int issued = 0;   // tiles whose copy was issued (thread 0)
+  if (tid == 0) {
+    for (; issued < NS && issued < ntiles; ++issued)
+      bulk_load(ring + (issued % NS) * TE, p.ev + e0 + (int64_t)issued * TE, (uint32_t)tile_n(issued) * 16u,
+                &bar[issued % NS]);
+  }
+  // input checks spread over every sweep thread: parent[v] = v - 1, and every query
+  // (sorted by state, state and bounds in range) -- queries behind an out-of-order
+  // one may never be reached by a tile, so they are checked here, not when consumed
+  for (int64_t v = (int64_t)b * NT + tid; v < p.S; v += (int64_t)p.B * NT)
+    if (p.parent[v] != (int32_t)(v - 1)) set_status(p.status, BW_STATUS_BAD_PARENT);
+  for (int64_t i = (int64_t)b * NT + tid; i < p.Q; i += (int64_t)p.B * NT) {
+    const uint32_t* r = reinterpret_cast<const uint32_t*>(p.qs + i);
+    const uint32_t qst = r[0], lo = r[1], hi = r[2];
+    if (i > 0 && qst < p.qs[i - 1].state) set_status(p.status, BW_STATUS_QUERIES_UNSORTED);
+    if (qst >= (uint32_t)p.S) set_status(p.status, BW_STATUS_STATE_RANGE);
+    if (lo > C || hi > C) set_status(p.status, BW_STATUS_QUERY_RANGE);
+  }
+  // the block's first query: position >= e0, i.e. state >= state of event e0 - 1
+  const int64_t qstart = b > 0 ? first_query_at_or_after(p.qs, p.Q, m->prev_state[0]) : 0;
+
+  QCache qc{-1, 0, 0, 0};
+  int64_t qcur = qstart;
+  if (warp == QW) qcache_fetch(qc, p.qs, p.Q, qcur, lane);
+
+  uint4 cur[kChainEvPerThread];
+  bool rows_live = false;   // the int64 row holds data (set by the first flush)
+  uint32_t win = 0;         // |delta| sum in the int32 window (the same in every thread)
+  int bigp = 0, lost = 0;
+  if (ntiles > 0) {
+    if (!mbar_wait(&bar[0], 0)) {
+      set_status(p.status, BW_STATUS_TIMEOUT);
+      lost = 1;
+    } else {
+      const int n = tile_n(0);
+      uint64_t s = 0;
+#pragma unroll
+      for (int k = 0; k < kChainEvPerThread; ++k) {
+        const int idx = tid + k * NT;
+        cur[k] = idx < n ? ring[idx] : make_uint4(0, 0, 0, 0);
+        if (idx < n) s += uabs64(((uint64_t)cur[k].w << 32) | cur[k].z);
+      }
+      bigp = s >= kBigThread;
+      if (warp == QW) find_tile_queries(p, qc, qcur, ring[n - 1].x, qbuf, m->tq[0], lane);
+    }
+  }
+  // end-of-tile barrier: OR of the next tile's wide flag and of lost waits (a
+  // second barrier separates the two only when the first is set)
+  auto tile_barrier = [&](int wide, int gone, int& big_out) -> bool {
+    if (!__syncthreads_or(wide | gone)) {
+      big_out = 0;
+      return false;
+    }
+    const bool ab = __syncthreads_or(gone);
+    big_out = __syncthreads_or(wide);
+    return ab;
+  };
+  int big = 0;
+  bool aborted = tile_barrier(bigp, lost, big);
+
+  int t = 0;
+  for (; t < ntiles && !aborted; ++t) {
+    const int n = tile_n(t);
+    const uint4* tile = ring + (t % NS) * TE;
+    if (tid == 0 && t >= 1 && issued < ntiles) {
+      // stage (t-1) % NS was released by the barrier that ended tile t-1
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bulk_load(ring + (issued % NS) * TE, p.ev + e0 + (int64_t)issued * TE, (uint32_t)tile_n(issued) * 16u,
+                &bar[issued % NS]);
+      ++issued;
+    }
+    const int64_t tq0 = m->tq[t & 1][0], tq1 = m->tq[t & 1][1];
+    if (t > 0) {   // window updates of the previous tile, summed over its warps
+      const uint4* w4 = reinterpret_cast<const uint4*>(m->wsum[(t - 1) & 1]);
+#pragma unroll
+      for (int i = 0; i < NW / 4; ++i) {
+        const uint4 v = w4[i];
+        win += v.x + v.y + v.z + v.w;
+      }
+    }
+    // flush the int32 window into the int64 row: before it could overflow, and
+    // before a wide tile (which adds straight into the row)
+    if (win >= kFlushAt || (big && (win > 0 || !rows_live))) {
+      for (uint32_t k = tid; k < C; k += NT) {
+        const int32_t v = H[k];
+        if (rows_live) {
+          if (v) row[k] = (int64_t)((uint64_t)__ldcg(row + k) + (uint64_t)(int64_t)v);
+        } else {
+          row[k] = v;
+        }
+        H[k] = 0;
+      }
+      for (int c = tid; c < p.nch; c += NT) {
+        int64_t s = 0;
+        for (int l = 0; l < 32; ++l) {
+          s += T[c * 32 + l];
+          T[c * 32 + l] = 0;
+        }
+        T64[c] += (unsigned long long)s;
+      }
+      win = 0;
+      rows_live = true;
+      __syncthreads();
+    }
+    // the tile's queries, one warp each
+    if (tq1 > tq0) {
+      for (int64_t i = tq0 + warp; i < tq1; i += NW) {
+        uint32_t qst, lo, hi;
+        if (i - tq0 < QB) {
+          const uint32_t* r = qbuf + 3 * (i - tq0);
+          qst = r[0];
+          lo = r[1];
+          hi = r[2];
+        } else {
+          const uint32_t* r = reinterpret_cast<const uint32_t*>(p.qs + i);
+          qst = r[0];
+          lo = r[1];
+          hi = r[2];
+        }
+        const int64_t a = answer_one(p, H, T, T64, row, rows_live, big != 0, tile, n, qst, lo, hi, lane);
+        if (lane == 0) p.ans[i] = a;
+      }
+      __syncthreads();
+    }
+    // apply the tile
+    uint32_t wsum = 0;
+#pragma unroll
+    for (int k = 0; k < kChainEvPerThread; ++k) {
+      const int idx = tid + k * NT;
+      if (idx < n) {
+        const uint4 e = cur[k];
+        const uint32_t prev = idx ? tile[idx - 1].x : m->prev_state[t & 1];
+        if (e.x < prev) set_status(p.status, BW_STATUS_EVENTS_UNSORTED);
+        if (e.x >= (uint32_t)p.S) set_status(p.status, BW_STATUS_STATE_RANGE);
+        if (e.y >= C) {
+          set_status(p.status, BW_STATUS_EVENT_KEY_RANGE);
+        } else if (!big) {
+          atomicAdd(&H[e.y], (int32_t)e.z);
+          atomicAdd(&T[(e.y >> p.chs) * 32 + lane], (int32_t)e.z);
+          wsum += (uint32_t)uabs64(((uint64_t)e.w << 32) | e.z);
+        } else {
+          const uint64_t d = ((uint64_t)e.w << 32) | e.z;
+          atomicAdd(reinterpret_cast<unsigned long long*>(row + e.y), (unsigned long long)d);
+          shared_add_u64(&T64[e.y >> p.chs], d);
+        }
+      }
+    }
+    {
+      const uint32_t ws = __reduce_add_sync(0xffffffffu, wsum);
+      if (lane == 0) m->wsum[t & 1][warp] = ws;
+    }
+    if (tid == 0) m->prev_state[(t + 1) & 1] = tile[n - 1].x;
+    // next tile: wait for its copy, load this thread's events, find its queries
+    bigp = 0;
+    if (t + 1 < ntiles) {
+      const int nn = tile_n(t + 1);
+      const uint4* nt = ring + ((t + 1) % NS) * TE;
+      if (!mbar_wait(&bar[(t + 1) % NS], (uint32_t)(((t + 1) / NS) & 1))) {
+        set_status(p.status, BW_STATUS_TIMEOUT);
+        lost = 1;
+      } else {
+        uint64_t s = 0;
+#pragma unroll
+        for (int k = 0; k < kChainEvPerThread; ++k) {
+          const int idx = tid + k * NT;
+          cur[k] = idx < nn ? nt[idx] : make_uint4(0, 0, 0, 0);
+          if (idx < nn) s += uabs64(((uint64_t)cur[k].w << 32) | cur[k].z);
+        }
+        bigp = s >= kBigThread;
+        if (warp == QW) find_tile_queries(p, qc, qcur, nt[nn - 1].x, qbuf, m->tq[(t + 1) & 1], lane);
+      }
+    }
+    aborted = tile_barrier(bigp, lost, big);
+  }
+
+  if (aborted) {
+    // wait (bounded) for the copies still in flight before the CTA exits: tiles
+    // from the one whose wait gave up to the last one issued
+    if (tid == 0)
+      for (int u = t; u < issued; ++u)
+        mbar_wait(&bar[u % NS], (uint32_t)((u / NS) & 1));
+    __syncthreads();
+    return;
+  }
+  // last block: the queries after its last event see every event of the chain
+  if (b == p.B - 1) {
+    const int64_t qend = p.Q;
+    if (warp == QW && lane == 0) m->tail_q0 = qcur;
+    __syncthreads();
+    const int64_t from = m->tail_q0;
+    for (int64_t i = from + warp; i < qend; i += NW) {
+      const uint32_t* r = reinterpret_cast<const uint32_t*>(p.qs + i);
+      const uint32_t qst = r[0], lo = r[1], hi = r[2];
+      const int64_t a = answer_one(p, H, T, T64, row, rows_live, false, nullptr, 0, qst, lo, hi, lane);
+      if (lane == 0) p.ans[i] = a;
+    }
+    if (warp == QW) qcur = qend;
+    __syncthreads();   // every probe has read the window and the row before the flush folds one into the other
+  }
+  // final flush: the block's whole key histogram into its row
+  for (uint32_t k = tid; k < C; k += NT) {
+    const int32_t v = H[k];
+    row[k] = rows_live ? (int64_t)((uint64_t)__ldcg(row + k) + (uint64_t)(int64_t)v) : (int64_t)v;
+  }
+  if (warp == QW && lane == 0) {
+    p.btab[2 * b] = qstart;
+    p.btab[2 * b + 1] = qcur;
+  }
+}
+
+// Segment sums of the block rows, column by column.
+__global__ void k_chain_colsum(ChainParams p) {
+  const uint32_t k = blockIdx.y * 256 + threadIdx.x;
+  if (k >= p.C) return;
+  const int b0 = blockIdx.x * kChainSegRows, b1 = min(p.B, b0 + kChainSegRows);
+  uint64_t s = 0;
+  for (int b = b0; b < b1; ++b) s += (uint64_t)p.rows[(int64_t)b * (p.C + 1) + k];
+  p.seg[(int64_t)blockIdx.x * (p.C + 1) + k] = (int64_t)s;
+}
+
+// Rows become exclusive column prefixes: the carry of each block.
+__global__ void k_chain_colfix(ChainParams p) {
+  const uint32_t k = blockIdx.y * 256 + threadIdx.x;
+  if (k >= p.C) return;
+  uint64_t run = 0;
+  for (int s = 0; s < (int)blockIdx.x; ++s) run += (uint64_t)p.seg[(int64_t)s * (p.C + 1) + k];
+  const int b0 = blockIdx.x * kChainSegRows, b1 = min(p.B, b0 + kChainSegRows);
+  for (int b = b0; b < b1; ++b) {
+    int64_t* x = p.rows + (int64_t)b * (p.C + 1) + k;
+    const uint64_t v = (uint64_t)*x;
+    *x = (int64_t)run;
+    run += v;
+  }
+}
+
+// Block b >= 1: its carry row scanned over keys (row[k] = carry below key k), then
+// every query of the block adds the carry inside [lo, hi).
+__global__ void __launch_bounds__(NT) k_chain_fixup(ChainParams p) {
+  const int b = blockIdx.x + 1;
+  int64_t* row = p.rows + (int64_t)b * (p.C + 1);
+  const uint32_t n = p.C + 1;
+  const uint32_t per = (n + NT - 1) / NT;
+  const uint32_t lo0 = threadIdx.x * per, hi0 = min(n, lo0 + per);
+  uint64_t local = 0;
+  for (uint32_t i = lo0; i < hi0; ++i) local += i < p.C ? (uint64_t)row[i] : 0;
+  uint64_t run = block_exclusive_scan<uint64_t>(local);
+  for (uint32_t i = lo0; i < hi0; ++i) {
+    const uint64_t v = i < p.C ? (uint64_t)row[i] : 0;
+    row[i] = (int64_t)run;
+    run += v;
+  }
+  __syncthreads();
+  const int64_t q0 = p.btab[2 * b], q1 = p.btab[2 * b + 1];
+  for (int64_t i = q0 + threadIdx.x; i < q1; i += NT) {
+    const BwQuery q = p.qs[i];
+    const uint32_t lo = min(q.lo, p.C), hi = min(q.hi, p.C);
+    if (lo < hi) p.ans[i] = (int64_t)((uint64_t)p.ans[i] + (uint64_t)row[hi] - (uint64_t)row[lo]);
+  }
+}
+
+std::once_flag g_attr_once;
+cudaError_t g_attr_err = cudaSuccess;
+
+}  // namespace
+
+bool chain_selected(const BwReplayArgs* a) {
+  if (!(a->flags & BW_REPLAY_CHAIN_HINT) || (a->flags & BW_REPLAY_GENERAL)) return false;
+  if (a->n_keys > kChainMaxKeys || a->n_states < 1) return false;
+  if (a->events && (reinterpret_cast<uintptr_t>(a->events) & 15) != 0) return false;
+  return (a->flags & BW_REPLAY_CHAIN_KERNEL) || a->n_queries * 8 <= a->n_events;
+}
+
+int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
+  s.S = a->n_states;
+  s.C = a->n_keys;
+  s.E = a->n_events;
+  s.Q = a->n_queries;
+  int lg = 0;
+  while ((1u << lg) < s.C) ++lg;
+  s.chs = lg - 5 > 5 ? lg - 5 : 5;
+  s.nch = (int32_t)((s.C + (1u << s.chs) - 1) >> s.chs);
+  s.smem = sweep_smem(s.C, s.nch).bytes;
+  s.ctas_per_sm = (int32_t)(kSmemPerSM / (s.smem + 1024));
+  if (s.ctas_per_sm > 2) s.ctas_per_sm = 2;   // __launch_bounds__(512, 2)
+  if (s.ctas_per_sm < 1) return BW_EINVAL;
+  int64_t B = a->blocks > 0 ? a->blocks : (s.E + kChainMinBlockEvents - 1) / kChainMinBlockEvents;
+  const int64_t cap = (int64_t)sms * s.ctas_per_sm;
+  if (a->blocks <= 0 && B > cap) B = cap;
+  if (B > s.E) B = s.E;
+  if (B < 1) B = 1;
+  if (B > (1 << 20)) return BW_EINVAL;
+  s.B = (int32_t)B;
+  s.nseg = (s.B + kChainSegRows - 1) / kChainSegRows;
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  size_t o = 256;   // status word
+  s.off_btab = o;  o = al(o + (size_t)s.B * 16);
+  s.off_rows = o;  o = al(o + (size_t)s.B * (s.C + 1) * 8);
+  s.off_seg = o;   o = al(o + (size_t)s.nseg * (s.C + 1) * 8);
+  s.total = o;
+  return 0;
+}
+
+int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int* kernels) {
+  std::call_once(g_attr_once, [] {
+    g_attr_err = cudaFuncSetAttribute(k_chain_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+  });
+  if (g_attr_err != cudaSuccess) return report(g_attr_err, "chain sweep attribute");
+  cudaStream_t st = static_cast<cudaStream_t>(a->stream);
+  char* ws = static_cast<char*>(a->workspace);
+  ChainParams p;
+  p.ev = reinterpret_cast<const uint4*>(a->events);
+  p.qs = a->queries;
+  p.ans = a->answers;
+  p.parent = a->parent;
+  p.E = s.E;
+  p.Q = s.Q;
+  p.S = s.S;
+  p.C = s.C;
+  p.B = s.B;
+  p.chs = s.chs;
+  p.nch = s.nch;
+  p.nseg = s.nseg;
+  p.rows = reinterpret_cast<int64_t*>(ws + s.off_rows);
+  p.btab = reinterpret_cast<int64_t*>(ws + s.off_btab);
+  p.seg = reinterpret_cast<int64_t*>(ws + s.off_seg);
+  p.status = reinterpret_cast<int32_t*>(ws);
+  int rc = report(cudaMemsetAsync(ws, 0, 4, st), "status reset");
+  if (rc) return rc;
+  if (evs) {
+    for (int i = 0; i <= BW_STAGE_SWEEP; ++i)
+      if ((rc = report(cudaEventRecord(evs->ev[i], st), "event record"))) return rc;
+  }
+  k_chain_sweep<<<s.B, NT, s.smem, st>>>(p);
+  int k = 1;
+  if ((rc = report(cudaGetLastError(), "chain sweep launch"))) return rc;
+  if (evs && (rc = report(cudaEventRecord(evs->ev[BW_STAGE_SWEEP + 1], st), "event record"))) return rc;
+  if (s.B > 1) {
+    const dim3 g((unsigned)s.nseg, (s.C + 255) / 256);
+    k_chain_colsum<<<g, 256, 0, st>>>(p);
+    k_chain_colfix<<<g, 256, 0, st>>>(p);
+    k_chain_fixup<<<s.B - 1, NT, 0, st>>>(p);
+    k += 3;
+    if ((rc = report(cudaGetLastError(), "chain carry launch"))) return rc;
+  }
+  if (evs) {
+    evs->chain = 1;
+    if ((rc = report(cudaEventRecord(evs->ev[BW_STAGE_COUNT + 1], st), "event record"))) return rc;
+  }
+  if (kernels) *kernels += k;
+  return 0;
+}
+
+}  // namespace bw

@@ -2330,6 +2330,7 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
   int kernels = 0;
   auto chk = [&](const char* what) { ++kernels; return report(cudaGetLastError(), what); };
   auto mark = [&](int i) { return timing ? report(cudaEventRecord(timing->ev[i], st), "event record") : 0; };
+  if (timing) timing->chain = 0;
   if ((rc = mark(0))) return rc;
 
   // ---- 0/1. init + ingest

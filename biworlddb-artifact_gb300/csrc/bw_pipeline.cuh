@@ -222,8 +222,13 @@ enum {
 // misc words
 enum { M_STATUS = 0, M_PREP_TICKET = 1, M_SWEEP_TICKET = 2, M_CHAIN = 3, M_PREPB_TICKET = 4, M_ROUNDS = 32 };  // 64 words
 
-// Stage timing events of one launch.
-struct EventSet { cudaEvent_t ev[BW_STAGE_COUNT + 1]; };
+// Stage timing events of one launch: stage i runs from ev[i] to ev[i + 1]; a chain
+// launch (chain = 1) records the sweep from ev[BW_STAGE_SWEEP] to ev[BW_STAGE_SWEEP+1]
+// and the carry that follows it up to ev[BW_STAGE_COUNT + 1].
+struct EventSet {
+  cudaEvent_t ev[BW_STAGE_COUNT + 2];
+  int chain = 0;
+};
 
 // Build the spec of a forest (tree shapes on the host).  Returns 0 or BW_EINVAL.
 int pipe_spec_forest(int32_t T, const int64_t* soff, const int64_t* eoff, const int64_t* qoff,

@@ -13,30 +13,28 @@
 //
 // The region, kNoAllocScratchBytes (32 MiB), is a file-scope __device__ array: every
 // GPU that loads this library holds it until the process exits.  Its device address
-// is looked up once per device (cudaGetSymbolAddress, with that device current) by
-// the first call made on that device; make that first call before any stream
-// capture.  All calls share the one region and the replay initialises every scratch
-// word it reads, so nothing is carried over between calls; calls whose work overlaps
-// on the GPU (different streams, or host threads racing) would overwrite each
-// other's scratch and must not be issued.  With a non-NULL `status` the call waits
-// for its stream and reports the device's input check (BW_STATUS_*); with NULL it
-// returns as soon as the work is enqueued.
+// is looked up on every call (cudaGetSymbolAddress, with the caller's device
+// current): the lookup allocates nothing, and the address stays right when the
+// module is reloaded at a different address after the primary context was torn
+// down (cudaDeviceReset).  The first call on a device loads the module there, so
+// make it before any stream capture.  All calls share the one region and the replay
+// initialises every scratch word it reads, so nothing is carried over between
+// calls; calls whose work overlaps on the GPU (different streams, or host threads
+// racing) would overwrite each other's scratch and must not be issued.  With a
+// non-NULL `status` the call waits for its stream and reports the device's input
+// check (BW_STATUS_*); with NULL it returns as soon as the work is enqueued and
+// that check is not reported (the next call resets the status word).
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
-#include <mutex>
 
 #include "bw_gpu.h"
 
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = (size_t)32 << 20;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
-
-std::mutex g_mu;
-void* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 int fail(cudaError_t e, const char* what) {
   std::fprintf(stderr, "bw_replay_launch_noalloc: %s failed: %s\n", what, cudaGetErrorString(e));
@@ -51,22 +49,9 @@ extern "C" int bw_replay_launch_noalloc(const BwReplayArgs* a, int32_t* status) 
     std::fprintf(stderr, "bw_replay_launch_noalloc: leave workspace NULL; the library's own region is used\n");
     return BW_EINVAL;
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(e, "cudaGetDevice");
-  if (dev < 0 || dev >= kMaxDevices) return BW_EINVAL;
   void* scratch = nullptr;
-  {
-    std::lock_guard<std::mutex> g(g_mu);
-    if (!g_scratch_ptr[dev]) {
-      e = cudaGetSymbolAddress(&g_scratch_ptr[dev], g_noalloc_scratch);
-      if (e != cudaSuccess) {
-        g_scratch_ptr[dev] = nullptr;
-        return fail(e, "cudaGetSymbolAddress");
-      }
-    }
-    scratch = g_scratch_ptr[dev];
-  }
+  const cudaError_t e = cudaGetSymbolAddress(&scratch, g_noalloc_scratch);   // current device's copy
+  if (e != cudaSuccess) return fail(e, "cudaGetSymbolAddress");
   size_t need = 0;
   int rc = bw_replay_workspace_size(a, &need);
   if (rc) return rc;

@@ -45,7 +45,7 @@ constexpr int kD = 32;                       // overlay members per version list
 constexpr int kServeThreads = 256;
 constexpr int kServeWarps = kServeThreads / 32;
 constexpr int kMaxCommit = 128;              // events per commit
-constexpr uint64_t kSpinLimit = 1ull << 25;  // bounded waits (each with a nanosleep backoff)
+constexpr uint64_t kSpinLimit = 1ull << 25;  // default bound of every device wait, in polls (each with a nanosleep backoff)
 constexpr int kRowThreads = 256;
 
 int report(cudaError_t e, const char* what) {
@@ -81,6 +81,7 @@ struct RunDev {
   uint32_t* dtail;             // device: copy of the published count (written by the dispatcher)
   uint32_t n;
   int32_t* err;                // host-mapped: first error (1 = wait limit or abort)
+  uint64_t spin_limit;         // polls before a wait gives up
 };
 
 __device__ __forceinline__ uint32_t ld_acquire_sys(const uint32_t* p) {
@@ -120,7 +121,7 @@ __device__ bool wait_ready(const StoreDev& d, const RunDev& r, int32_t v) {
     uint64_t it = 0;
     unsigned ns = 32;
     while (ld_acquire_gpu(d.ready + v) == 0) {
-      if (++it > kSpinLimit || ((it & 255) == 0 && ld_volatile(r.abort))) {
+      if (++it > r.spin_limit || ((it & 255) == 0 && ld_volatile(r.abort))) {
         atomicCAS(r.err, 0, 1);
         ok = 0;
         break;
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(kServeThreads) k_serve(StoreDev d, RunDev r) {
           idle = 0;
           asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(r.dtail), "r"(t) : "memory");
         } else {
-          if (ld_volatile(r.abort) || ++idle > kSpinLimit) {
+          if (ld_volatile(r.abort) || ++idle > r.spin_limit) {
             atomicCAS(r.err, 0, 1);
             break;
           }
@@ -178,7 +179,7 @@ __global__ void __launch_bounds__(kServeThreads) k_serve(StoreDev d, RunDev r) {
         asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(t) : "l"(r.dtail) : "memory");
         if (t > idx) break;
         // the host-mapped abort/error words are read only every 256 polls (C2C traffic)
-        if (++it > kSpinLimit ||
+        if (++it > r.spin_limit ||
             ((it & 255) == 0 && (ld_volatile(r.abort) || ld_volatile(reinterpret_cast<const uint32_t*>(r.err))))) {
           atomicCAS(r.err, 0, 1);
           ok = 0;
@@ -332,6 +333,7 @@ struct BwServe {
   unsigned int* head = nullptr;
   int32_t warps = 0;
   int32_t grid = 0;
+  uint64_t spin_limit = 0;   // polls before a device wait gives up
 };
 
 namespace {
@@ -469,6 +471,7 @@ extern "C" int bw_serve_create(const BwServeConfig* cfg, BwServe** out) {
   int rc = report(cudaGetDevice(&s->dev), "cudaGetDevice");
   if (rc) { delete s; return rc; }
   s->C = C; s->S0 = S; s->next = S; s->max_versions = V; s->arena_cap = Ecap; s->arena_used0 = E;
+  s->spin_limit = cfg->spin_limit ? cfg->spin_limit : kSpinLimit;
   s->checkpoints = nck; s->spacing = spacing; s->store_bytes = total;
   size_t o = 0;
   auto take = [&](size_t bytes) { const size_t at = o; o += align256(bytes); return at; };
@@ -660,6 +663,7 @@ extern "C" int bw_serve_run(BwServe* s, const BwServeRequest* reqs, int64_t n, c
   r.head = s->head;
   r.dtail = reinterpret_cast<uint32_t*>(s->head) + 1;
   r.n = (uint32_t)n;
+  r.spin_limit = s->spin_limit;
   r.err = reinterpret_cast<int32_t*>(const_cast<uint32_t*>(r.tail) + 2);
   cudaStream_t st = nullptr;
   if ((rc = report(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream"))) { cleanup(); return rc; }

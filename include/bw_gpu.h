@@ -97,6 +97,99 @@ int gpu_combine_launch(const struct GpuV7CombineArgs* a);
 int bw_v7_carry_launch(int B, int Cpfx, const int64_t* vbase, const int64_t* dV,
                        int64_t* carrypref, void* stream);
 
+/* ------------------------------------------------------------ v7b drop-in
+ * Layouts identical to the reference's compact plan (gpu_v7b.h:6-48): a 40-byte node
+ * (kind bits: 1 row, 2 factor, bit 2 ex_old, bit 3 ex_new; a, b = amt_old, amt_new
+ * for a row edit, fac_val, fac_prev for a factor edit) and block-start deviation
+ * snapshots made on the device by the snapshot entry. */
+struct GpuV7bNode {
+  uint8_t kind;
+  int16_t g_old, g_new;
+  int32_t c_old, c_new;
+  int32_t ti_old, ti_new;
+  int64_t a, b;
+};
+
+struct GpuV7bSnapArgs {
+  int nstates;                  /* kStates */
+  const struct GpuV7bNode* nodes;
+  const int32_t* bidx;          /* state -> block */
+  const int32_t* gb_off;        /* G+1 */
+  const int32_t* gb_block;      /* per (group, block) occurrence, ascending blocks per group */
+  const int64_t* gb_reg;        /* devbuf offset of the group's region in that block */
+  int64_t* devbuf;              /* in/out: snapshots accumulate into it (caller zeroes it) */
+};
+
+struct GpuV7bArgs {
+  int B, G, Cpfx, ncls, q;
+  const struct GpuV7bNode* nodes;
+  const int32_t *bv0, *bv1;
+  const int64_t* fac_start;     /* B*G */
+  const int32_t* g2row;         /* G */
+  const int32_t* ms_off;        /* n_active+1 */
+  const int64_t *ms_cls, *ms_base;
+  const int32_t* ms_dev;
+  int64_t* devbuf;
+  const int64_t* need_off;      /* B*G */
+  const int32_t *qlb, *qhb;
+  int64_t *lvals, *dV;
+  int threads;                  /* hint only */
+  int shared_bytes;             /* hint only */
+};
+
+struct GpuV7bCombineArgs {      /* same layout as GpuV7CombineArgs */
+  int nstates, q, Cpfx;
+  const int32_t *qlb, *qhb;
+  const int64_t* carrypref;     /* B*Cpfx */
+  const int32_t* bidx;
+  const int64_t* lvals;
+  int64_t* answers;
+};
+
+/* Replace gpu_v7b_snap_launch / gpu_v7b_launch / gpu_v7b_combine_launch
+ * (gpu_v7b.h:50-52, gpu_v7b.cu:13-141): the snapshot entry adds every row edit's
+ * deviation delta into the regions of the later blocks that need its group; the
+ * block and combine entries are those of gpu_v7.h on the compact node.  Default
+ * stream, asynchronous. */
+int gpu_v7b_snap_launch(const struct GpuV7bSnapArgs* a);
+int gpu_v7b_launch(const struct GpuV7bArgs* a);
+int gpu_v7b_combine_launch(const struct GpuV7bCombineArgs* a);
+
+/* ------------------------------------------------------------ session drop-in
+ * Layouts identical to the reference's session backend (gpu_session.h:4-20): the
+ * prefix structure of each block lives in caller-owned global memory (fen, leaf:
+ * B*Cpfx int64 each), so the class domain is not bounded by shared memory; a
+ * session uploads once and reruns run + combine per query batch. */
+struct GpuSessNode { uint8_t kind; int16_t g_old, g_new; int32_t c_old, c_new, ti_old, ti_new; int64_t a, b; };
+struct GpuSessResetArgs { int B, Cpfx; int64_t* fen; int64_t* leaf; };
+struct GpuSessRunArgs {
+  int B, G, Cpfx, ncls, q;
+  const struct GpuSessNode* nodes;
+  const int32_t *bv0, *bv1;
+  const int64_t* fac_start;
+  const int32_t* g2row;
+  const int32_t* ms_off; const int64_t *ms_cls, *ms_base; const int32_t* ms_dev;
+  int64_t* devbuf; const int64_t* need_off;
+  const int32_t *qlb, *qhb;
+  int64_t* lvals; int64_t* dV;
+  int64_t* fen; int64_t* leaf;  /* B*Cpfx each */
+  int threads;                  /* hint only */
+};
+struct GpuSessCombineArgs { int nstates, q, Cpfx; const int32_t *qlb, *qhb; const int64_t* carrypref;
+                            const int32_t* bidx; const int64_t* lvals; int64_t* answers; };
+struct GpuSessSnapArgs { int nstates; const struct GpuSessNode* nodes; const int32_t* bidx; const int32_t* gb_off;
+                         const int32_t* gb_block; const int64_t* gb_reg; int64_t* devbuf; };
+
+/* Replace gpu_sess_reset_launch / gpu_sess_run_launch / gpu_sess_snap_launch /
+ * gpu_sess_combine_launch (gpu_session.h:21-24): reset zeroes fen and leaf, run
+ * replays every block with its prefix structure in fen/leaf and writes lvals, the
+ * block leaf deltas into both leaf and dV, and devbuf as gpu_v7_launch does;
+ * snap and combine are the v7b ones. */
+int gpu_sess_reset_launch(const struct GpuSessResetArgs* a);
+int gpu_sess_run_launch(const struct GpuSessRunArgs* a);
+int gpu_sess_snap_launch(const struct GpuSessSnapArgs* a);
+int gpu_sess_combine_launch(const struct GpuSessCombineArgs* a);
+
 /* ===================================================================== event model */
 typedef struct { uint32_t state, key; int64_t delta; } BwEvent;   /* 16 bytes */
 typedef struct { uint32_t state, lo, hi; } BwQuery;               /* 12 bytes */
@@ -119,8 +212,16 @@ typedef struct {
 
 #define BW_REPLAY_CHAIN_HINT 1  /* caller asserts parent[v] == v-1; any fork is rejected (BW_STATUS_BAD_PARENT) */
 #define BW_REPLAY_TIMING 2      /* record CUDA events between pipeline stages (see below) */
+/* With BW_REPLAY_CHAIN_HINT, a key domain of at most 32,768 keys and 16-byte aligned
+ * events, the replay takes the single-pass chain path (each event read once, no
+ * Euler tour) when the workload has at most one query per 8 events; these flags
+ * force either path instead (tests, benchmarks). */
+#define BW_REPLAY_CHAIN_KERNEL 4
+#define BW_REPLAY_GENERAL 8
 
-/* Pipeline stages timed under BW_REPLAY_TIMING, in order. */
+/* Pipeline stages timed under BW_REPLAY_TIMING, in order (the chain path has only
+ * the sweep, which reads the events, and the carry scan with the answer fix-up that
+ * follows it; its other stages read 0). */
 enum {
   BW_STAGE_INGEST = 0,     /* per-state offsets + validation */
   BW_STAGE_LINEARISE = 1,  /* Euler tour / chain layout */
@@ -140,7 +241,8 @@ enum {
   BW_STATUS_QUERY_RANGE = 4,
   BW_STATUS_BAD_PARENT = 5,
   BW_STATUS_TOO_MANY_SLICES = 6,
-  BW_STATUS_STATE_RANGE = 7
+  BW_STATUS_STATE_RANGE = 7,
+  BW_STATUS_TIMEOUT = 8      /* a bounded device wait gave up (the kernel returned early) */
 };
 
 /* Bytes of device workspace needed for these arguments (pointers unused). */
@@ -152,9 +254,13 @@ int bw_replay_launch(const BwReplayArgs* a);
 /* Synchronise a->stream and read the device status word written by the last
  * bw_replay_launch with this workspace; *status receives a BW_STATUS_* code. */
 int bw_replay_status(const BwReplayArgs* a, int32_t* status);
-/* Number of kernels the last bw_replay_launch on this workspace enqueued and the
- * state-block count it used (host-side bookkeeping, no synchronisation). */
+/* Number of kernels the most recent bw_replay_launch of this process enqueued (any
+ * workspace, any thread: the record is process-wide) and the state-block count it
+ * used (host-side bookkeeping, no synchronisation). */
 int bw_replay_last_info(const BwReplayArgs* a, int32_t* kernels, int32_t* blocks);
+/* *chain = 1 when these arguments take the single-pass chain path, 0 for the
+ * general pipeline (host-side decision from the sizes, flags and event alignment). */
+int bw_replay_path(const BwReplayArgs* a, int32_t* chain);
 
 /* Stage timing over a run of launches made with BW_REPLAY_TIMING (CUDA events
  * recorded on each launch's stream).  bw_replay_timing_reset() starts a new run;
@@ -171,10 +277,13 @@ int bw_replay_stage_times(float* ms, int32_t* launches);
  * a->workspace_bytes 0: the scratch comes from a fixed 32 MiB region compiled into
  * the library (held by every GPU that loads it until exit); workloads needing more
  * (bw_replay_workspace_size) are rejected with BW_EINVAL.  Nothing is allocated or
- * freed.  The first call on a device looks the region up and should come before
- * any stream capture.  Calls share the region, so calls overlapping on the GPU
- * race.  A non-NULL host `status` makes the call wait for its stream and receive
- * the BW_STATUS_* code; NULL returns once the work is enqueued. */
+ * freed.  Every call looks the region's device address up on the current device
+ * (an allocation-free lookup that stays right after a context reset); the first
+ * call on a device loads the library's module there and should come before any
+ * stream capture.  Calls share the region, so calls overlapping on the GPU race.
+ * A non-NULL host `status` makes the call wait for its stream and receive the
+ * BW_STATUS_* code; NULL returns once the work is enqueued, and the device's input
+ * check is then not reported. */
 int bw_replay_launch_noalloc(const BwReplayArgs* a, int32_t* status);
 
 /* ============================================================ batched version forests
@@ -286,6 +395,9 @@ typedef struct {
   int64_t max_events;        /* event arena: initial events + events runs may commit */
   size_t hbm_cap_bytes;      /* admission cap of the whole store */
   int32_t chain_limit;       /* largest checkpoint spacing allowed (<= 32; 0 = 32) */
+  uint32_t spin_limit;       /* polls (each with a nanosleep backoff of up to ~2 us) before a
+                                device wait for an unpublished request or an unfinished version
+                                gives up and ends the run with an error; 0 = 2^25 */
 } BwServeConfig;
 
 typedef struct {
@@ -313,7 +425,9 @@ int bw_serve_reset(BwServe* s);
  * clock.  The log is checked first (versions exist before they are read, new ids
  * are consecutive, bounds and keys in range) and admitted only if its commit
  * events fit the free event arena.  Blocks until every request completes or
- * timeout_s elapses (BW_EINVAL). */
+ * timeout_s elapses, or a device wait reaches its spin_limit (both BW_EINVAL, after
+ * the loop has returned; the store stays usable and bw_serve_reset forgets the
+ * partial run). */
 int bw_serve_run(BwServe* s, const BwServeRequest* reqs, int64_t n, const BwEvent* commit_events,
                  int64_t n_commit_events, const double* arrival_s, int32_t max_inflight, double timeout_s,
                  int64_t* answers, float* latency_us, BwServeStats* stats);

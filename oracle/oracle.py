@@ -260,6 +260,17 @@ def max_threads() -> int:
     return int(lib().bwo_max_threads())
 
 
+def reference_dir() -> Path | None:
+    """The reference checkout used to build the pinning binaries: $BW_REFERENCE_DIR,
+    else a ``reference`` directory beside this repository; None when neither holds
+    the reference sources."""
+    cand = [os.environ.get("BW_REFERENCE_DIR"), str(HERE.parent.parent / "reference")]
+    for c in cand:
+        if c and (Path(c) / "src" / "oracle.cpp").exists():
+            return Path(c)
+    return None
+
+
 def ref_binary(name: str, states: int) -> Path | None:
     """Path of a reference binary built by oracle/ref.mk, when present."""
     p = HERE / "_ref" / f"{name}_{states}"

@@ -2,8 +2,10 @@
 # oracle/_ref/ (git-ignored).  Used only to pin the oracle and as a CPU
 # reference where the sources exist.  No cmake: g++ on the reference's worker
 # sources directly, with a local stand-in for the absent OpenSSL header.
-#   make -f oracle/ref.mk REF=/root/reference STATES=2049
-REF ?= /root/reference
+#   make -f oracle/ref.mk REF=<reference checkout> STATES=2049
+ifeq ($(REF),)
+$(error REF must name the reference checkout (the directory holding src/oracle.cpp))
+endif
 STATES ?= 2049
 MAXQ ?= 32
 OUT ?= oracle/_ref
@@ -38,4 +40,26 @@ $(OUT)/fuzz_ref_$(STATES): oracle/ref_fuzz.cpp $(OUT)/sha_shim.o
 	$(CXX) -std=c++17 -O2 -DNDEBUG -DBWH_STATES=$(STATES) -DBWH_MAXQ=$(MAXQ) -Ioracle/ref_shim -I$(REF)/src \
 	  oracle/ref_fuzz.cpp $(OUT)/bwo.o -o $@
 
-.PHONY: all fuzz
+# The reference's own GPU workers (panel_batch_gpu*.cpp, panel_gpu_session.cpp)
+# compiled against this repository's include/bw_gpu.h and linked with libbwgpu.so:
+# a shadow source directory of symlinks to the reference's files in which
+# gpu_v7.h, gpu_v7b.h and gpu_session.h are the stand-ins of oracle/ref_shim/dropin.
+PKG ?= biworlddb-artifact_gb300
+CUDA ?= /usr/local/cuda
+DROPIN_SRC = $(OUT)/dropin_src
+DROPIN_WORKERS = panel_batch_gpu panel_batch_gpu2 panel_batch_gpu3 panel_gpu_session
+dropin: $(foreach w,$(DROPIN_WORKERS),$(OUT)/$(w)_$(STATES))
+
+$(DROPIN_SRC)/.stamp: oracle/ref_shim/dropin/gpu_v7.h oracle/ref_shim/dropin/gpu_v7b.h oracle/ref_shim/dropin/gpu_session.h
+	mkdir -p $(DROPIN_SRC)
+	for f in $(REF)/src/*; do case $$(basename $$f) in gpu_v7.h|gpu_v7b.h|gpu_session.h) ;; \
+	  *) ln -sf $$f $(DROPIN_SRC)/ ;; esac; done
+	for h in gpu_v7.h gpu_v7b.h gpu_session.h; do ln -sf $(CURDIR)/oracle/ref_shim/dropin/$$h $(DROPIN_SRC)/$$h; done
+	touch $@
+
+$(OUT)/%_$(STATES): $(DROPIN_SRC)/.stamp $(OUT)/sha_shim.o $(PKG)/libbwgpu.so
+	$(CXX) -std=c++17 -O2 -w -fopenmp -DBWH_STATES=$(STATES) -DBWH_MAXQ=$(MAXQ) -Iinclude -Ioracle/ref_shim \
+	  -I$(CUDA)/include $(DROPIN_SRC)/$*.cpp $(OUT)/sha_shim.o $(OUT)/bwo.o -L$(PKG) -lbwgpu \
+	  -L$(CUDA)/lib64 -lcudart -Wl,-rpath,$(CURDIR)/$(PKG) -o $@
+
+.PHONY: all fuzz dropin

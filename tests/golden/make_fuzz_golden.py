@@ -8,7 +8,7 @@ of the fixture file the reference wrote and the SHA-256 of its answer vector.
 Two state counts: 33 (the reference fuzz's own build, fuzz_fullpath.cpp:23-26)
 and 257 (deeper trees, several state blocks on the GPU).
 
-Usage: python tests/golden/make_fuzz_golden.py [--ref /path/to/reference]
+Usage: python tests/golden/make_fuzz_golden.py [--ref <reference checkout>]
 """
 from __future__ import annotations
 
@@ -26,8 +26,17 @@ RUNS = [(33, 600), (257, 150)]   # (states, cases)
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("BW_REFERENCE_DIR", "/root/reference"))
+    ap.add_argument("--ref", default=None, help="reference checkout (default: $BW_REFERENCE_DIR, else a "
+                    "'reference' directory beside this repository)")
     args = ap.parse_args()
+    if args.ref is None:
+        import sys
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle  # noqa: E402  (test infrastructure)
+        ref = oracle.reference_dir()
+        if ref is None:
+            raise SystemExit("reference checkout not found: pass --ref or set BW_REFERENCE_DIR")
+        args.ref = str(ref)
     out = {"source": "reference fuzz_fullpath.cpp build_case + rf arm (oracle/ref_fuzz.cpp)", "runs": []}
     with tempfile.TemporaryDirectory() as tmp:
         for states, n in RUNS:

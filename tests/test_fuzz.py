@@ -7,8 +7,9 @@ dense 8-tick frame, mixed), 3 topologies (chain, bushy, star) and both range sco
 (per-state and shared), the first 60 cases being the deterministic edge cases.  It
 checks its arms against a rollback-Fenwick oracle but never runs the v7 executor or
 any GPU kernel (fuzz_fullpath.cpp:38-44).  Here every case runs through the host
-front end (bw_native_build_declared) and the CUDA replay (bw_replay_launch, with and
-without the chain hint, with forced state blocks), chains also through the gpu_v7.h
+front end (bw_native_build_declared) and the CUDA replay (bw_replay_launch: the
+general pipeline with and without the chain hint and with forced state blocks, and
+for chains the single-pass chain path too), chains also through the gpu_v7.h
 drop-in (gpu_v7_launch + carry + gpu_combine_launch), and every answer vector must
 hash to the value the reference's own build_case + "rf" arm produced
 (tests/golden/fuzz_golden.json, made by make_fuzz_golden.py).
@@ -126,7 +127,9 @@ def test_gpu_fuzz_replay(bw, torch_cuda, chunk):
     for rec, c in cases_of(chunk):
         w = bw.native_workload_declared(c.fixture, c, c.name)
         p, e, q = evgen.to_device(torch_cuda, w.parent, w.events, w.queries)
-        variants = [dict(), dict(blocks=3)] + ([dict(chain=True), dict(chain=True, blocks=5)] if w.chain else [])
+        variants = [dict(), dict(blocks=3)] + ([dict(chain=True), dict(chain=True, blocks=5),
+                                                dict(chain=True, path="chain"),
+                                                dict(chain=True, path="chain", blocks=4)] if w.chain else [])
         for kw in variants:
             ans = bw.replay(p, w.n_keys, e, q, **kw).cpu().numpy()
             assert bw.sha256_hex(ans.tobytes()) == rec["answers_sha256"], (c.name, kw)

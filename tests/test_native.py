@@ -76,6 +76,10 @@ def test_gpu_replay_reproduces_golden(bw, torch_cuda, case):
     p, e, q = evgen.to_device(torch_cuda, w.parent, w.events, w.queries)
     ans = bw.replay(p, w.n_keys, e, q, chain=w.chain).cpu().numpy()
     assert bw.sha256_hex(ans.tobytes()) == expected(case)
+    if w.chain and w.n_keys <= 32768:   # the single-pass chain path, forced on this query-heavy case
+        for blocks in (0, 6):
+            ans = bw.replay(p, w.n_keys, e, q, chain=True, path="chain", blocks=blocks).cpu().numpy()
+            assert bw.sha256_hex(ans.tobytes()) == expected(case)
 
 
 @pytest.mark.gpu
@@ -111,4 +115,30 @@ def test_gpu_v7_dropin_large_reference_case(bw, torch_cuda, case):
     plan = bw.v7_plan(fixture(case["fixture"]), case["states"], case["seed"], case["factor_period"],
                       case["q"], blocks=128)
     ans, _, _ = bw.run_v7_plan(plan)
+    assert bw.sha256_hex(ans.tobytes()) == case["reference"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", [c for c in CASES if c["topology"] == 0], ids=cid)
+@pytest.mark.parametrize("blocks", [1, 9, 64])
+def test_gpu_v7b_and_session_reproduce_golden(bw, torch_cuda, case, blocks):
+    """The compact (gpu_v7b.h) and session (gpu_session.h) drop-in entries: device
+    snapshots equal the host plan's block-start deviations, and the answers hash to
+    the golden value (session: two query batches from the same snapshots)."""
+    plan = bw.v7_plan(fixture(case["fixture"]), case["states"], case["seed"], case["factor_period"],
+                      case["q"], blocks=blocks, per_state=case["per_state"])
+    ans, snap = bw.run_v7b_plan(plan)
+    np.testing.assert_array_equal(snap[:plan["devbuf"].size], plan["devbuf"])
+    assert bw.sha256_hex(ans.tobytes()) == expected(case)
+    ans, snap = bw.run_v7b_plan(plan, session=True, batches=2)
+    np.testing.assert_array_equal(snap[:plan["devbuf"].size], plan["devbuf"])
+    assert bw.sha256_hex(ans.tobytes()) == expected(case)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", LARGE, ids=cid)
+def test_gpu_session_large_reference_case(bw, torch_cuda, case):
+    plan = bw.v7_plan(fixture(case["fixture"]), case["states"], case["seed"], case["factor_period"],
+                      case["q"], blocks=128)
+    ans, _ = bw.run_v7b_plan(plan, session=True)
     assert bw.sha256_hex(ans.tobytes()) == case["reference"]

@@ -125,3 +125,49 @@ def test_admission_and_malformed_logs(bw, torch_cuda):
     with pytest.raises(RuntimeError):   # the store itself over the cap
         bw.Server(b.parent, b.n_keys, b.events, max_versions=len(b.parent), max_events=len(b.events),
                   hbm_cap_bytes=1 << 20)
+
+
+def _late_arrivals(log, cut):
+    """Arrival times that publish only the first `cut` requests within the run."""
+    arr = np.zeros(len(log.requests))
+    arr[cut:] = 1e4
+    return arr
+
+
+def test_serve_host_timeout_stops_loop(bw, torch_cuda, oracle_mod):
+    """A host timeout while requests are still unpublished: the host raises the abort
+    word, the loop's bounded waits see it and return, the run reports an error, and
+    the store and context stay usable."""
+    import time
+    log = bw.workloads.serving(6, base=small_base(bw, 6), requests=4_000)
+    srv = server_for(bw, log)
+    t0 = time.perf_counter()
+    with pytest.raises(RuntimeError, match="1001"):
+        srv.run(log.requests, log.commit_events, _late_arrivals(log, 1500), timeout_s=0.5)
+    assert time.perf_counter() - t0 < 20.0
+    srv.reset()
+    ans, _, _ = srv.run(log.requests, log.commit_events)
+    q = log.requests["kind"] == 0
+    np.testing.assert_array_equal(ans[q], oracle_answers(oracle_mod, log)[q])
+    srv.close()
+
+
+def test_serve_device_wait_limit_stops_loop(bw, torch_cuda, oracle_mod):
+    """A device wait that reaches its poll limit (requests that never arrive within
+    it): the loop records the error word and returns before the host timeout; a new
+    store on the same context then serves the full log exactly."""
+    import time
+    log = bw.workloads.serving(7, base=small_base(bw, 7), requests=4_000)
+    b = log.base
+    srv = bw.Server(b.parent, b.n_keys, b.events, max_versions=len(b.parent) + len(log.requests),
+                    max_events=len(b.events) + len(log.commit_events), hbm_cap_bytes=8 << 30, spin_limit=4000)
+    t0 = time.perf_counter()
+    with pytest.raises(RuntimeError, match="1001"):
+        srv.run(log.requests, log.commit_events, _late_arrivals(log, 1000), timeout_s=60.0)
+    assert time.perf_counter() - t0 < 30.0
+    srv.close()
+    srv = server_for(bw, log)
+    ans, _, _ = srv.run(log.requests, log.commit_events)
+    q = log.requests["kind"] == 0
+    np.testing.assert_array_equal(ans[q], oracle_answers(oracle_mod, log)[q])
+    srv.close()
