@@ -24,6 +24,7 @@ import ctypes as C
 from pathlib import Path
 
 from . import _build, workloads  # noqa: F401
+from . import shard  # noqa: F401,E402
 
 PKG = _build.PKG
 
@@ -96,7 +97,7 @@ GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch", "gpu
                "bw_forest_destroy", "bw_forest_autotune_workspace", "bw_forest_autotune",
                "bw_forest_launch_timed",
                "bw_serve_create", "bw_serve_reset", "bw_serve_run", "bw_serve_info", "bw_serve_destroy",
-               "bw_forest_plan_stats"]
+               "bw_forest_plan_stats", "bw_key_histogram", "bw_key_prefix", "bw_add_range_carry"]
 
 _gpu = None
 

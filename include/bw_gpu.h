@@ -286,6 +286,25 @@ int bw_replay_stage_times(float* ms, int32_t* launches);
  * check is then not reported. */
 int bw_replay_launch_noalloc(const BwReplayArgs* a, int32_t* status);
 
+/* ============================================================ one chain across ranks
+ * A chain split into contiguous state ranges, one per rank (one process per GPU):
+ * each rank replays its range as a chain of its own (local states start at 0), and
+ * the only exchange is the carry, an exclusive scan over ranks of each rank's dense
+ * key histogram -- the reference's serial carry pass (batch_engine_v7.hpp:936-945)
+ * lifted from state blocks to ranks; the carry is then added to the rank's answers
+ * inside [lo, hi) as the reference's combine does (batch_engine_v7.hpp:948-961).
+ * The scan is the caller's (an identity on one rank; torch.distributed between
+ * processes).  Asynchronous on `stream`. */
+/* hist[k] = wrapping sum of the deltas of events with key k, k < n_keys (device
+ * arrays; the call zeroes hist first; keys >= n_keys are ignored). */
+int bw_key_histogram(const BwEvent* events, int64_t n, uint32_t n_keys, int64_t* hist, void* stream);
+/* prefix[k] = sum of vec[j] for j < k, k = 0..n (prefix holds n+1 entries). */
+int bw_key_prefix(const int64_t* vec, uint32_t n, int64_t* prefix, void* stream);
+/* answers[i] += prefix[hi] - prefix[lo] for every query with lo < hi (bounds clamped to
+ * n_keys): the carry below the rank inside each query's interval. */
+int bw_add_range_carry(const BwQuery* queries, int64_t n, uint32_t n_keys, const int64_t* prefix,
+                       int64_t* answers, void* stream);
+
 /* ============================================================ batched version forests
  * Thousands of independent version trees replayed in one pipeline (the reference
  * replays one chain per worker process, panel_batch_gpu.cpp:182-214, and its
