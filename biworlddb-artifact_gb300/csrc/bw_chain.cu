@@ -1,26 +1,28 @@
 // bw_chain.cu -- single-pass replay of a linear version chain (see bw_chain.cuh).
 //
-// Sweep (k_chain_sweep, one CTA per state block, 512 threads):
-//   * the block's events [e0, e1) stream through a ring of kChainStages tiles of
-//     kChainTile events, each tile one cp.async.bulk copy from global memory into
-//     shared memory completed on the stage's mbarrier (bounded waits);
+// Sweep (k_chain_sweep, one CTA per state block; 128, 256 or 512 threads with
+// tiles of 512-1024 events, picked per key domain by occupancy):
+//   * the block's events [e0, e1) stream through a ring of kChainStages tiles,
+//     each tile one cp.async.bulk copy from global memory into shared memory
+//     completed on the stage's mbarrier (bounded waits);
 //   * the running key histogram of the block lives in shared memory as exact
 //     int32 window accumulators H[key] plus lane-replicated chunk totals T[chunk]
 //     (each lane of a warp adds into its own copy, so chunk updates never collide).
 //     A window holds events whose absolute sum stays below 2^28 + 2^29, so every
 //     partial sum of it is exact in int32; before it can grow past that it is
 //     flushed into the block's int64 row in global memory (plus int64 chunk
-//     totals in shared memory).  Tiles with a large delta (a thread's two events
-//     summing to >= 2^20 in magnitude) bypass the window: they add straight into
-//     the int64 row with 64-bit global atomics;
+//     totals in shared memory).  Tiles holding a delta outside (-2^19, 2^19)
+//     bypass the window: they add straight into the int64 row with 64-bit global
+//     atomics;
 //   * a tile owns the queries whose position (number of events at or before their
 //     state) falls inside it: state < state of the tile's last event.  Their local
 //     answer = the window + row probe over [lo, hi) before the tile is applied,
-//     plus the tile's events at or before the query's state inside [lo, hi);
-//     one warp per query, int32 lane sums reduced with redux.sync;
-//   * one warp (the last) finds the next tile's queries while the others apply
-//     the current tile: its query states are prefetched into registers one tile
-//     ahead, its records copied into shared memory.
+//     plus the tile's first `pos` events inside [lo, hi); one warp per query,
+//     int32 lane sums reduced with redux.sync;
+//   * one warp (the last) finds the next tile's queries and their positions while
+//     the others answer the current tile's: the query records come through a
+//     32-record window that cp.async fills one tile ahead, and land in a
+//     double-buffered shared query buffer.
 // Carry (k_chain_colsum, k_chain_colfix): exclusive column scan over the block
 // rows in two passes (segment sums, then segment-local prefixes), in place.
 // Fix-up (k_chain_fixup): each block's carry row is scanned over keys in place and
@@ -28,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "bw_gpu.h"
@@ -37,15 +40,14 @@
 namespace bw {
 namespace {
 
-constexpr int NT = kChainThreads;
-constexpr int NW = NT / 32;
-constexpr int QW = NW - 1;                       // the query warp
-constexpr int TE = kChainTile;
+constexpr int TE = kChainTile;   // largest tile (the shared-memory ring is sized per geometry)
 constexpr int NS = kChainStages;
 constexpr int QB = kChainQBuf;
+constexpr int kMaxWarps = kChainThreads / 32;
 constexpr uint32_t kWaitLimit = 1u << 22;        // mbarrier polls before a stage is declared lost
-constexpr uint64_t kBigThread = 1ull << 20;      // a thread's |delta| sum below which its tile is int32-safe
 constexpr uint32_t kFlushAt = 1u << 28;          // window |delta| sum that triggers a flush
+// A tile is int32-safe when every delta lies in (-2^19, 2^19): with at most 1024
+// events its absolute sum is then below 2^29.
 
 struct ChainParams {
   const uint4* ev;        // events as 16-byte records (state, key, delta lo, delta hi)
@@ -67,25 +69,26 @@ struct ChainParams {
 // tile parity: a fast warp may already write the next tile's copy while a slow one
 // still reads this tile's.
 struct Misc {
-  uint32_t wsum[2][NW];   // per-warp |delta| sum of a tile's window updates
-  int64_t tq[2][2];       // queries [tq0, tq1) of a tile
-  uint32_t prev_state[2]; // state of the event before a tile
+  uint32_t wsum[2][kMaxWarps];   // per-warp |delta| sum of a tile's window updates
+  int64_t tq[2][2];              // queries [tq0, tq1) of a tile
+  uint32_t prev_state[2];        // state of the event before a tile
   int64_t tail_q0;
 };
 
 // Dynamic shared memory of the sweep, every region 16-byte aligned.
 struct SweepSmem {
-  size_t ring, H, T, T64, qbuf, bar, misc, bytes;
+  size_t ring, H, T, T64, qbuf, qpre, bar, misc, bytes;
 };
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
-__host__ __device__ inline SweepSmem sweep_smem(uint32_t C, int nch) {
+__host__ __device__ inline SweepSmem sweep_smem(uint32_t C, int nch, int te) {
   SweepSmem L;
   size_t o = 0;
-  L.ring = o;  o = al16(o + (size_t)NS * TE * 16);
+  L.ring = o;  o = al16(o + (size_t)NS * te * 16);
   L.H = o;     o = al16(o + (size_t)C * 4);
   L.T = o;     o = al16(o + (size_t)nch * 32 * 4);
   L.T64 = o;   o = al16(o + (size_t)nch * 8);
-  L.qbuf = o;  o = al16(o + (size_t)QB * 12);
+  L.qbuf = o;  o = al16(o + 2 * (size_t)QB * 16);   // two tiles' query records
+  L.qpre = o;  o = al16(o + 32 * 12);                // prefetched window of 32 query records
   L.bar = o;   o = al16(o + (size_t)NS * 8);
   L.misc = o;  o = al16(o + sizeof(Misc));
   L.bytes = o;
@@ -125,8 +128,10 @@ __device__ __forceinline__ void set_status(int32_t* st, int32_t code) {
   if (*reinterpret_cast<volatile int32_t*>(st) == 0) atomicCAS(st, 0, code);
 }
 
-__device__ __forceinline__ uint64_t uabs64(uint64_t d) {
-  return (int64_t)d < 0 ? (uint64_t)0 - d : d;
+// delta in (-2^19, 2^19): its high word is the sign extension of its low word
+__device__ __forceinline__ bool small_delta(const uint4& e) {
+  const int32_t lo = (int32_t)e.z;
+  return e.w == (uint32_t)(lo >> 31) && (uint32_t)(lo + (1 << 19)) < (1u << 20);
 }
 
 __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
@@ -168,36 +173,26 @@ __device__ __forceinline__ uint64_t probe64(const int64_t* row, const unsigned l
   return s;
 }
 
-// Lane share of the tile's events at or before state qst with key in [lo, hi).
-template <bool WIDE>
-__device__ __forceinline__ uint64_t tile_corr(const uint4* tile, int n, uint32_t qst, uint32_t lo, uint32_t hi,
-                                              int lane) {
-  uint64_t s = 0;
-  int32_t s32 = 0;
-  for (int base = 0; base < n; base += 32) {
-    const int j = base + lane;
-    bool le = false;
-    if (j < n) {
-      const uint4 e = tile[j];
-      le = e.x <= qst;
-      if (le && e.y >= lo && e.y < hi) {
-        if (WIDE) s += ((uint64_t)e.w << 32) | e.z;
-        else s32 += (int32_t)e.z;
-      }
-    }
-    if (!__all_sync(0xffffffffu, le)) break;
+// Position of a query in its tile: the number of the tile's events at or before
+// its state (upper bound over the tile's sorted states).
+__device__ __forceinline__ uint32_t tile_pos(const uint4* tile, int n, uint32_t qst) {
+  uint32_t lo = 0, hi = (uint32_t)n;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (tile[mid].x <= qst) lo = mid + 1; else hi = mid;
   }
-  return WIDE ? s : (uint64_t)(uint32_t)s32;
+  return lo;
 }
 
 // First query index in [0, Q) whose state is >= x (Q when none), found by the
-// whole CTA in rounds of NT probes.
+// whole CTA in rounds of one probe per thread.
 __device__ int64_t first_query_at_or_after(const BwQuery* qs, int64_t Q, uint32_t x) {
+  const int nt = blockDim.x;
   int64_t lo = 0, hi = Q;
   while (true) {
     const int64_t n = hi - lo;
     if (n <= 0) return lo;
-    const int64_t step = (n + NT - 1) / NT;
+    const int64_t step = (n + nt - 1) / nt;
     const int64_t pos = lo + (int64_t)threadIdx.x * step;
     const bool lt = pos < hi && qs[pos].state < x;
     const int cnt = __syncthreads_count(lt);
@@ -208,70 +203,88 @@ __device__ int64_t first_query_at_or_after(const BwQuery* qs, int64_t Q, uint32_
   }
 }
 
-// The query warp's prefetched window of 32 query records.
-struct QCache {
-  int64_t base;
-  uint32_t st, lo, hi;
-};
-
-__device__ __forceinline__ void qcache_fetch(QCache& c, const BwQuery* qs, int64_t Q, int64_t base, int lane) {
-  c.base = base;
+// The query warp's window of the next 32 query records, copied into shared memory
+// with cp.async one tile before it is read (so the copy's latency stays hidden).
+__device__ __forceinline__ void qpre_issue(uint32_t* qpre, const BwQuery* qs, int64_t Q, int64_t base, int lane) {
   const int64_t i = base + lane;
   if (i < Q) {
-    const uint32_t* r = reinterpret_cast<const uint32_t*>(qs + i);
-    c.st = r[0];
-    c.lo = r[1];
-    c.hi = r[2];
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(qs + i);
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(qpre + 3 * lane + j)), "l"(src + j)
+                   : "memory");
   } else {
-    c.st = 0xffffffffu;
-    c.lo = c.hi = 0;
+    qpre[3 * lane] = 0xffffffffu;   // past the last query
   }
+  asm volatile("cp.async.commit_group;" ::: "memory");
 }
 
-// Query warp: the queries of the tile whose last event has state x are those from
-// qcur on with state < x.  Their records go to qbuf (the first QB), their range to
-// tq; qcur advances past them.
-__device__ void find_tile_queries(const ChainParams& p, QCache& c, int64_t& qcur, uint32_t x, uint32_t* qbuf,
-                                  int64_t* tq, int lane) {
+// Query warp: the queries of a tile (n events, the last with state x) are those
+// from qcur on with state < x.  Their records and positions in the tile go to qbuf
+// (the first QB), their range to tq; qcur advances past them.  `pbase` is the first
+// query of the window in flight.
+__device__ void find_tile_queries(const ChainParams& p, uint32_t* qpre, int64_t& pbase, int64_t& qcur,
+                                  const uint4* tile, int n, uint32_t* qbuf, int64_t* tq, int lane) {
+  const uint32_t x = tile[n - 1].x;
   const int64_t tq0 = qcur;
   while (true) {
-    if (c.base != qcur) qcache_fetch(c, p.qs, p.Q, qcur, lane);
+    if (pbase != qcur) {
+      qpre_issue(qpre, p.qs, p.Q, qcur, lane);
+      pbase = qcur;
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    const uint32_t st = qpre[3 * lane], lo = qpre[3 * lane + 1], hi = qpre[3 * lane + 2];
     const bool valid = qcur + lane < p.Q;
-    const uint32_t ball = __ballot_sync(0xffffffffu, valid && c.st < x);
-    const int n = ball == 0xffffffffu ? 32 : __ffs(~ball) - 1;
-    if (lane < n) {
+    const uint32_t ball = __ballot_sync(0xffffffffu, valid && st < x);
+    const int k = ball == 0xffffffffu ? 32 : __ffs(~ball) - 1;
+    if (lane < k) {
       const int64_t slot = qcur - tq0 + lane;
       if (slot < QB) {
-        qbuf[3 * slot] = c.st;
-        qbuf[3 * slot + 1] = c.lo;
-        qbuf[3 * slot + 2] = c.hi;
+        uint4 r;
+        r.x = st;
+        r.y = lo;
+        r.z = hi;
+        r.w = tile_pos(tile, n, st);
+        reinterpret_cast<uint4*>(qbuf)[slot] = r;
       }
     }
-    qcur += n;
-    if (n < 32) break;
-    qcache_fetch(c, p.qs, p.Q, qcur, lane);
+    __syncwarp();   // every lane has read the window before it is refilled
+    qcur += k;
+    if (k < 32) break;
   }
   if (lane == 0) {
     tq[0] = tq0;
     tq[1] = qcur;
   }
-  qcache_fetch(c, p.qs, p.Q, qcur, lane);   // consumed at the next tile
+  qpre_issue(qpre, p.qs, p.Q, qcur, lane);   // read at the next tile
+  pbase = qcur;
 }
 
-// Answer of one query by one warp: window + row probe, plus the tile correction
-// (tile == nullptr: no correction).
+// Answer of one query by one warp: window + row probe, plus the tile's events
+// before position `pos` inside [lo, hi) (tile == nullptr: no correction).
 __device__ __forceinline__ int64_t answer_one(const ChainParams& p, const int32_t* H, const int32_t* T,
                                               const unsigned long long* T64, const int64_t* row, bool rows_live,
-                                              bool wide_tile, const uint4* tile, int n, uint32_t qst, uint32_t lo,
+                                              bool wide_tile, const uint4* tile, uint32_t pos, uint32_t lo,
                                               uint32_t hi, int lane) {
   lo = min(lo, p.C);
   hi = min(hi, p.C);
   if (lo >= hi) return 0;
+  const uint32_t w = hi - lo;
   int32_t part = probe32(H, T, lo, hi, p.chs, lane);
   uint64_t wide = 0;
   if (tile) {
-    if (wide_tile) wide = tile_corr<true>(tile, n, qst, lo, hi, lane);
-    else part += (int32_t)(uint32_t)tile_corr<false>(tile, n, qst, lo, hi, lane);
+    if (wide_tile) {
+      for (uint32_t j = lane; j < pos; j += 32) {
+        const uint4 e = tile[j];
+        if (e.y - lo < w) wide += ((uint64_t)e.w << 32) | e.z;
+      }
+    } else {
+#pragma unroll 4
+      for (uint32_t j = lane; j < pos; j += 32) {
+        const uint4 e = tile[j];
+        if (e.y - lo < w) part += (int32_t)e.z;
+      }
+    }
   }
   int64_t total = (int64_t)(int32_t)__reduce_add_sync(0xffffffffu, (uint32_t)part);
   if (rows_live || wide_tile) {
@@ -281,29 +294,37 @@ __device__ __forceinline__ int64_t answer_one(const ChainParams& p, const int32_
   return total;
 }
 
-__global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
+// Tile geometry: NT threads, EPT events per thread, TL = NT * EPT events per tile
+// (<= 1024, so an int32-safe tile's absolute sum stays below 2^29); MINB CTAs per SM.
+template <int NT, int EPT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
+  constexpr int NW = NT / 32, QW = NW - 1, TL = NT * EPT;
+  static_assert(TL <= TE && NW <= kMaxWarps && NW >= 2, "tile geometry");
   extern __shared__ __align__(128) unsigned char sm[];
   const uint32_t C = p.C;
-  const SweepSmem SL = sweep_smem(C, p.nch);
+  const SweepSmem SL = sweep_smem(C, p.nch, TL);
   uint4* ring = reinterpret_cast<uint4*>(sm + SL.ring);
   int32_t* H = reinterpret_cast<int32_t*>(sm + SL.H);
   int32_t* T = reinterpret_cast<int32_t*>(sm + SL.T);
   unsigned long long* T64 = reinterpret_cast<unsigned long long*>(sm + SL.T64);
-  uint32_t* qbuf = reinterpret_cast<uint32_t*>(sm + SL.qbuf);
+  uint32_t* qbuf = reinterpret_cast<uint32_t*>(sm + SL.qbuf);   // [2][QB] uint4, by tile parity
+  uint32_t* qpre = reinterpret_cast<uint32_t*>(sm + SL.qpre);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + SL.bar);
   Misc* m = reinterpret_cast<Misc*>(sm + SL.misc);
+  auto qbuf_of = [&](int t) { return qbuf + (size_t)(t & 1) * QB * 4; };
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.x;
   const int64_t e0 = (int64_t)b * p.E / p.B, e1 = (int64_t)(b + 1) * p.E / p.B;
   const int64_t ne = e1 - e0;
-  const int ntiles = (int)((ne + TE - 1) / TE);
+  const int ntiles = (int)((ne + TL - 1) / TL);
   int64_t* row = p.rows + (int64_t)b * (C + 1);
-  auto tile_n = [&](int t) { return (int)min((int64_t)TE, ne - (int64_t)t * TE); };
+  auto tile_n = [&](int t) { return (int)min((int64_t)TL, ne - (int64_t)t * TL); };
 
   for (uint32_t i = tid; i < C; i += NT) H[i] = 0;
   for (int i = tid; i < p.nch * 32; i += NT) T[i] = 0;
   for (int i = tid; i < p.nch; i += NT) T64[i] = 0;
+  if (tid < 2 * kMaxWarps) m->wsum[tid / kMaxWarps][tid % kMaxWarps] = 0;
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -313,7 +334,7 @@ __global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
   int issued = 0;   // tiles whose copy was issued (thread 0)
   if (tid == 0) {
     for (; issued < NS && issued < ntiles; ++issued)
-      bulk_load(ring + (issued % NS) * TE, p.ev + e0 + (int64_t)issued * TE, (uint32_t)tile_n(issued) * 16u,
+      bulk_load(ring + (issued % NS) * TL, p.ev + e0 + (int64_t)issued * TL, (uint32_t)tile_n(issued) * 16u,
                 &bar[issued % NS]);
   }
   // input checks spread over every sweep thread: parent[v] = v - 1, and every query
@@ -331,11 +352,10 @@ __global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
   // the block's first query: position >= e0, i.e. state >= state of event e0 - 1
   const int64_t qstart = b > 0 ? first_query_at_or_after(p.qs, p.Q, m->prev_state[0]) : 0;
 
-  QCache qc{-1, 0, 0, 0};
-  int64_t qcur = qstart;
-  if (warp == QW) qcache_fetch(qc, p.qs, p.Q, qcur, lane);
+  int64_t qcur = qstart, pbase = qstart;
+  if (warp == QW) qpre_issue(qpre, p.qs, p.Q, qcur, lane);
 
-  uint4 cur[kChainEvPerThread];
+  uint4 cur[EPT];
   bool rows_live = false;   // the int64 row holds data (set by the first flush)
   uint32_t win = 0;         // |delta| sum in the int32 window (the same in every thread)
   int bigp = 0, lost = 0;
@@ -345,15 +365,13 @@ __global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
       lost = 1;
     } else {
       const int n = tile_n(0);
-      uint64_t s = 0;
 #pragma unroll
-      for (int k = 0; k < kChainEvPerThread; ++k) {
+      for (int k = 0; k < EPT; ++k) {
         const int idx = tid + k * NT;
         cur[k] = idx < n ? ring[idx] : make_uint4(0, 0, 0, 0);
-        if (idx < n) s += uabs64(((uint64_t)cur[k].w << 32) | cur[k].z);
+        bigp |= !small_delta(cur[k]);
       }
-      bigp = s >= kBigThread;
-      if (warp == QW) find_tile_queries(p, qc, qcur, ring[n - 1].x, qbuf, m->tq[0], lane);
+      if (warp == QW) find_tile_queries(p, qpre, pbase, qcur, ring, n, qbuf_of(0), m->tq[0], lane);
     }
   }
   // end-of-tile barrier: OR of the next tile's wide flag and of lost waits (a
@@ -373,22 +391,18 @@ __global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
   int t = 0;
   for (; t < ntiles && !aborted; ++t) {
     const int n = tile_n(t);
-    const uint4* tile = ring + (t % NS) * TE;
+    const uint4* tile = ring + (t % NS) * TL;
     if (tid == 0 && t >= 1 && issued < ntiles) {
       // stage (t-1) % NS was released by the barrier that ended tile t-1
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      bulk_load(ring + (issued % NS) * TE, p.ev + e0 + (int64_t)issued * TE, (uint32_t)tile_n(issued) * 16u,
+      bulk_load(ring + (issued % NS) * TL, p.ev + e0 + (int64_t)issued * TL, (uint32_t)tile_n(issued) * 16u,
                 &bar[issued % NS]);
       ++issued;
     }
     const int64_t tq0 = m->tq[t & 1][0], tq1 = m->tq[t & 1][1];
     if (t > 0) {   // window updates of the previous tile, summed over its warps
-      const uint4* w4 = reinterpret_cast<const uint4*>(m->wsum[(t - 1) & 1]);
-#pragma unroll
-      for (int i = 0; i < NW / 4; ++i) {
-        const uint4 v = w4[i];
-        win += v.x + v.y + v.z + v.w;
-      }
+      const uint32_t v = lane < NW ? m->wsum[(t - 1) & 1][lane] : 0u;
+      win += __reduce_add_sync(0xffffffffu, v);
     }
     // flush the int32 window into the int64 row: before it could overflow, and
     // before a wide tile (which adds straight into the row)
@@ -414,42 +428,61 @@ __global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
       rows_live = true;
       __syncthreads();
     }
-    // the tile's queries, one warp each
-    if (tq1 > tq0) {
-      for (int64_t i = tq0 + warp; i < tq1; i += NW) {
-        uint32_t qst, lo, hi;
+    // the tile's queries, one warp each; meanwhile the query warp waits for the next
+    // tile and finds its queries (into the other query buffer)
+    const bool has_q = tq1 > tq0;
+    bool next_found = false;
+    if (has_q) {
+      if (warp == QW) {
+        if (t + 1 < ntiles) {
+          const uint4* nt = ring + ((t + 1) % NS) * TL;
+          if (!mbar_wait(&bar[(t + 1) % NS], (uint32_t)(((t + 1) / NS) & 1))) {
+            set_status(p.status, BW_STATUS_TIMEOUT);
+            lost = 1;
+          } else {
+            find_tile_queries(p, qpre, pbase, qcur, nt, tile_n(t + 1), qbuf_of(t + 1), m->tq[(t + 1) & 1], lane);
+          }
+        }
+        next_found = true;
+      }
+      const uint4* qb = reinterpret_cast<const uint4*>(qbuf_of(t));
+      for (int64_t i = tq0 + warp; warp < QW && i < tq1; i += QW) {
+        uint32_t lo, hi, pos;
         if (i - tq0 < QB) {
-          const uint32_t* r = qbuf + 3 * (i - tq0);
-          qst = r[0];
-          lo = r[1];
-          hi = r[2];
+          const uint4 r = qb[i - tq0];
+          lo = r.y;
+          hi = r.z;
+          pos = r.w;
         } else {
           const uint32_t* r = reinterpret_cast<const uint32_t*>(p.qs + i);
-          qst = r[0];
           lo = r[1];
           hi = r[2];
+          pos = tile_pos(tile, n, r[0]);
         }
-        const int64_t a = answer_one(p, H, T, T64, row, rows_live, big != 0, tile, n, qst, lo, hi, lane);
+        const int64_t a = answer_one(p, H, T, T64, row, rows_live, big != 0, tile, pos, lo, hi, lane);
         if (lane == 0) p.ans[i] = a;
       }
       __syncthreads();
     }
-    // apply the tile
+    // apply the tile (the state before each event comes from the previous lane; lane
+    // 0 reads it from the tile, or from the previous tile for the first event)
     uint32_t wsum = 0;
 #pragma unroll
-    for (int k = 0; k < kChainEvPerThread; ++k) {
+    for (int k = 0; k < EPT; ++k) {
       const int idx = tid + k * NT;
+      const uint32_t up = __shfl_up_sync(0xffffffffu, cur[k].x, 1);
       if (idx < n) {
         const uint4 e = cur[k];
-        const uint32_t prev = idx ? tile[idx - 1].x : m->prev_state[t & 1];
+        const uint32_t prev = lane ? up : (idx ? tile[idx - 1].x : m->prev_state[t & 1]);
         if (e.x < prev) set_status(p.status, BW_STATUS_EVENTS_UNSORTED);
         if (e.x >= (uint32_t)p.S) set_status(p.status, BW_STATUS_STATE_RANGE);
         if (e.y >= C) {
           set_status(p.status, BW_STATUS_EVENT_KEY_RANGE);
         } else if (!big) {
-          atomicAdd(&H[e.y], (int32_t)e.z);
-          atomicAdd(&T[(e.y >> p.chs) * 32 + lane], (int32_t)e.z);
-          wsum += (uint32_t)uabs64(((uint64_t)e.w << 32) | e.z);
+          const int32_t d = (int32_t)e.z;
+          atomicAdd(&H[e.y], d);
+          atomicAdd(&T[(e.y >> p.chs) * 32 + lane], d);
+          wsum += (uint32_t)(d < 0 ? -d : d);
         } else {
           const uint64_t d = ((uint64_t)e.w << 32) | e.z;
           atomicAdd(reinterpret_cast<unsigned long long*>(row + e.y), (unsigned long long)d);
@@ -462,35 +495,36 @@ __global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
       if (lane == 0) m->wsum[t & 1][warp] = ws;
     }
     if (tid == 0) m->prev_state[(t + 1) & 1] = tile[n - 1].x;
-    // next tile: wait for its copy, load this thread's events, find its queries
+    // next tile: wait for its copy, load this thread's events (and, when no query
+    // phase ran, let the query warp find the next tile's queries)
     bigp = 0;
     if (t + 1 < ntiles) {
       const int nn = tile_n(t + 1);
-      const uint4* nt = ring + ((t + 1) % NS) * TE;
+      const uint4* nt = ring + ((t + 1) % NS) * TL;
       if (!mbar_wait(&bar[(t + 1) % NS], (uint32_t)(((t + 1) / NS) & 1))) {
         set_status(p.status, BW_STATUS_TIMEOUT);
         lost = 1;
       } else {
-        uint64_t s = 0;
 #pragma unroll
-        for (int k = 0; k < kChainEvPerThread; ++k) {
+        for (int k = 0; k < EPT; ++k) {
           const int idx = tid + k * NT;
           cur[k] = idx < nn ? nt[idx] : make_uint4(0, 0, 0, 0);
-          if (idx < nn) s += uabs64(((uint64_t)cur[k].w << 32) | cur[k].z);
+          bigp |= !small_delta(cur[k]);
         }
-        bigp = s >= kBigThread;
-        if (warp == QW) find_tile_queries(p, qc, qcur, nt[nn - 1].x, qbuf, m->tq[(t + 1) & 1], lane);
+        if (warp == QW && !next_found)
+          find_tile_queries(p, qpre, pbase, qcur, nt, nn, qbuf_of(t + 1), m->tq[(t + 1) & 1], lane);
       }
     }
     aborted = tile_barrier(bigp, lost, big);
   }
 
+  // the query warp's last window copy lands before its shared memory goes away
+  if (warp == QW) asm volatile("cp.async.wait_all;" ::: "memory");
   if (aborted) {
     // wait (bounded) for the copies still in flight before the CTA exits: tiles
     // from the one whose wait gave up to the last one issued
     if (tid == 0)
-      for (int u = t; u < issued; ++u)
-        mbar_wait(&bar[u % NS], (uint32_t)((u / NS) & 1));
+      for (int u = t; u < issued; ++u) mbar_wait(&bar[u % NS], (uint32_t)((u / NS) & 1));
     __syncthreads();
     return;
   }
@@ -502,8 +536,7 @@ __global__ void __launch_bounds__(NT, 2) k_chain_sweep(ChainParams p) {
     const int64_t from = m->tail_q0;
     for (int64_t i = from + warp; i < qend; i += NW) {
       const uint32_t* r = reinterpret_cast<const uint32_t*>(p.qs + i);
-      const uint32_t qst = r[0], lo = r[1], hi = r[2];
-      const int64_t a = answer_one(p, H, T, T64, row, rows_live, false, nullptr, 0, qst, lo, hi, lane);
+      const int64_t a = answer_one(p, H, T, T64, row, rows_live, false, nullptr, 0, r[1], r[2], lane);
       if (lane == 0) p.ans[i] = a;
     }
     if (warp == QW) qcur = qend;
@@ -547,11 +580,11 @@ __global__ void k_chain_colfix(ChainParams p) {
 
 // Block b >= 1: its carry row scanned over keys (row[k] = carry below key k), then
 // every query of the block adds the carry inside [lo, hi).
-__global__ void __launch_bounds__(NT) k_chain_fixup(ChainParams p) {
+__global__ void __launch_bounds__(kChainThreads) k_chain_fixup(ChainParams p) {
   const int b = blockIdx.x + 1;
   int64_t* row = p.rows + (int64_t)b * (p.C + 1);
   const uint32_t n = p.C + 1;
-  const uint32_t per = (n + NT - 1) / NT;
+  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
   const uint32_t lo0 = threadIdx.x * per, hi0 = min(n, lo0 + per);
   uint64_t local = 0;
   for (uint32_t i = lo0; i < hi0; ++i) local += i < p.C ? (uint64_t)row[i] : 0;
@@ -563,11 +596,35 @@ __global__ void __launch_bounds__(NT) k_chain_fixup(ChainParams p) {
   }
   __syncthreads();
   const int64_t q0 = p.btab[2 * b], q1 = p.btab[2 * b + 1];
-  for (int64_t i = q0 + threadIdx.x; i < q1; i += NT) {
+  for (int64_t i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
     const BwQuery q = p.qs[i];
     const uint32_t lo = min(q.lo, p.C), hi = min(q.hi, p.C);
     if (lo < hi) p.ans[i] = (int64_t)((uint64_t)p.ans[i] + (uint64_t)row[hi] - (uint64_t)row[lo]);
   }
+}
+
+// Sweep geometries: threads per CTA, events per thread, CTAs per SM the kernel is
+// compiled for.  Smaller CTAs give more state blocks and shorter per-tile
+// barriers; larger ones amortise the query warp over more appliers.
+struct Geometry {
+  int threads, ept, minb;
+};
+constexpr Geometry kGeometries[] = {{128, 4, 5}, {256, 4, 3}, {512, 2, 2}};
+constexpr int kNumGeometries = 3;
+
+// BW_CHAIN_GEOMETRY=<index into kGeometries> pins the geometry (tuning runs).
+// Otherwise: 256 threads x 4 events when at least two such CTAs fit an SM and the
+// events fill every one of them with full state blocks (measured fastest on
+// byte-dominated chains); else the geometry with the most resident threads per SM
+// (few, short state blocks: wide CTAs finish each sooner).
+int geometry_override() {
+  static const int g = [] {
+    const char* v = std::getenv("BW_CHAIN_GEOMETRY");
+    if (!v || !*v) return -1;
+    const int i = std::atoi(v);
+    return i >= 0 && i < kNumGeometries ? i : -1;
+  }();
+  return g;
 }
 
 std::once_flag g_attr_once;
@@ -591,10 +648,33 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
   while ((1u << lg) < s.C) ++lg;
   s.chs = lg - 5 > 5 ? lg - 5 : 5;
   s.nch = (int32_t)((s.C + (1u << s.chs) - 1) >> s.chs);
-  s.smem = sweep_smem(s.C, s.nch).bytes;
-  s.ctas_per_sm = (int32_t)(kSmemPerSM / (s.smem + 1024));
-  if (s.ctas_per_sm > 2) s.ctas_per_sm = 2;   // __launch_bounds__(512, 2)
-  if (s.ctas_per_sm < 1) return BW_EINVAL;
+  int pin = geometry_override();
+  int fit[kNumGeometries];
+  size_t need[kNumGeometries];
+  for (int g = 0; g < kNumGeometries; ++g) {
+    const Geometry& G = kGeometries[g];
+    need[g] = sweep_smem(s.C, s.nch, G.threads * G.ept).bytes;
+    fit[g] = (int)(kSmemPerSM / (need[g] + 1024));
+    if (fit[g] > G.minb) fit[g] = G.minb;
+  }
+  if (pin >= 0 && fit[pin] < 1) pin = -1;
+  if (pin < 0 && fit[1] >= 2 && s.E >= (int64_t)sms * fit[1] * kChainMinBlockEvents) pin = 1;
+  int best = -1, best_threads = 0;
+  for (int g = 0; g < kNumGeometries; ++g) {
+    const Geometry& G = kGeometries[g];
+    const size_t smem = need[g];
+    const int ctas = fit[g];
+    if (ctas < 1) continue;
+    if (pin >= 0 ? g == pin : ctas * G.threads >= best_threads) {
+      best = g;
+      best_threads = ctas * G.threads;
+      s.threads = G.threads;
+      s.ept = G.ept;
+      s.smem = smem;
+      s.ctas_per_sm = ctas;
+    }
+  }
+  if (best < 0) return BW_EINVAL;
   int64_t B = a->blocks > 0 ? a->blocks : (s.E + kChainMinBlockEvents - 1) / kChainMinBlockEvents;
   const int64_t cap = (int64_t)sms * s.ctas_per_sm;
   if (a->blocks <= 0 && B > cap) B = cap;
@@ -614,7 +694,10 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
 
 int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int* kernels) {
   std::call_once(g_attr_once, [] {
-    g_attr_err = cudaFuncSetAttribute(k_chain_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemLimit);
+    const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    g_attr_err = cudaFuncSetAttribute(k_chain_sweep<128, 4, 5>, A, kSmemLimit);
+    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 4, 3>, A, kSmemLimit);
+    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<512, 2, 2>, A, kSmemLimit);
   });
   if (g_attr_err != cudaSuccess) return report(g_attr_err, "chain sweep attribute");
   cudaStream_t st = static_cast<cudaStream_t>(a->stream);
@@ -642,7 +725,9 @@ int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int*
     for (int i = 0; i <= BW_STAGE_SWEEP; ++i)
       if ((rc = report(cudaEventRecord(evs->ev[i], st), "event record"))) return rc;
   }
-  k_chain_sweep<<<s.B, NT, s.smem, st>>>(p);
+  if (s.threads == 128) k_chain_sweep<128, 4, 5><<<s.B, 128, s.smem, st>>>(p);
+  else if (s.threads == 256) k_chain_sweep<256, 4, 3><<<s.B, 256, s.smem, st>>>(p);
+  else k_chain_sweep<512, 2, 2><<<s.B, 512, s.smem, st>>>(p);
   int k = 1;
   if ((rc = report(cudaGetLastError(), "chain sweep launch"))) return rc;
   if (evs && (rc = report(cudaEventRecord(evs->ev[BW_STAGE_SWEEP + 1], st), "event record"))) return rc;
@@ -650,7 +735,7 @@ int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int*
     const dim3 g((unsigned)s.nseg, (s.C + 255) / 256);
     k_chain_colsum<<<g, 256, 0, st>>>(p);
     k_chain_colfix<<<g, 256, 0, st>>>(p);
-    k_chain_fixup<<<s.B - 1, NT, 0, st>>>(p);
+    k_chain_fixup<<<s.B - 1, kChainThreads, 0, st>>>(p);
     k += 3;
     if ((rc = report(cudaGetLastError(), "chain carry launch"))) return rc;
   }

@@ -19,9 +19,8 @@
 
 namespace bw {
 
-constexpr int kChainThreads = 512;
-constexpr int kChainEvPerThread = 2;
-constexpr int kChainTile = kChainThreads * kChainEvPerThread;   // events per tile (16 KiB)
+constexpr int kChainThreads = 512;                              // largest sweep CTA (and the fix-up CTA)
+constexpr int kChainTile = 1024;                                // largest tile, events (16 KiB)
 constexpr int kChainStages = 3;                                 // tiles in the shared-memory ring
 constexpr int kChainQBuf = 128;                                 // query records staged per tile
 constexpr uint32_t kChainMaxKeys = 32768;                       // key domain held in shared memory
@@ -37,6 +36,8 @@ struct ChainSpec {
   int32_t nch = 1;        // chunks
   int32_t nseg = 1;       // column-scan segments
   int32_t ctas_per_sm = 1;
+  int32_t threads = 512;  // sweep geometry: threads per CTA, events per thread
+  int32_t ept = 2;
   size_t smem = 0;        // dynamic shared memory of the sweep
   size_t off_btab = 0, off_rows = 0, off_seg = 0, total = 0;   // workspace layout
 };
