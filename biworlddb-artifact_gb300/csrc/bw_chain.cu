@@ -41,11 +41,12 @@ namespace bw {
 namespace {
 
 constexpr int TE = kChainTile;   // largest tile (the shared-memory ring is sized per geometry)
-constexpr int NS = kChainStages;
 constexpr int QB = kChainQBuf;
 constexpr int kMaxWarps = kChainThreads / 32;
+constexpr int kChunkShift = 5;                   // chunk totals cover 32 keys each
+constexpr uint32_t kFlatKeys = 4096;             // key domains up to this size keep no chunk totals
 constexpr uint32_t kWaitLimit = 1u << 22;        // mbarrier polls before a stage is declared lost
-constexpr uint32_t kFlushAt = 1u << 28;          // window |delta| sum that triggers a flush
+constexpr uint32_t kFoldAt = 1u << 28;           // window |delta| sum that triggers a fold
 // A tile is int32-safe when every delta lies in (-2^19, 2^19): with at most 1024
 // events its absolute sum is then below 2^29.
 
@@ -58,8 +59,9 @@ struct ChainParams {
   int32_t S;
   uint32_t C;
   int32_t B;
-  int32_t chs, nch, nseg;
-  int64_t* rows;          // B rows of C+1 int64
+  int32_t nch, nseg;
+  int64_t* rows;          // B rows of C+1 int64: key prefixes (row[k] = sum below key k)
+  int64_t* wide;          // B rows of C int64: key histogram of the block's wide tiles
   int64_t* btab;          // B x (first query, end query)
   int64_t* seg;           // nseg rows of C+1 uint64
   int32_t* status;
@@ -73,23 +75,23 @@ struct Misc {
   int64_t tq[2][2];              // queries [tq0, tq1) of a tile
   uint32_t prev_state[2];        // state of the event before a tile
   int64_t tail_q0;
+  unsigned long long scan[kMaxWarps];   // warp totals of the fold's key scan
 };
 
 // Dynamic shared memory of the sweep, every region 16-byte aligned.
 struct SweepSmem {
-  size_t ring, H, T, T64, qbuf, qpre, bar, misc, bytes;
+  size_t ring, H, T, qbuf, qpre, bar, misc, bytes;
 };
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
-__host__ __device__ inline SweepSmem sweep_smem(uint32_t C, int nch, int te) {
+__host__ __device__ inline SweepSmem sweep_smem(uint32_t C, int nch, int te, int ns) {
   SweepSmem L;
   size_t o = 0;
-  L.ring = o;  o = al16(o + (size_t)NS * te * 16);
+  L.ring = o;  o = al16(o + (size_t)ns * te * 16);
   L.H = o;     o = al16(o + (size_t)C * 4);
-  L.T = o;     o = al16(o + (size_t)nch * 32 * 4);
-  L.T64 = o;   o = al16(o + (size_t)nch * 8);
+  L.T = o;     o = al16(o + (size_t)nch * 4);
   L.qbuf = o;  o = al16(o + 2 * (size_t)QB * 16);   // two tiles' query records
   L.qpre = o;  o = al16(o + 32 * 12);                // prefetched window of 32 query records
-  L.bar = o;   o = al16(o + (size_t)NS * 8);
+  L.bar = o;   o = al16(o + (size_t)ns * 8);
   L.misc = o;  o = al16(o + sizeof(Misc));
   L.bytes = o;
   return L;
@@ -140,36 +142,35 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
   return v;
 }
 
-// Lane share of the window sum over keys [lo, hi): partial chunks from H, whole
-// chunks from the lane's own chunk-total copy.
-__device__ __forceinline__ int32_t probe32(const int32_t* H, const int32_t* T, uint32_t lo, uint32_t hi, int chs,
-                                           int lane) {
-  const uint32_t clo = (lo + (1u << chs) - 1) >> chs, chi = hi >> chs;
+// Lane share of the window sum over keys [lo, hi) (lo < hi <= C): the partial
+// chunks at either end from H (fewer than 32 keys each), the whole chunks from T.
+__device__ __forceinline__ int32_t probe32(const int32_t* H, const int32_t* T, uint32_t lo, uint32_t hi, int lane) {
+  const uint32_t clo = (lo + 31) >> kChunkShift, chi = hi >> kChunkShift;
   int32_t s = 0;
-  if (clo >= chi) {
+  if (clo >= chi) {   // fewer than 64 keys
     for (uint32_t k = lo + lane; k < hi; k += 32) s += H[k];
     return s;
   }
-  for (uint32_t k = lo + lane; k < (clo << chs); k += 32) s += H[k];
-  for (uint32_t c = clo; c < chi; ++c) s += T[c * 32 + lane];
-  for (uint32_t k = (chi << chs) + lane; k < hi; k += 32) s += H[k];
+  const uint32_t a = lo + lane, z = (chi << kChunkShift) + lane;
+  if (a < (clo << kChunkShift)) s += H[a];
+  if (z < hi) s += H[z];
+  for (uint32_t c = clo + lane; c < chi; c += 32) s += T[c];
   return s;
 }
 
-// Lane share of the int64 row over [lo, hi): partial chunks from the row, whole
-// chunks from the int64 chunk totals.  Row words are read from L2 (__ldcg): wide
-// tiles update them with global atomics, which do not update L1.
-__device__ __forceinline__ uint64_t probe64(const int64_t* row, const unsigned long long* T64, uint32_t lo,
-                                            uint32_t hi, int chs, int lane) {
-  const uint32_t clo = (lo + (1u << chs) - 1) >> chs, chi = hi >> chs;
-  uint64_t s = 0;
-  if (clo >= chi) {
-    for (uint32_t k = lo + lane; k < hi; k += 32) s += (uint64_t)__ldcg(row + k);
-    return s;
+// Lane share of the window sum over keys [lo, hi) (lo < hi <= C) without chunk
+// totals: 128-bit reads of H, four keys per lane, masked to the interval.  H is
+// 16-byte aligned and padded to a multiple of four keys, so the last read stays in
+// the region; padding keys fall outside [lo, hi).
+__device__ __forceinline__ int32_t probe_flat(const int32_t* H, uint32_t lo, uint32_t hi, int lane) {
+  const uint32_t w = hi - lo;
+  int32_t s = 0;
+#pragma unroll 2
+  for (uint32_t k = (lo & ~3u) + 4 * lane; k < hi; k += 128) {
+    const int4 v = *reinterpret_cast<const int4*>(H + k);
+    const uint32_t d = k - lo;
+    s += (d < w ? v.x : 0) + (d + 1 < w ? v.y : 0) + (d + 2 < w ? v.z : 0) + (d + 3 < w ? v.w : 0);
   }
-  for (uint32_t k = lo + lane; k < (clo << chs); k += 32) s += (uint64_t)__ldcg(row + k);
-  for (uint32_t c = clo + lane; c < chi; c += 32) s += T64[c];
-  for (uint32_t k = (chi << chs) + lane; k < hi; k += 32) s += (uint64_t)__ldcg(row + k);
   return s;
 }
 
@@ -260,17 +261,19 @@ __device__ void find_tile_queries(const ChainParams& p, uint32_t* qpre, int64_t&
   pbase = qcur;
 }
 
-// Answer of one query by one warp: window + row probe, plus the tile's events
-// before position `pos` inside [lo, hi) (tile == nullptr: no correction).
+// Answer of one query by one warp, valid in lane 0: the folded key prefix row
+// (P[hi] - P[lo], when it holds data), the window probe, and the tile's first
+// `pos` events inside [lo, hi) (tile == nullptr: none).
 __device__ __forceinline__ int64_t answer_one(const ChainParams& p, const int32_t* H, const int32_t* T,
-                                              const unsigned long long* T64, const int64_t* row, bool rows_live,
-                                              bool wide_tile, const uint4* tile, uint32_t pos, uint32_t lo,
-                                              uint32_t hi, int lane) {
+                                              const int64_t* P, bool rows_live, bool wide_tile, const uint4* tile,
+                                              uint32_t pos, uint32_t lo, uint32_t hi, int lane) {
   lo = min(lo, p.C);
   hi = min(hi, p.C);
   if (lo >= hi) return 0;
   const uint32_t w = hi - lo;
-  int32_t part = probe32(H, T, lo, hi, p.chs, lane);
+  uint64_t pv = 0;
+  if (rows_live && lane < 2) pv = (uint64_t)__ldcg(P + (lane ? hi : lo));   // both ends in flight at once
+  int32_t part = p.nch ? probe32(H, T, lo, hi, lane) : probe_flat(H, lo, hi, lane);
   uint64_t wide = 0;
   if (tile) {
     if (wide_tile) {
@@ -286,27 +289,67 @@ __device__ __forceinline__ int64_t answer_one(const ChainParams& p, const int32_
       }
     }
   }
-  int64_t total = (int64_t)(int32_t)__reduce_add_sync(0xffffffffu, (uint32_t)part);
-  if (rows_live || wide_tile) {
-    if (rows_live) wide += probe64(row, T64, lo, hi, p.chs, lane);
-    total = (int64_t)((uint64_t)total + warp_sum_u64(wide));
+  uint64_t total = (uint64_t)(int64_t)(int32_t)__reduce_add_sync(0xffffffffu, (uint32_t)part);
+  if (wide_tile) total += warp_sum_u64(wide);
+  const uint64_t phi = __shfl_down_sync(0xffffffffu, pv, 1);
+  return (int64_t)(total + phi - pv);
+}
+
+// Fold of the window (and of the wide tiles' histogram) into the block's key
+// prefix row: P[k+1] += sum of H[j] + wide[j] over j <= k.  Each thread takes a
+// contiguous key segment; a CTA-wide exclusive scan of the segment sums gives its
+// base.  H, T and the consumed wide entries return to zero.  All threads call it.
+template <int NT>
+__device__ void fold(const ChainParams& p, int32_t* H, int32_t* T, int64_t* P, int64_t* wide, bool rows_live,
+                     bool wide_live, Misc* m) {
+  constexpr int NW = NT / 32;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t C = p.C, per = (C + NT - 1) / NT;
+  const uint32_t k0 = min(C, (uint32_t)tid * per), k1 = min(C, k0 + per);
+  uint64_t s = 0;
+  for (uint32_t k = k0; k < k1; ++k) {
+    s += (uint64_t)(int64_t)H[k];
+    if (wide_live) s += (uint64_t)__ldcg(wide + k);
   }
-  return total;
+  uint64_t incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) m->scan[warp] = incl;
+  __syncthreads();
+  uint64_t run = incl - s;
+#pragma unroll
+  for (int w = 0; w < NW; ++w)
+    if (w < warp) run += m->scan[w];
+  for (uint32_t k = k0; k < k1; ++k) {
+    run += (uint64_t)(int64_t)H[k];
+    H[k] = 0;
+    if (wide_live) {
+      run += (uint64_t)__ldcg(wide + k);
+      wide[k] = 0;
+    }
+    P[k + 1] = rows_live ? (int64_t)((uint64_t)__ldcg(P + k + 1) + run) : (int64_t)run;
+  }
+  if (tid == 0 && !rows_live) P[0] = 0;
+  for (int c = tid; c < p.nch; c += NT) T[c] = 0;
+  __syncthreads();
 }
 
 // Tile geometry: NT threads, EPT events per thread, TL = NT * EPT events per tile
-// (<= 1024, so an int32-safe tile's absolute sum stays below 2^29); MINB CTAs per SM.
-template <int NT, int EPT, int MINB>
+// (<= 1024, so an int32-safe tile's absolute sum stays below 2^29); MINB CTAs per SM;
+// NS tiles in the shared-memory ring.
+template <int NT, int EPT, int MINB, int NS>
 __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
   constexpr int NW = NT / 32, QW = NW - 1, TL = NT * EPT;
   static_assert(TL <= TE && NW <= kMaxWarps && NW >= 2, "tile geometry");
   extern __shared__ __align__(128) unsigned char sm[];
   const uint32_t C = p.C;
-  const SweepSmem SL = sweep_smem(C, p.nch, TL);
+  const SweepSmem SL = sweep_smem(C, p.nch, TL, NS);
   uint4* ring = reinterpret_cast<uint4*>(sm + SL.ring);
   int32_t* H = reinterpret_cast<int32_t*>(sm + SL.H);
   int32_t* T = reinterpret_cast<int32_t*>(sm + SL.T);
-  unsigned long long* T64 = reinterpret_cast<unsigned long long*>(sm + SL.T64);
   uint32_t* qbuf = reinterpret_cast<uint32_t*>(sm + SL.qbuf);   // [2][QB] uint4, by tile parity
   uint32_t* qpre = reinterpret_cast<uint32_t*>(sm + SL.qpre);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + SL.bar);
@@ -318,12 +361,12 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
   const int64_t e0 = (int64_t)b * p.E / p.B, e1 = (int64_t)(b + 1) * p.E / p.B;
   const int64_t ne = e1 - e0;
   const int ntiles = (int)((ne + TL - 1) / TL);
-  int64_t* row = p.rows + (int64_t)b * (C + 1);
+  int64_t* P = p.rows + (int64_t)b * (C + 1);
+  int64_t* wrow = p.wide + (int64_t)b * C;
   auto tile_n = [&](int t) { return (int)min((int64_t)TL, ne - (int64_t)t * TL); };
 
   for (uint32_t i = tid; i < C; i += NT) H[i] = 0;
-  for (int i = tid; i < p.nch * 32; i += NT) T[i] = 0;
-  for (int i = tid; i < p.nch; i += NT) T64[i] = 0;
+  for (int i = tid; i < p.nch; i += NT) T[i] = 0;
   if (tid < 2 * kMaxWarps) m->wsum[tid / kMaxWarps][tid % kMaxWarps] = 0;
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
@@ -356,9 +399,12 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
   if (warp == QW) qpre_issue(qpre, p.qs, p.Q, qcur, lane);
 
   uint4 cur[EPT];
-  bool rows_live = false;   // the int64 row holds data (set by the first flush)
+  bool rows_live = false;   // the prefix row holds data (set by the first fold)
+  bool wide_init = false;   // the wide histogram row has been zeroed
+  bool wide_live = false;   // a wide tile was applied since the last fold
   uint32_t win = 0;         // |delta| sum in the int32 window (the same in every thread)
   int bigp = 0, lost = 0;
+  uint32_t bad = 0;         // event defects seen by this thread (reported at the end)
   if (ntiles > 0) {
     if (!mbar_wait(&bar[0], 0)) {
       set_status(p.status, BW_STATUS_TIMEOUT);
@@ -404,28 +450,17 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
       const uint32_t v = lane < NW ? m->wsum[(t - 1) & 1][lane] : 0u;
       win += __reduce_add_sync(0xffffffffu, v);
     }
-    // flush the int32 window into the int64 row: before it could overflow, and
-    // before a wide tile (which adds straight into the row)
-    if (win >= kFlushAt || (big && (win > 0 || !rows_live))) {
-      for (uint32_t k = tid; k < C; k += NT) {
-        const int32_t v = H[k];
-        if (rows_live) {
-          if (v) row[k] = (int64_t)((uint64_t)__ldcg(row + k) + (uint64_t)(int64_t)v);
-        } else {
-          row[k] = v;
-        }
-        H[k] = 0;
-      }
-      for (int c = tid; c < p.nch; c += NT) {
-        int64_t s = 0;
-        for (int l = 0; l < 32; ++l) {
-          s += T[c * 32 + l];
-          T[c * 32 + l] = 0;
-        }
-        T64[c] += (unsigned long long)s;
-      }
+    // fold the window into the prefix row before it could overflow, and after a
+    // wide tile (whose events went to the wide histogram)
+    if (win >= kFoldAt || wide_live) {
+      fold<NT>(p, H, T, P, wrow, rows_live, wide_live, m);
       win = 0;
       rows_live = true;
+      wide_live = false;
+    }
+    if (big && !wide_init) {
+      for (uint32_t k = tid; k < C; k += NT) wrow[k] = 0;
+      wide_init = true;
       __syncthreads();
     }
     // the tile's queries, one warp each; meanwhile the query warp waits for the next
@@ -459,7 +494,7 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
           hi = r[2];
           pos = tile_pos(tile, n, r[0]);
         }
-        const int64_t a = answer_one(p, H, T, T64, row, rows_live, big != 0, tile, pos, lo, hi, lane);
+        const int64_t a = answer_one(p, H, T, P, rows_live, big != 0, tile, pos, lo, hi, lane);
         if (lane == 0) p.ans[i] = a;
       }
       __syncthreads();
@@ -474,22 +509,20 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
       if (idx < n) {
         const uint4 e = cur[k];
         const uint32_t prev = lane ? up : (idx ? tile[idx - 1].x : m->prev_state[t & 1]);
-        if (e.x < prev) set_status(p.status, BW_STATUS_EVENTS_UNSORTED);
-        if (e.x >= (uint32_t)p.S) set_status(p.status, BW_STATUS_STATE_RANGE);
+        bad |= (e.x < prev ? 1u : 0u) | (e.x >= (uint32_t)p.S ? 2u : 0u);
         if (e.y >= C) {
-          set_status(p.status, BW_STATUS_EVENT_KEY_RANGE);
+          bad |= 4u;
         } else if (!big) {
           const int32_t d = (int32_t)e.z;
           atomicAdd(&H[e.y], d);
-          atomicAdd(&T[(e.y >> p.chs) * 32 + lane], d);
+          if (p.nch) atomicAdd(&T[e.y >> kChunkShift], d);
           wsum += (uint32_t)(d < 0 ? -d : d);
         } else {
-          const uint64_t d = ((uint64_t)e.w << 32) | e.z;
-          atomicAdd(reinterpret_cast<unsigned long long*>(row + e.y), (unsigned long long)d);
-          shared_add_u64(&T64[e.y >> p.chs], d);
+          atomicAdd(reinterpret_cast<unsigned long long*>(wrow + e.y), ((unsigned long long)e.w << 32) | e.z);
         }
       }
     }
+    wide_live |= big != 0;
     {
       const uint32_t ws = __reduce_add_sync(0xffffffffu, wsum);
       if (lane == 0) m->wsum[t & 1][warp] = ws;
@@ -518,6 +551,9 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
     aborted = tile_barrier(bigp, lost, big);
   }
 
+  if (bad)
+    set_status(p.status, (bad & 1u) ? BW_STATUS_EVENTS_UNSORTED
+                                    : (bad & 2u) ? BW_STATUS_STATE_RANGE : BW_STATUS_EVENT_KEY_RANGE);
   // the query warp's last window copy lands before its shared memory goes away
   if (warp == QW) asm volatile("cp.async.wait_all;" ::: "memory");
   if (aborted) {
@@ -528,24 +564,18 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
     __syncthreads();
     return;
   }
-  // last block: the queries after its last event see every event of the chain
+  // final fold: the block's whole key histogram as a key prefix row
+  if (warp == QW && lane == 0) m->tail_q0 = qcur;
+  fold<NT>(p, H, T, P, wrow, rows_live, wide_live, m);
+  // last block: the queries after its last event see every event of the chain,
+  // all of it now in the prefix row
   if (b == p.B - 1) {
-    const int64_t qend = p.Q;
-    if (warp == QW && lane == 0) m->tail_q0 = qcur;
-    __syncthreads();
-    const int64_t from = m->tail_q0;
-    for (int64_t i = from + warp; i < qend; i += NW) {
+    for (int64_t i = m->tail_q0 + tid; i < p.Q; i += NT) {
       const uint32_t* r = reinterpret_cast<const uint32_t*>(p.qs + i);
-      const int64_t a = answer_one(p, H, T, T64, row, rows_live, false, nullptr, 0, r[1], r[2], lane);
-      if (lane == 0) p.ans[i] = a;
+      const uint32_t lo = min(r[1], C), hi = min(r[2], C);
+      p.ans[i] = lo < hi ? (int64_t)((uint64_t)__ldcg(P + hi) - (uint64_t)__ldcg(P + lo)) : 0;
     }
-    if (warp == QW) qcur = qend;
-    __syncthreads();   // every probe has read the window and the row before the flush folds one into the other
-  }
-  // final flush: the block's whole key histogram into its row
-  for (uint32_t k = tid; k < C; k += NT) {
-    const int32_t v = H[k];
-    row[k] = rows_live ? (int64_t)((uint64_t)__ldcg(row + k) + (uint64_t)(int64_t)v) : (int64_t)v;
+    if (warp == QW) qcur = p.Q;
   }
   if (warp == QW && lane == 0) {
     p.btab[2 * b] = qstart;
@@ -553,20 +583,21 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
   }
 }
 
-// Segment sums of the block rows, column by column.
+// Segment sums of the block prefix rows, column by column (column 0 is always 0).
 __global__ void k_chain_colsum(ChainParams p) {
-  const uint32_t k = blockIdx.y * 256 + threadIdx.x;
-  if (k >= p.C) return;
+  const uint32_t k = blockIdx.y * 256 + threadIdx.x + 1;
+  if (k > p.C) return;
   const int b0 = blockIdx.x * kChainSegRows, b1 = min(p.B, b0 + kChainSegRows);
   uint64_t s = 0;
   for (int b = b0; b < b1; ++b) s += (uint64_t)p.rows[(int64_t)b * (p.C + 1) + k];
   p.seg[(int64_t)blockIdx.x * (p.C + 1) + k] = (int64_t)s;
 }
 
-// Rows become exclusive column prefixes: the carry of each block.
+// Rows become exclusive column prefixes: row b = the key prefix of the carry of
+// blocks 0 .. b-1.
 __global__ void k_chain_colfix(ChainParams p) {
-  const uint32_t k = blockIdx.y * 256 + threadIdx.x;
-  if (k >= p.C) return;
+  const uint32_t k = blockIdx.y * 256 + threadIdx.x + 1;
+  if (k > p.C) return;
   uint64_t run = 0;
   for (int s = 0; s < (int)blockIdx.x; ++s) run += (uint64_t)p.seg[(int64_t)s * (p.C + 1) + k];
   const int b0 = blockIdx.x * kChainSegRows, b1 = min(p.B, b0 + kChainSegRows);
@@ -578,23 +609,10 @@ __global__ void k_chain_colfix(ChainParams p) {
   }
 }
 
-// Block b >= 1: its carry row scanned over keys (row[k] = carry below key k), then
-// every query of the block adds the carry inside [lo, hi).
+// Block b >= 1: every query of the block adds the carry inside [lo, hi).
 __global__ void __launch_bounds__(kChainThreads) k_chain_fixup(ChainParams p) {
   const int b = blockIdx.x + 1;
-  int64_t* row = p.rows + (int64_t)b * (p.C + 1);
-  const uint32_t n = p.C + 1;
-  const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
-  const uint32_t lo0 = threadIdx.x * per, hi0 = min(n, lo0 + per);
-  uint64_t local = 0;
-  for (uint32_t i = lo0; i < hi0; ++i) local += i < p.C ? (uint64_t)row[i] : 0;
-  uint64_t run = block_exclusive_scan<uint64_t>(local);
-  for (uint32_t i = lo0; i < hi0; ++i) {
-    const uint64_t v = i < p.C ? (uint64_t)row[i] : 0;
-    row[i] = (int64_t)run;
-    run += v;
-  }
-  __syncthreads();
+  const int64_t* row = p.rows + (int64_t)b * (p.C + 1);
   const int64_t q0 = p.btab[2 * b], q1 = p.btab[2 * b + 1];
   for (int64_t i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
     const BwQuery q = p.qs[i];
@@ -607,16 +625,18 @@ __global__ void __launch_bounds__(kChainThreads) k_chain_fixup(ChainParams p) {
 // compiled for.  Smaller CTAs give more state blocks and shorter per-tile
 // barriers; larger ones amortise the query warp over more appliers.
 struct Geometry {
-  int threads, ept, minb;
+  int threads, ept, minb, stages;
 };
-constexpr Geometry kGeometries[] = {{128, 4, 5}, {256, 4, 3}, {512, 2, 2}};
-constexpr int kNumGeometries = 3;
+constexpr Geometry kGeometries[] = {{128, 4, 5, 3}, {256, 4, 3, 3}, {512, 2, 2, 3},
+                                     {256, 4, 4, 2}, {256, 2, 4, 4}, {512, 2, 2, 2}};
+constexpr int kNumGeometries = 6;
 
 // BW_CHAIN_GEOMETRY=<index into kGeometries> pins the geometry (tuning runs).
-// Otherwise: 256 threads x 4 events when at least two such CTAs fit an SM and the
-// events fill every one of them with full state blocks (measured fastest on
-// byte-dominated chains); else the geometry with the most resident threads per SM
-// (few, short state blocks: wide CTAs finish each sooner).
+// Otherwise: 256 threads x 4 events with a two-tile ring when at least three such
+// CTAs fit an SM, else with a three-tile ring when two fit, provided the events
+// fill every CTA with full state blocks (measured fastest on byte-dominated
+// chains); else the geometry with the most resident threads per SM (few, short
+// state blocks: wide CTAs finish each sooner).
 int geometry_override() {
   static const int g = [] {
     const char* v = std::getenv("BW_CHAIN_GEOMETRY");
@@ -644,20 +664,18 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
   s.C = a->n_keys;
   s.E = a->n_events;
   s.Q = a->n_queries;
-  int lg = 0;
-  while ((1u << lg) < s.C) ++lg;
-  s.chs = lg - 5 > 5 ? lg - 5 : 5;
-  s.nch = (int32_t)((s.C + (1u << s.chs) - 1) >> s.chs);
+  s.nch = s.C > kFlatKeys ? (int32_t)((s.C + 31) >> 5) : 0;
   int pin = geometry_override();
   int fit[kNumGeometries];
   size_t need[kNumGeometries];
   for (int g = 0; g < kNumGeometries; ++g) {
     const Geometry& G = kGeometries[g];
-    need[g] = sweep_smem(s.C, s.nch, G.threads * G.ept).bytes;
+    need[g] = sweep_smem(s.C, s.nch, G.threads * G.ept, G.stages).bytes;
     fit[g] = (int)(kSmemPerSM / (need[g] + 1024));
     if (fit[g] > G.minb) fit[g] = G.minb;
   }
   if (pin >= 0 && fit[pin] < 1) pin = -1;
+  if (pin < 0 && fit[3] >= 3 && s.E >= (int64_t)sms * fit[3] * kChainMinBlockEvents) pin = 3;
   if (pin < 0 && fit[1] >= 2 && s.E >= (int64_t)sms * fit[1] * kChainMinBlockEvents) pin = 1;
   int best = -1, best_threads = 0;
   for (int g = 0; g < kNumGeometries; ++g) {
@@ -670,6 +688,7 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
       best_threads = ctas * G.threads;
       s.threads = G.threads;
       s.ept = G.ept;
+      s.geometry = g;
       s.smem = smem;
       s.ctas_per_sm = ctas;
     }
@@ -687,6 +706,7 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
   size_t o = 256;   // status word
   s.off_btab = o;  o = al(o + (size_t)s.B * 16);
   s.off_rows = o;  o = al(o + (size_t)s.B * (s.C + 1) * 8);
+  s.off_wide = o;  o = al(o + (size_t)s.B * s.C * 8);
   s.off_seg = o;   o = al(o + (size_t)s.nseg * (s.C + 1) * 8);
   s.total = o;
   return 0;
@@ -695,9 +715,12 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
 int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int* kernels) {
   std::call_once(g_attr_once, [] {
     const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    g_attr_err = cudaFuncSetAttribute(k_chain_sweep<128, 4, 5>, A, kSmemLimit);
-    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 4, 3>, A, kSmemLimit);
-    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<512, 2, 2>, A, kSmemLimit);
+    g_attr_err = cudaFuncSetAttribute(k_chain_sweep<128, 4, 5, 3>, A, kSmemLimit);
+    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 4, 3, 3>, A, kSmemLimit);
+    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<512, 2, 2, 3>, A, kSmemLimit);
+    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 4, 4, 2>, A, kSmemLimit);
+    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 2, 4, 4>, A, kSmemLimit);
+    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<512, 2, 2, 2>, A, kSmemLimit);
   });
   if (g_attr_err != cudaSuccess) return report(g_attr_err, "chain sweep attribute");
   cudaStream_t st = static_cast<cudaStream_t>(a->stream);
@@ -712,10 +735,10 @@ int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int*
   p.S = s.S;
   p.C = s.C;
   p.B = s.B;
-  p.chs = s.chs;
   p.nch = s.nch;
   p.nseg = s.nseg;
   p.rows = reinterpret_cast<int64_t*>(ws + s.off_rows);
+  p.wide = reinterpret_cast<int64_t*>(ws + s.off_wide);
   p.btab = reinterpret_cast<int64_t*>(ws + s.off_btab);
   p.seg = reinterpret_cast<int64_t*>(ws + s.off_seg);
   p.status = reinterpret_cast<int32_t*>(ws);
@@ -725,14 +748,19 @@ int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int*
     for (int i = 0; i <= BW_STAGE_SWEEP; ++i)
       if ((rc = report(cudaEventRecord(evs->ev[i], st), "event record"))) return rc;
   }
-  if (s.threads == 128) k_chain_sweep<128, 4, 5><<<s.B, 128, s.smem, st>>>(p);
-  else if (s.threads == 256) k_chain_sweep<256, 4, 3><<<s.B, 256, s.smem, st>>>(p);
-  else k_chain_sweep<512, 2, 2><<<s.B, 512, s.smem, st>>>(p);
+  switch (s.geometry) {
+    case 0: k_chain_sweep<128, 4, 5, 3><<<s.B, 128, s.smem, st>>>(p); break;
+    case 1: k_chain_sweep<256, 4, 3, 3><<<s.B, 256, s.smem, st>>>(p); break;
+    case 2: k_chain_sweep<512, 2, 2, 3><<<s.B, 512, s.smem, st>>>(p); break;
+    case 3: k_chain_sweep<256, 4, 4, 2><<<s.B, 256, s.smem, st>>>(p); break;
+    case 4: k_chain_sweep<256, 2, 4, 4><<<s.B, 256, s.smem, st>>>(p); break;
+    default: k_chain_sweep<512, 2, 2, 2><<<s.B, 512, s.smem, st>>>(p); break;
+  }
   int k = 1;
   if ((rc = report(cudaGetLastError(), "chain sweep launch"))) return rc;
   if (evs && (rc = report(cudaEventRecord(evs->ev[BW_STAGE_SWEEP + 1], st), "event record"))) return rc;
   if (s.B > 1) {
-    const dim3 g((unsigned)s.nseg, (s.C + 255) / 256);
+    const dim3 g((unsigned)s.nseg, (s.C + 255) / 256);   // columns 1 .. C
     k_chain_colsum<<<g, 256, 0, st>>>(p);
     k_chain_colfix<<<g, 256, 0, st>>>(p);
     k_chain_fixup<<<s.B - 1, kChainThreads, 0, st>>>(p);

@@ -21,7 +21,6 @@ namespace bw {
 
 constexpr int kChainThreads = 512;                              // largest sweep CTA (and the fix-up CTA)
 constexpr int kChainTile = 1024;                                // largest tile, events (16 KiB)
-constexpr int kChainStages = 3;                                 // tiles in the shared-memory ring
 constexpr int kChainQBuf = 128;                                 // query records staged per tile
 constexpr uint32_t kChainMaxKeys = 32768;                       // key domain held in shared memory
 constexpr int kChainSegRows = 16;                               // block rows per column-scan segment
@@ -32,14 +31,14 @@ struct ChainSpec {
   uint32_t C = 0;
   int64_t E = 0, Q = 0;
   int32_t B = 1;          // state blocks (= sweep CTAs)
-  int32_t chs = 5;        // log2 of the chunk width of the chunk totals
-  int32_t nch = 1;        // chunks
+  int32_t nch = 1;        // 32-key chunks of the window's chunk totals
   int32_t nseg = 1;       // column-scan segments
   int32_t ctas_per_sm = 1;
-  int32_t threads = 512;  // sweep geometry: threads per CTA, events per thread
+  int32_t geometry = 2;   // sweep geometry: index, threads per CTA, events per thread
+  int32_t threads = 512;
   int32_t ept = 2;
   size_t smem = 0;        // dynamic shared memory of the sweep
-  size_t off_btab = 0, off_rows = 0, off_seg = 0, total = 0;   // workspace layout
+  size_t off_btab = 0, off_rows = 0, off_wide = 0, off_seg = 0, total = 0;   // workspace layout
 };
 
 // Whether a replay takes the chain path: the caller asserts a chain
