@@ -1,32 +1,31 @@
 // bw_chain.cu -- single-pass replay of a linear version chain (see bw_chain.cuh).
 //
-// Sweep (k_chain_sweep, one CTA per state block; 128, 256 or 512 threads with
-// tiles of 512-1024 events, picked per key domain by occupancy):
-//   * the block's events [e0, e1) stream through a ring of kChainStages tiles,
-//     each tile one cp.async.bulk copy from global memory into shared memory
-//     completed on the stage's mbarrier (bounded waits);
-//   * the running key histogram of the block lives in shared memory as exact
-//     int32 window accumulators H[key] plus lane-replicated chunk totals T[chunk]
-//     (each lane of a warp adds into its own copy, so chunk updates never collide).
-//     A window holds events whose absolute sum stays below 2^28 + 2^29, so every
-//     partial sum of it is exact in int32; before it can grow past that it is
-//     flushed into the block's int64 row in global memory (plus int64 chunk
-//     totals in shared memory).  Tiles holding a delta outside (-2^19, 2^19)
-//     bypass the window: they add straight into the int64 row with 64-bit global
-//     atomics;
+// Sweep (k_chain_sweep, one CTA per state block; 128-512 threads, tiles of 512-1024
+// events, a ring of 2-3 tiles, the geometry picked per workload by occupancy):
+//   * the block's events [e0, e1) stream through the ring, each tile one
+//     cp.async.bulk copy from global memory into shared memory completed on the
+//     stage's mbarrier (bounded waits);
+//   * the running key histogram of the block is an exact int32 window H[key] in
+//     shared memory (plus int32 totals of 32-key chunks when the key domain is
+//     larger than 4,096 keys).  A window holds events whose absolute sum stays
+//     below 2^28 + 2^29, so every partial sum of it is exact in int32; before it
+//     can grow past that it is folded into the block's key prefix row in global
+//     memory (P[k] = sum of the folded events below key k, int64).  Tiles holding a
+//     delta outside (-2^19, 2^19) bypass the window: their events go to a per-block
+//     int64 key histogram with global atomics, folded into P before the next tile;
 //   * a tile owns the queries whose position (number of events at or before their
 //     state) falls inside it: state < state of the tile's last event.  Their local
-//     answer = the window + row probe over [lo, hi) before the tile is applied,
+//     answer = P[hi] - P[lo] + the window over [lo, hi) before the tile is applied,
 //     plus the tile's first `pos` events inside [lo, hi); one warp per query,
 //     int32 lane sums reduced with redux.sync;
 //   * one warp (the last) finds the next tile's queries and their positions while
 //     the others answer the current tile's: the query records come through a
 //     32-record window that cp.async fills one tile ahead, and land in a
 //     double-buffered shared query buffer.
-// Carry (k_chain_colsum, k_chain_colfix): exclusive column scan over the block
-// rows in two passes (segment sums, then segment-local prefixes), in place.
-// Fix-up (k_chain_fixup): each block's carry row is scanned over keys in place and
-// every query of the block adds row[hi] - row[lo].
+// Carry (k_chain_colsum, k_chain_colfix): exclusive column scan over the blocks'
+// final prefix rows in two passes (segment sums, then segment-local prefixes), in
+// place: row b becomes the key prefix of the events of blocks 0 .. b-1.
+// Fix-up (k_chain_fixup): every query of block b >= 1 adds row[hi] - row[lo].
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -627,16 +626,17 @@ __global__ void __launch_bounds__(kChainThreads) k_chain_fixup(ChainParams p) {
 struct Geometry {
   int threads, ept, minb, stages;
 };
-constexpr Geometry kGeometries[] = {{128, 4, 5, 3}, {256, 4, 3, 3}, {512, 2, 2, 3},
-                                     {256, 4, 4, 2}, {256, 2, 4, 4}, {512, 2, 2, 2}};
-constexpr int kNumGeometries = 6;
+constexpr Geometry kGeometries[] = {{128, 4, 5, 3}, {256, 4, 3, 3}, {512, 2, 2, 3}, {256, 4, 4, 2},
+                                     {256, 2, 4, 4}, {512, 2, 2, 2}, {256, 3, 4, 3}};
+constexpr int kNumGeometries = 7;
 
 // BW_CHAIN_GEOMETRY=<index into kGeometries> pins the geometry (tuning runs).
-// Otherwise: 256 threads x 4 events with a two-tile ring when at least three such
-// CTAs fit an SM, else with a three-tile ring when two fit, provided the events
-// fill every CTA with full state blocks (measured fastest on byte-dominated
-// chains); else the geometry with the most resident threads per SM (few, short
-// state blocks: wide CTAs finish each sooner).
+// Otherwise, when the events fill every CTA with full state blocks, 256 threads
+// with (in this order of preference, measured on byte-dominated chains) 3 events
+// each and a three-tile ring at four CTAs per SM, 4 events and a two-tile ring at
+// three or more, 4 events and a three-tile ring at two or more; else the geometry
+// with the most resident threads per SM (few, short state blocks: wide CTAs finish
+// each sooner).
 int geometry_override() {
   static const int g = [] {
     const char* v = std::getenv("BW_CHAIN_GEOMETRY");
@@ -675,6 +675,7 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
     if (fit[g] > G.minb) fit[g] = G.minb;
   }
   if (pin >= 0 && fit[pin] < 1) pin = -1;
+  if (pin < 0 && fit[6] >= 4 && s.E >= (int64_t)sms * fit[6] * kChainMinBlockEvents) pin = 6;
   if (pin < 0 && fit[3] >= 3 && s.E >= (int64_t)sms * fit[3] * kChainMinBlockEvents) pin = 3;
   if (pin < 0 && fit[1] >= 2 && s.E >= (int64_t)sms * fit[1] * kChainMinBlockEvents) pin = 1;
   int best = -1, best_threads = 0;
@@ -721,6 +722,7 @@ int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int*
     if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 4, 4, 2>, A, kSmemLimit);
     if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 2, 4, 4>, A, kSmemLimit);
     if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<512, 2, 2, 2>, A, kSmemLimit);
+    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 3, 4, 3>, A, kSmemLimit);
   });
   if (g_attr_err != cudaSuccess) return report(g_attr_err, "chain sweep attribute");
   cudaStream_t st = static_cast<cudaStream_t>(a->stream);
@@ -754,7 +756,8 @@ int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int*
     case 2: k_chain_sweep<512, 2, 2, 3><<<s.B, 512, s.smem, st>>>(p); break;
     case 3: k_chain_sweep<256, 4, 4, 2><<<s.B, 256, s.smem, st>>>(p); break;
     case 4: k_chain_sweep<256, 2, 4, 4><<<s.B, 256, s.smem, st>>>(p); break;
-    default: k_chain_sweep<512, 2, 2, 2><<<s.B, 512, s.smem, st>>>(p); break;
+    case 5: k_chain_sweep<512, 2, 2, 2><<<s.B, 512, s.smem, st>>>(p); break;
+    default: k_chain_sweep<256, 3, 4, 3><<<s.B, 256, s.smem, st>>>(p); break;
   }
   int k = 1;
   if ((rc = report(cudaGetLastError(), "chain sweep launch"))) return rc;

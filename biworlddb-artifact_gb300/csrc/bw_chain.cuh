@@ -21,7 +21,7 @@ namespace bw {
 
 constexpr int kChainThreads = 512;                              // largest sweep CTA (and the fix-up CTA)
 constexpr int kChainTile = 1024;                                // largest tile, events (16 KiB)
-constexpr int kChainQBuf = 128;                                 // query records staged per tile
+constexpr int kChainQBuf = 64;                                  // query records staged per tile
 constexpr uint32_t kChainMaxKeys = 32768;                       // key domain held in shared memory
 constexpr int kChainSegRows = 16;                               // block rows per column-scan segment
 constexpr int64_t kChainMinBlockEvents = 8192;
