@@ -97,7 +97,8 @@ GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch", "gpu
                "bw_forest_destroy", "bw_forest_autotune_workspace", "bw_forest_autotune",
                "bw_forest_launch_timed",
                "bw_serve_create", "bw_serve_reset", "bw_serve_run", "bw_serve_info", "bw_serve_destroy",
-               "bw_forest_plan_stats", "bw_key_histogram", "bw_key_prefix", "bw_add_range_carry"]
+               "bw_forest_plan_stats", "bw_key_histogram", "bw_key_prefix", "bw_add_range_carry",
+               "bw_scatter_answers"]
 
 _gpu = None
 
@@ -579,7 +580,9 @@ class BwNativeWorkload(C.Structure):
 
 HOST_SYMBOLS = ["bw_fixture_open", "bw_fixture_from_memory", "bw_fixture_close", "bw_fixture_rows",
                 "bw_native_build", "bw_native_free", "bw_native_build_declared", "bw_v7_plan_build",
-                "bw_v7_plan_build_declared", "bw_v7_plan_free", "bw_sha256_hex", "bw_fnv1a"]
+                "bw_v7_plan_build_declared", "bw_v7_plan_free", "bw_sha256_hex", "bw_fnv1a",
+                "bw_sha256_init", "bw_sha256_update", "bw_sha256_final", "bw_fnv1a_update",
+                "bw_stream_build", "bw_stream_free"]
 
 _host = None
 
@@ -602,6 +605,11 @@ def host_lib(build_if_missing: bool = True):
         L.bw_sha256_hex.argtypes = [C.c_void_p, C.c_size_t, C.c_char_p]
         L.bw_fnv1a.argtypes = [C.c_void_p, C.c_size_t]
         L.bw_fnv1a.restype = C.c_uint64
+        L.bw_sha256_init.argtypes = [C.c_void_p]
+        L.bw_sha256_update.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+        L.bw_sha256_final.argtypes = [C.c_void_p, C.c_char_p]
+        L.bw_fnv1a_update.argtypes = [C.c_uint64, C.c_void_p, C.c_size_t]
+        L.bw_fnv1a_update.restype = C.c_uint64
         _host = L
     return _host
 
@@ -618,6 +626,30 @@ def fnv1a(buf) -> int:
     import numpy as np
     a = np.ascontiguousarray(np.frombuffer(memoryview(buf).cast("B"), dtype=np.uint8))
     return int(host_lib().bw_fnv1a(a.ctypes.data if a.size else None, a.size))
+
+
+class Digest:
+    """Streaming SHA-256 + FNV-1a over bytes fed in pieces (bw_sha256_update,
+    bw_fnv1a_update): the worker's extract digests each downloaded chunk this way."""
+
+    FNV_BASIS = 1469598103934665603
+
+    def __init__(self):
+        self._state = C.create_string_buffer(8 * 4 + 8 + 64 + 8)   # BwSha256, padded
+        host_lib().bw_sha256_init(self._state)
+        self._fnv = self.FNV_BASIS
+
+    def update(self, buf) -> None:
+        import numpy as np
+        a = np.ascontiguousarray(np.frombuffer(memoryview(buf).cast("B"), dtype=np.uint8))
+        ptr = a.ctypes.data if a.size else None
+        host_lib().bw_sha256_update(self._state, ptr, a.size)
+        self._fnv = int(host_lib().bw_fnv1a_update(self._fnv, ptr, a.size))
+
+    def final(self):
+        out = C.create_string_buffer(65)
+        host_lib().bw_sha256_final(self._state, out)
+        return out.value.decode(), self._fnv
 
 
 class BwDeclared(C.Structure):
@@ -706,6 +738,50 @@ def native_workload_declared(fixture: bytes, decl, name: str = "declared") -> "w
         chain = bool(np.all(par[1:] == np.arange(par.size - 1)))
         return _native_result(L, out, name, chain)
     return _with_fixture(fixture, run)
+
+
+class BwStreamWorkload(C.Structure):
+    _fields_ = [("chain", BwNativeWorkload), ("slot", C.c_void_p), ("n_answers", C.c_int64), ("q", C.c_int32)]
+
+
+def stream_workload(fixture: bytes, stream: bytes, name: str = "stream"):
+    """The reference's BWLEV001 event stream (emit_events.cpp) over a BWBASE02 fixture,
+    compiled into a linear-chain event workload (bw_stream_build).  Returns
+    (workload, slot, n_answers): answers of the chain queries, scattered by ``slot``
+    (-1: not in the answer vector), give the reference's answer vector."""
+    import numpy as np
+
+    def run(L, fx):
+        L.bw_stream_build.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t, C.POINTER(C.POINTER(BwStreamWorkload))]
+        L.bw_stream_free.argtypes = [C.POINTER(BwStreamWorkload)]
+        out = C.POINTER(BwStreamWorkload)()
+        rc = L.bw_stream_build(fx, stream, len(stream), C.byref(out))
+        if rc:
+            raise ValueError(f"event stream rejected (rc={rc})")
+        try:
+            o = out.contents
+            w = o.chain
+            S, E, Q = w.n_states, w.n_events, w.n_queries
+            parent = np.ctypeslib.as_array(C.cast(w.parent, C.POINTER(C.c_int32)), (S,)).copy()
+            ev = np.frombuffer(C.string_at(w.events, 16 * E), dtype=workloads.EVENT_DTYPE).copy() \
+                if E else np.empty(0, dtype=workloads.EVENT_DTYPE)
+            qs = np.frombuffer(C.string_at(w.queries, 12 * Q), dtype=workloads.QUERY_DTYPE).copy() \
+                if Q else np.empty(0, dtype=workloads.QUERY_DTYPE)
+            slot = np.frombuffer(C.string_at(o.slot, 8 * Q), dtype=np.int64).copy() if Q else \
+                np.empty(0, dtype=np.int64)
+            return workloads.Workload(name, parent, int(w.n_keys), ev, qs, True), slot, int(o.n_answers)
+        finally:
+            L.bw_stream_free(out)
+    return _with_fixture(fixture, run)
+
+
+def scatter_answers(chain_answers, slot, n_answers):
+    """The answer vector from a stream workload's chain answers (stream order)."""
+    import numpy as np
+    out = np.zeros(n_answers, dtype=np.int64)
+    keep = slot >= 0
+    out[slot[keep]] = np.asarray(chain_answers)[keep]
+    return out
 
 
 class BwV7Plan(C.Structure):

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <unordered_map>
 #include <vector>
 
 struct BwFixture {
@@ -456,6 +457,182 @@ extern "C" void bw_native_free(BwNativeWorkload* w) {
   delete w;
 }
 
+// ------------------------------------------------------------------ BWLEV001 stream
+// The reference's sequential event stream (emit_events.cpp:5-8, 21-27, 62-66): the
+// header "BWLEV001" + u64 record count, then 36-byte little-endian records
+//   kind u32, state u32, qidx u32, g i32, w i32, a i64, b i64
+// kind 0 row delta (a = t, b = amount, g = group, w = +1 insert / -1 retract),
+// kind 1 factor set (g, a = the group's new factor), kind 2 query (state v, bag
+// index k, interval [a, b)).  Its consumers start from the fixture's base rows and
+// answer each query from the rows live at that point of the stream: the sum over
+// groups of factor x the amounts with t in [lo, hi); the answer vector is ordered
+// by (state, k) without state 0 (external/dd_probe/src/main.rs:66-80, 245-262).
+//
+// As an event-model chain: chain state i is the stream before its i-th query
+// (records after query i-1 get state i; query i sits at state i).  Keys are
+// endpoint classes over the distinct query bounds (class(t) = bounds <= t), so
+// t in [lo, hi) is the key range [class(lo), class(hi)).  A row delta is the event
+// (class(t), w * amount * factor(g)); a factor change of group g from m to m' is one
+// event (class, (m' - m) * L) per class of the group's live mass L.  Base rows are
+// state-0 events.  An interval with hi <= lo answers 0.
+namespace {
+struct StreamRec {
+  uint32_t kind, state, qidx;
+  int32_t g, w;
+  int64_t a, b;
+};
+inline StreamRec stream_rec(const uint8_t* p) {
+  StreamRec r;
+  std::memcpy(&r.kind, p, 4);
+  std::memcpy(&r.state, p + 4, 4);
+  std::memcpy(&r.qidx, p + 8, 4);
+  std::memcpy(&r.g, p + 12, 4);
+  std::memcpy(&r.w, p + 16, 4);
+  std::memcpy(&r.a, p + 20, 8);
+  std::memcpy(&r.b, p + 28, 8);
+  return r;
+}
+}  // namespace
+
+extern "C" int bw_stream_build(const BwFixture* fx, const void* data, size_t bytes, BwStreamWorkload** out) {
+  if (!fx || !out || (!data && bytes)) return 2;
+  *out = nullptr;
+  const uint8_t* p = static_cast<const uint8_t*>(data);
+  if (bytes < 16 || std::memcmp(p, "BWLEV001", 8) != 0) return 3;
+  uint64_t n = 0;
+  std::memcpy(&n, p + 8, 8);
+  if (n > (bytes - 16) / 36 || 16 + 36 * n != bytes) return 3;
+  const uint8_t* rec = p + 16;
+  const int32_t G = fx->G;
+  // pass 1: validation, query bounds, answer shape
+  std::vector<int64_t> bounds;
+  int64_t nq = 0;
+  uint32_t max_state = 0, max_k = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const StreamRec r = stream_rec(rec + 36 * i);
+    if (r.kind == 2) {
+      bounds.push_back(r.a);
+      bounds.push_back(r.b);
+      ++nq;
+      max_state = std::max(max_state, r.state);
+      max_k = std::max(max_k, r.qidx);
+    } else if (r.kind == 0) {
+      if (r.g < 0 || r.g >= G || (r.w != 1 && r.w != -1)) return 3;
+    } else if (r.kind == 1) {
+      if (r.g < 0 || r.g >= G) return 3;
+    } else {
+      return 3;
+    }
+  }
+  if (nq >= ((int64_t)1 << 31) - 1 || max_k >= 4096) return 3;
+  std::sort(bounds.begin(), bounds.end());
+  bounds.erase(std::unique(bounds.begin(), bounds.end()), bounds.end());
+  if (bounds.size() >= ((size_t)1 << 32) - 1) return 3;
+  auto cls = [&](int64_t t) {
+    return (uint32_t)(std::upper_bound(bounds.begin(), bounds.end(), t) - bounds.begin());
+  };
+  const int32_t q = nq ? (int32_t)max_k + 1 : 0;
+  const int64_t n_answers = (int64_t)max_state * q;
+  std::vector<int64_t> slot((size_t)nq, -1);
+  std::vector<uint8_t> seen((size_t)n_answers, 0);
+
+  // pass 2: events and queries in stream order (states non-decreasing)
+  std::vector<BwEvent> ev;
+  std::vector<BwQuery> qs;
+  ev.reserve((size_t)fx->n + n);
+  qs.reserve((size_t)nq);
+  std::vector<int64_t> mul(G);
+  for (int32_t g = 0; g < G; ++g) mul[g] = fx->factor(g);
+  std::unordered_map<uint64_t, int64_t> live;     // (group, class) -> live amount
+  std::vector<std::vector<uint32_t>> gcls(G);      // classes each group has touched
+  auto add_live = [&](int32_t g, uint32_t c, int64_t amt) {
+    const uint64_t key = ((uint64_t)(uint32_t)g << 32) | c;
+    auto it = live.find(key);
+    if (it == live.end()) {
+      live.emplace(key, amt);
+      gcls[g].push_back(c);
+    } else {
+      it->second = (int64_t)((uint64_t)it->second + (uint64_t)amt);
+    }
+  };
+  auto wmul = [](int64_t x, int64_t y) { return (int64_t)((uint64_t)x * (uint64_t)y); };
+  for (int64_t i = 0; i < fx->n; ++i) {
+    const int32_t g = fx->row_g(i);
+    if (g < 0 || g >= G) return 3;
+    const uint32_t c = cls(fx->row_t(i));
+    add_live(g, c, fx->row_amt(i));
+    const int64_t d = wmul(fx->row_amt(i), mul[g]);
+    if (d) ev.push_back(BwEvent{0u, c, d});
+  }
+  uint32_t state = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    const StreamRec r = stream_rec(rec + 36 * i);
+    if (r.kind == 0) {
+      const uint32_t c = cls(r.a);
+      const int64_t amt = r.w > 0 ? r.b : (int64_t)(0 - (uint64_t)r.b);
+      add_live(r.g, c, amt);
+      const int64_t d = wmul(amt, mul[r.g]);
+      if (d) ev.push_back(BwEvent{state, c, d});
+    } else if (r.kind == 1) {
+      const int64_t dm = (int64_t)((uint64_t)r.a - (uint64_t)mul[r.g]);
+      if (dm) {
+        for (uint32_t c : gcls[r.g]) {
+          const int64_t L = live[((uint64_t)(uint32_t)r.g << 32) | c];
+          const int64_t d = wmul(dm, L);
+          if (d) ev.push_back(BwEvent{state, c, d});
+        }
+      }
+      mul[r.g] = r.a;
+    } else {
+      const uint32_t lo = cls(r.a), hi = cls(r.b);
+      qs.push_back(BwQuery{state, lo, hi < lo ? lo : hi});
+      if (r.state > 0) {
+        const int64_t s = (int64_t)(r.state - 1) * q + r.qidx;
+        if (seen[(size_t)s]) return 3;   // a (state, k) answered twice
+        seen[(size_t)s] = 1;
+        slot[qs.size() - 1] = s;
+      }
+      ++state;
+    }
+  }
+  for (uint8_t x : seen)
+    if (!x) return 3;   // the answer vector would have a hole
+
+  BwStreamWorkload* o = new (std::nothrow) BwStreamWorkload();
+  if (!o) return 2;
+  BwNativeWorkload& w = o->chain;
+  w.n_states = (int32_t)state + 1;
+  w.n_keys = (uint32_t)bounds.size() + 1;
+  w.n_events = (int64_t)ev.size();
+  w.n_queries = (int64_t)qs.size();
+  w.n_factor_events = 0;
+  w.parent = new (std::nothrow) int32_t[(size_t)w.n_states];
+  w.events = new (std::nothrow) BwEvent[ev.size() ? ev.size() : 1];
+  w.queries = new (std::nothrow) BwQuery[qs.size() ? qs.size() : 1];
+  o->slot = new (std::nothrow) int64_t[slot.size() ? slot.size() : 1];
+  if (!w.parent || !w.events || !w.queries || !o->slot) {
+    bw_stream_free(o);
+    return 2;
+  }
+  for (int32_t v = 0; v < w.n_states; ++v) w.parent[v] = v - 1;
+  std::memcpy(w.events, ev.data(), ev.size() * sizeof(BwEvent));
+  std::memcpy(w.queries, qs.data(), qs.size() * sizeof(BwQuery));
+  std::memcpy(o->slot, slot.data(), slot.size() * 8);
+  o->n_answers = n_answers;
+  o->q = q;
+  *out = o;
+  return 0;
+}
+
+extern "C" void bw_stream_free(BwStreamWorkload* w) {
+  if (!w) return;
+  delete[] w->chain.parent;
+  delete[] w->chain.events;
+  delete[] w->chain.queries;
+  delete[] w->slot;
+  delete w;
+}
+
 // ------------------------------------------------------------------ digests
 namespace {
 // FIPS 180-4 SHA-256; round constants and initial hash derived from the cube and
@@ -507,35 +684,63 @@ void sha_compress(uint32_t h[8], const uint8_t* p, const uint32_t* K) {
 }
 }  // namespace
 
-extern "C" void bw_sha256_hex(const void* data, size_t n, char out_hex[65]) {
-  const Sha256Consts& C = sha_consts();
-  uint32_t h[8];
-  std::memcpy(h, C.h0, sizeof(h));
+extern "C" void bw_sha256_init(BwSha256* s) {
+  std::memcpy(s->h, sha_consts().h0, sizeof(s->h));
+  s->bytes = 0;
+  s->fill = 0;
+}
+
+extern "C" void bw_sha256_update(BwSha256* s, const void* data, size_t n) {
+  const uint32_t* K = sha_consts().k;
   const uint8_t* p = static_cast<const uint8_t*>(data);
-  const size_t full = n / 64;
-  for (size_t i = 0; i < full; ++i) sha_compress(h, p + 64 * i, C.k);
+  s->bytes += n;
+  if (s->fill) {
+    const size_t take = std::min<size_t>(n, 64 - s->fill);
+    std::memcpy(s->buf + s->fill, p, take);
+    s->fill += (uint32_t)take;
+    p += take;
+    n -= take;
+    if (s->fill < 64) return;
+    sha_compress(s->h, s->buf, K);
+    s->fill = 0;
+  }
+  for (; n >= 64; p += 64, n -= 64) sha_compress(s->h, p, K);
+  if (n) std::memcpy(s->buf, p, n);
+  s->fill = (uint32_t)n;
+}
+
+extern "C" void bw_sha256_final(BwSha256* s, char out_hex[65]) {
+  const uint32_t* K = sha_consts().k;
   uint8_t tail[128] = {0};
-  const size_t rem = n - full * 64;
-  if (rem) std::memcpy(tail, p + full * 64, rem);
+  const size_t rem = s->fill;
+  std::memcpy(tail, s->buf, rem);
   tail[rem] = 0x80;
   const size_t tl = rem < 56 ? 64 : 128;
-  const uint64_t bits = (uint64_t)n * 8u;
+  const uint64_t bits = s->bytes * 8u;
   for (int i = 0; i < 8; ++i) tail[tl - 1 - i] = (uint8_t)(bits >> (8 * i));
-  sha_compress(h, tail, C.k);
-  if (tl == 128) sha_compress(h, tail + 64, C.k);
+  sha_compress(s->h, tail, K);
+  if (tl == 128) sha_compress(s->h, tail + 64, K);
   static const char* hx = "0123456789abcdef";
   for (int i = 0; i < 8; ++i)
-    for (int j = 0; j < 8; ++j) out_hex[8 * i + j] = hx[(h[i] >> (28 - 4 * j)) & 15];
+    for (int j = 0; j < 8; ++j) out_hex[8 * i + j] = hx[(s->h[i] >> (28 - 4 * j)) & 15];
   out_hex[64] = 0;
 }
 
+extern "C" void bw_sha256_hex(const void* data, size_t n, char out_hex[65]) {
+  BwSha256 s;
+  bw_sha256_init(&s);
+  bw_sha256_update(&s, data, n);
+  bw_sha256_final(&s, out_hex);
+}
+
 // FNV-1a with the reference's offset basis 1469598103934665603 (common.hpp:396-400).
-extern "C" uint64_t bw_fnv1a(const void* data, size_t n) {
+extern "C" uint64_t bw_fnv1a_update(uint64_t h, const void* data, size_t n) {
   const uint8_t* p = static_cast<const uint8_t*>(data);
-  uint64_t h = 1469598103934665603ULL;
   for (size_t i = 0; i < n; ++i) h = (h ^ p[i]) * 1099511628211ULL;
   return h;
 }
+
+extern "C" uint64_t bw_fnv1a(const void* data, size_t n) { return bw_fnv1a_update(BW_FNV1A_BASIS, data, n); }
 
 // ------------------------------------------------------------------ v7 chain plan
 // Host-side restatement of the reference's v7 setup for chains in the argument

@@ -70,6 +70,15 @@ __global__ void k_add_carry(const BwQuery* qs, int64_t n, uint32_t C, const int6
   }
 }
 
+// dst[slot[i]] = src[i] where 0 <= slot[i] < n_dst: answers of a stream workload's
+// chain queries (stream order) into the reference's answer order.
+__global__ void k_scatter(const int64_t* src, const int64_t* slot, int64_t n, int64_t* dst, int64_t n_dst) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = slot[i];
+    if (s >= 0 && s < n_dst) dst[s] = src[i];
+  }
+}
+
 int grid_for(int64_t n, int threads) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -117,4 +126,12 @@ extern "C" int bw_add_range_carry(const BwQuery* queries, int64_t n, uint32_t n_
   if (n == 0) return 0;
   k_add_carry<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(queries, n, n_keys, prefix, answers);
   return shard_report(cudaGetLastError(), "carry launch");
+}
+
+extern "C" int bw_scatter_answers(const int64_t* src, const int64_t* slot, int64_t n, int64_t* dst, int64_t n_dst,
+                                  void* stream) {
+  if (n < 0 || n_dst < 0 || (n && (!src || !slot || !dst))) return BW_EINVAL;
+  if (n == 0) return 0;
+  k_scatter<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(src, slot, n, dst, n_dst);
+  return shard_report(cudaGetLastError(), "scatter launch");
 }

@@ -4,7 +4,13 @@
 //
 //   bw_worker --fixture PATH --base-id ID --topology T --seed S --factor-period P
 //             --q Q --repeat R --answers A --json J [--arm gb300|gpu_v7]
-//             [--states N] [--blocks B]
+//             [--states N] [--blocks B] [--events STREAM]
+//
+// * --events takes the workload from a BWLEV001 event stream over the fixture (the
+//   reference's emit_events.cpp output) instead of the declared generator: the
+//   stream compiles into a linear-chain event workload (bw_stream_build), replays on
+//   the gb300 arm, and its answers go back to (state, k) order on the device
+//   (bw_scatter_answers); --topology/--seed/--factor-period/--q are then only echoed;
 //
 // * the range scope comes from BWH_RANGE_SCOPE ("per_state", anything else shared),
 //   the state count from --states, else BWH_STATES, else 2049 (the reference fixes it
@@ -24,12 +30,16 @@
 // gpu_combine_launch.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cinttypes>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
+#include <iterator>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "bw_gpu.h"
@@ -78,6 +88,17 @@ struct Timings {
   double algorithmic_bytes = 0;
 };
 
+// Answers an arm leaves on the device for the extract phase, and every device
+// buffer of the run (freed at cleanup).
+struct DeviceAnswers {
+  int64_t* d = nullptr;
+  size_t n = 0;
+  std::vector<void*> owned;
+  ~DeviceAnswers() {
+    for (void* b : owned) cudaFree(b);
+  }
+};
+
 template <typename T>
 int upload(T** dst, const T* src, size_t n) {
   CUDA_OR_5(cudaMalloc(reinterpret_cast<void**>(dst), (n ? n : 1) * sizeof(T)));
@@ -86,7 +107,7 @@ int upload(T** dst, const T* src, size_t n) {
 }
 
 // The event-model replay of a declared workload (any topology).
-int run_event_arm(const BwNativeWorkload* w, int32_t blocks, std::vector<int64_t>& answers, Timings& tm) {
+int run_event_arm(const BwNativeWorkload* w, int32_t blocks, DeviceAnswers& out, Timings& tm) {
   const auto u0 = clk::now();
   int32_t* d_parent = nullptr;
   BwEvent* d_ev = nullptr;
@@ -94,10 +115,14 @@ int run_event_arm(const BwNativeWorkload* w, int32_t blocks, std::vector<int64_t
   int64_t* d_ans = nullptr;
   void* ws = nullptr;
   int rc = upload(&d_parent, w->parent, (size_t)w->n_states);
+  out.owned.push_back(d_parent);
   if (!rc) rc = upload(&d_ev, w->events, (size_t)w->n_events);
+  out.owned.push_back(d_ev);
   if (!rc) rc = upload(&d_q, w->queries, (size_t)w->n_queries);
+  out.owned.push_back(d_q);
   if (rc) return rc;
   CUDA_OR_5(cudaMalloc(&d_ans, (size_t)(w->n_queries ? w->n_queries : 1) * 8));
+  out.owned.push_back(d_ans);
   bool chain = true;
   for (int32_t v = 1; v < w->n_states; ++v) chain = chain && w->parent[v] == v - 1;
   BwReplayArgs a{};
@@ -114,6 +139,7 @@ int run_event_arm(const BwNativeWorkload* w, int32_t blocks, std::vector<int64_t
   size_t need = 0;
   BW_OR_5(bw_replay_workspace_size(&a, &need), "bw_replay_workspace_size");
   CUDA_OR_5(cudaMalloc(&ws, need ? need : 256));
+  out.owned.push_back(ws);
   a.workspace = ws;
   a.workspace_bytes = need ? need : 256;
   CUDA_OR_5(cudaDeviceSynchronize());
@@ -133,31 +159,23 @@ int run_event_arm(const BwNativeWorkload* w, int32_t blocks, std::vector<int64_t
     std::fprintf(stderr, "the device rejected the workload (status %d)\n", st);
     return 3;
   }
-  const auto d0 = clk::now();
-  answers.assign((size_t)w->n_queries, 0);
-  if (w->n_queries) CUDA_OR_5(cudaMemcpy(answers.data(), d_ans, (size_t)w->n_queries * 8, cudaMemcpyDeviceToHost));
-  const auto d1 = clk::now();
+  out.d = d_ans;
+  out.n = (size_t)w->n_queries;
   int32_t kernels = 0, nb = 0;
   bw_replay_last_info(&a, &kernels, &nb);
   tm.upload = ns_between(u0, u1);
   tm.kernel = (int64_t)((double)ms * 1e6);
-  tm.download = ns_between(d0, d1);
   tm.blocks = nb;
   tm.kernels = kernels;
   tm.threads = 512;
   tm.algorithmic_bytes = 4.0 * w->n_states + 16.0 * (double)w->n_events + 20.0 * (double)w->n_queries;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  CUDA_OR_5(cudaFree(ws));
-  CUDA_OR_5(cudaFree(d_ans));
-  CUDA_OR_5(cudaFree(d_q));
-  CUDA_OR_5(cudaFree(d_ev));
-  CUDA_OR_5(cudaFree(d_parent));
   return 0;
 }
 
 // The gpu_v7.h drop-in path on the reference's v7 chain plan.
-int run_v7_arm(const BwV7Plan* p, std::vector<int64_t>& answers, Timings& tm) {
+int run_v7_arm(const BwV7Plan* p, DeviceAnswers& out, Timings& tm) {
   const int32_t B = p->B, G = p->G, Cp = p->Cpfx, S = p->n_states, q = p->q;
   const int32_t nms = p->ms_off[p->n_active];
   const auto u0 = clk::now();
@@ -181,12 +199,20 @@ int run_v7_arm(const BwV7Plan* p, std::vector<int64_t>& answers, Timings& tm) {
   if (!rc) rc = upload(&d_qhb, p->qhb, (size_t)S * q);
   if (!rc) rc = upload(&d_bidx, p->bidx, (size_t)S);
   if (!rc) rc = upload(&d_vbase, p->vbase, (size_t)Cp);
+  for (void* b : {(void*)d_nodes, (void*)d_v0, (void*)d_v1, (void*)d_fac, (void*)d_g2row, (void*)d_ms_off,
+                  (void*)d_ms_cls, (void*)d_ms_base, (void*)d_ms_dev, (void*)d_devbuf, (void*)d_need, (void*)d_qlb,
+                  (void*)d_qhb, (void*)d_bidx, (void*)d_vbase})
+    if (b) out.owned.push_back(b);
   if (rc) return rc;
   const size_t nans = (size_t)(S - 1) * q;
   CUDA_OR_5(cudaMalloc(&d_lvals, nans * 2 * 8));
+  out.owned.push_back(d_lvals);
   CUDA_OR_5(cudaMalloc(&d_dV, (size_t)B * Cp * 8));
+  out.owned.push_back(d_dV);
   CUDA_OR_5(cudaMalloc(&d_carry, (size_t)B * Cp * 8));
+  out.owned.push_back(d_carry);
   CUDA_OR_5(cudaMalloc(&d_ans, nans * 8));
+  out.owned.push_back(d_ans);
   CUDA_OR_5(cudaDeviceSynchronize());
   const auto u1 = clk::now();
   GpuV7Args a{};
@@ -212,31 +238,110 @@ int run_v7_arm(const BwV7Plan* p, std::vector<int64_t>& answers, Timings& tm) {
   CUDA_OR_5(cudaEventElapsedTime(&k_ms, ev[0], ev[1]));
   CUDA_OR_5(cudaEventElapsedTime(&c_ms, ev[1], ev[2]));
   CUDA_OR_5(cudaEventElapsedTime(&m_ms, ev[2], ev[3]));
-  const auto d0 = clk::now();
-  answers.assign(nans, 0);
-  if (nans) CUDA_OR_5(cudaMemcpy(answers.data(), d_ans, nans * 8, cudaMemcpyDeviceToHost));
-  const auto d1 = clk::now();
+  out.d = d_ans;
+  out.n = nans;
   tm.upload = ns_between(u0, u1);
   tm.kernel = (int64_t)((double)k_ms * 1e6);
   tm.carry = (int64_t)((double)c_ms * 1e6);
   tm.combine = (int64_t)((double)m_ms * 1e6);
-  tm.download = ns_between(d0, d1);
   tm.blocks = B;
   tm.threads = 512;
   tm.shared = (int32_t)(((size_t)Cp + (size_t)G) * 8);
   tm.kernels = 4;
   tm.algorithmic_bytes = 40.0 * S + 8.0 * nans * 3 + 16.0 * B * Cp;
   for (auto& e : ev) cudaEventDestroy(e);
-  void* bufs[] = {d_nodes, d_v0, d_v1, d_fac, d_g2row, d_ms_off, d_ms_cls, d_ms_base, d_ms_dev, d_devbuf,
-                  d_need, d_qlb, d_qhb, d_bidx, d_vbase, d_lvals, d_dV, d_carry, d_ans};
-  for (void* b : bufs) CUDA_OR_5(cudaFree(b));
+  return 0;
+}
+
+// Extract: the answers come down in 2 MiB chunks through a ring of pinned buffers
+// on a copy stream, and each landed chunk is digested while the next ones copy:
+// SHA-256 on this thread, FNV-1a and the raw answer-file write on a helper thread.
+// The digests equal the one-shot ones over the whole vector.  Returns 4 when the
+// answer file cannot be written, 5 on a CUDA error.
+struct ExtractResult {
+  char sha[65] = {0};
+  uint64_t fnv = 0;
+  int64_t download_ns = 0;   // summed device time of the chunk copies
+};
+
+int extract_answers(const DeviceAnswers& da, const std::string& path, ExtractResult& r) {
+  FILE* out = std::fopen(path.c_str(), "wb");
+  if (!out) return 4;
+  constexpr size_t kChunk = (size_t)1 << 18;   // answers per chunk
+  constexpr int kRing = 4;
+  const size_t nchunks = (da.n + kChunk - 1) / kChunk;
+  struct Ring {
+    int64_t* host[kRing] = {};
+    cudaEvent_t beg[kRing] = {}, end[kRing] = {};
+    cudaStream_t s = nullptr;
+    ~Ring() {
+      for (int k = 0; k < kRing; ++k) {
+        if (host[k]) cudaFreeHost(host[k]);
+        if (beg[k]) cudaEventDestroy(beg[k]);
+        if (end[k]) cudaEventDestroy(end[k]);
+      }
+      if (s) cudaStreamDestroy(s);
+    }
+  } ring;
+  auto fail = [&](cudaError_t e) {
+    std::fprintf(stderr, "CUDA error %s in the answer extract\n", cudaGetErrorString(e));
+    std::fclose(out);
+    return 5;
+  };
+  cudaError_t e = cudaStreamCreateWithFlags(&ring.s, cudaStreamNonBlocking);
+  for (int k = 0; e == cudaSuccess && k < kRing && (size_t)k < nchunks; ++k) {
+    e = cudaHostAlloc(reinterpret_cast<void**>(&ring.host[k]), kChunk * 8, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaEventCreate(&ring.beg[k]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ring.end[k]);
+  }
+  if (e != cudaSuccess) return fail(e);
+  auto chunk_len = [&](size_t c) { return std::min(kChunk, da.n - c * kChunk); };
+  auto issue = [&](size_t c) {
+    const int k = (int)(c % kRing);
+    cudaError_t x = cudaEventRecord(ring.beg[k], ring.s);
+    if (x == cudaSuccess)
+      x = cudaMemcpyAsync(ring.host[k], da.d + c * kChunk, chunk_len(c) * 8, cudaMemcpyDeviceToHost, ring.s);
+    if (x == cudaSuccess) x = cudaEventRecord(ring.end[k], ring.s);
+    return x;
+  };
+  for (size_t c = 0; e == cudaSuccess && c < nchunks && c < (size_t)kRing; ++c) e = issue(c);
+  if (e != cudaSuccess) return fail(e);
+  BwSha256 sh;
+  bw_sha256_init(&sh);
+  uint64_t fn = BW_FNV1A_BASIS;
+  bool wok = true;
+  double copy_ms = 0;
+  for (size_t c = 0; c < nchunks; ++c) {
+    const int k = (int)(c % kRing);
+    if ((e = cudaEventSynchronize(ring.end[k])) != cudaSuccess) return fail(e);
+    float ms = 0.f;
+    if ((e = cudaEventElapsedTime(&ms, ring.beg[k], ring.end[k])) != cudaSuccess) return fail(e);
+    copy_ms += ms;
+    const int64_t* buf = ring.host[k];
+    const size_t n = chunk_len(c);
+    std::thread side([&fn, &wok, buf, n, out] {
+      fn = bw_fnv1a_update(fn, buf, n * 8);
+      wok = std::fwrite(buf, 8, n, out) == n && wok;
+    });
+    bw_sha256_update(&sh, buf, n * 8);
+    side.join();
+    if (c + kRing < nchunks && (e = issue(c + kRing)) != cudaSuccess) return fail(e);
+  }
+  wok = std::fclose(out) == 0 && wok;
+  bw_sha256_final(&sh, r.sha);
+  r.fnv = fn;
+  r.download_ns = (int64_t)(copy_ms * 1e6);
+  if (!wok) {
+    std::fprintf(stderr, "short answer write\n");
+    return 4;
+  }
   return 0;
 }
 
 }  // namespace
 
 int main(int argc, char** argv) {
-  std::string arm = "gb300", fixture_path, base_id, answers_path, json_path;
+  std::string arm = "gb300", fixture_path, base_id, answers_path, json_path, events_path;
   int32_t topology = 0, seed = 7, factor_period = 4, q = 2, repeat = 0, states = 0, blocks = 0;
   for (int i = 1; i < argc; ++i) {
     auto next = [&](const char* k) -> std::string {
@@ -269,6 +374,7 @@ int main(int argc, char** argv) {
     else if (!std::strcmp(k, "--json")) json_path = next(k);
     else if (!std::strcmp(k, "--states")) states = num(k);
     else if (!std::strcmp(k, "--blocks")) blocks = num(k);
+    else if (!std::strcmp(k, "--events")) events_path = next(k);
     else {
       std::fprintf(stderr, "unknown argument %s\n", k);
       return 2;
@@ -277,11 +383,15 @@ int main(int argc, char** argv) {
   if (fixture_path.empty() || answers_path.empty() || json_path.empty()) {
     std::fprintf(stderr, "usage: bw_worker --fixture PATH --base-id ID --topology T --seed S "
                          "--factor-period P --q Q --repeat R --answers A --json J [--arm gb300|gpu_v7] "
-                         "[--states N] [--blocks B]\n");
+                         "[--states N] [--blocks B] [--events STREAM]\n");
     return 2;
   }
   if (arm != "gb300" && arm != "gpu_v7") {
     std::fprintf(stderr, "unknown arm %s (gb300 or gpu_v7)\n", arm.c_str());
+    return 2;
+  }
+  if (!events_path.empty() && arm != "gb300") {
+    std::fprintf(stderr, "--events replays on the gb300 arm only\n");
     return 2;
   }
   if (!states) {
@@ -311,7 +421,22 @@ int main(int argc, char** argv) {
   BwNativeSpec spec{states, topology, seed, factor_period, q, per_state ? 1 : 0, -1};
   BwNativeWorkload* w = nullptr;
   BwV7Plan* plan = nullptr;
-  if (arm == "gb300") {
+  BwStreamWorkload* sw = nullptr;
+  if (!events_path.empty()) {
+    std::ifstream in(events_path, std::ios::binary);
+    const std::vector<char> img((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+    if (!in.good() && !in.eof()) {
+      std::fprintf(stderr, "cannot read event stream\n");
+      return 3;
+    }
+    if (bw_stream_build(fx, img.data(), img.size(), &sw)) {
+      std::fprintf(stderr, "malformed event stream\n");
+      return 3;
+    }
+    w = &sw->chain;
+    q = sw->q;
+    if (q > 0) states = (int32_t)(sw->n_answers / q) + 1;
+  } else if (arm == "gb300") {
     if (bw_native_build(fx, &spec, &w)) {
       std::fprintf(stderr, "workload build failed (unsupported case)\n");
       return 3;
@@ -327,32 +452,44 @@ int main(int argc, char** argv) {
   // ---- execute: upload, replay, download
   CUDA_OR_5(cudaSetDevice(0));
   CUDA_OR_5(cudaFree(nullptr));   // context creation is not a copy cost
-  std::vector<int64_t> answers;
+  DeviceAnswers da;
   Timings tm;
   const auto te0 = clk::now();
-  const int rc = arm == "gb300" ? run_event_arm(w, blocks, answers, tm) : run_v7_arm(plan, answers, tm);
+  const int rc = arm == "gb300" ? run_event_arm(w, blocks, da, tm) : run_v7_arm(plan, da, tm);
   if (rc) return rc;
+  if (sw) {   // chain answers (stream order) -> the (state, k) answer vector
+    int64_t *d_slot = nullptr, *d_out = nullptr;
+    const size_t nq = (size_t)sw->chain.n_queries, na = (size_t)sw->n_answers;
+    if (upload(&d_slot, sw->slot, nq)) return 5;
+    da.owned.push_back(d_slot);
+    CUDA_OR_5(cudaMalloc(&d_out, (na ? na : 1) * 8));
+    da.owned.push_back(d_out);
+    CUDA_OR_5(cudaMemset(d_out, 0, (na ? na : 1) * 8));
+    BW_OR_5(bw_scatter_answers(da.d, d_slot, (int64_t)nq, d_out, (int64_t)na, nullptr), "bw_scatter_answers");
+    CUDA_OR_5(cudaDeviceSynchronize());
+    da.d = d_out;
+    da.n = na;
+  }
   const auto t3 = clk::now();
 
-  // ---- extract
-  FILE* out = std::fopen(answers_path.c_str(), "wb");
-  if (!out) {
-    std::fprintf(stderr, "cannot write answers\n");
-    return 4;
+  // ---- extract: pipelined download, digests and answer file
+  ExtractResult xr;
+  const int xrc = extract_answers(da, answers_path, xr);
+  if (xrc) {
+    if (xrc == 4) std::fprintf(stderr, "cannot write answers\n");
+    return xrc;
   }
-  const bool wok = std::fwrite(answers.data(), 8, answers.size(), out) == answers.size();
-  std::fclose(out);
-  if (!wok) {
-    std::fprintf(stderr, "short answer write\n");
-    return 4;
-  }
-  const uint64_t fn = bw_fnv1a(answers.data(), answers.size() * 8);
-  char sha[65];
-  bw_sha256_hex(answers.data(), answers.size() * 8, sha);
+  tm.download = xr.download_ns;
+  const uint64_t fn = xr.fnv;
+  const char* sha = xr.sha;
+  const size_t n_answers = da.n;
   const auto t4 = clk::now();
 
   // ---- cleanup
-  if (w) bw_native_free(w);
+  for (void* b : da.owned) cudaFree(b);
+  da.owned.clear();
+  if (sw) bw_stream_free(sw);
+  else if (w) bw_native_free(w);
   if (plan) bw_v7_plan_free(plan);
   bw_fixture_close(fx);
   const auto t5 = clk::now();
@@ -376,7 +513,7 @@ int main(int argc, char** argv) {
   std::fprintf(jf, "  \"fixture\": \"%s\",\n  \"topology\": %d,\n  \"seed\": %d,\n  \"factor_period\": %d,\n",
                fixture_path.c_str(), topology, seed, factor_period);
   std::fprintf(jf, "  \"q\": %d,\n  \"repeat\": %d,\n  \"n_states\": %d,\n  \"n_answers\": %zu,\n", q, repeat, states,
-               answers.size());
+               n_answers);
   std::fprintf(jf, "  \"range_scope\": \"%s\",\n", per_state ? "per_state" : "shared");
   std::fprintf(jf, "  \"answers_fn\": \"%016" PRIx64 "\",\n  \"answers_sha256\": \"%s\",\n", fn, sha);
   std::fprintf(jf,
@@ -390,7 +527,7 @@ int main(int argc, char** argv) {
                devname.c_str(), tm.blocks, tm.threads, tm.shared, tm.kernels, tm.upload, tm.kernel, tm.carry, tm.combine,
                tm.download);
   std::fprintf(jf, "  \"answers_per_s\": %.6g,\n  \"hbm_gbps\": %.6g,\n",
-               kernel_total ? (double)answers.size() / ((double)kernel_total * 1e-9) : 0.0,
+               kernel_total ? (double)n_answers / ((double)kernel_total * 1e-9) : 0.0,
                kernel_total ? tm.algorithmic_bytes / (double)kernel_total : 0.0);
   std::fprintf(jf, "  \"full_ns\": %" PRId64 ",\n  \"peak_rss_kb\": %" PRId64 "\n}\n", full_ns, peak_rss_kb());
   std::fclose(jf);

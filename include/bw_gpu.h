@@ -304,6 +304,11 @@ int bw_key_prefix(const int64_t* vec, uint32_t n, int64_t* prefix, void* stream)
  * n_keys): the carry below the rank inside each query's interval. */
 int bw_add_range_carry(const BwQuery* queries, int64_t n, uint32_t n_keys, const int64_t* prefix,
                        int64_t* answers, void* stream);
+/* dst[slot[i]] = src[i] for every i with 0 <= slot[i] < n_dst (device arrays): the
+ * answers of a BWLEV001 stream workload's chain queries, in stream order, into the
+ * reference's (state, k) answer order (bw_stream_build's slot, include/bw_host.h). */
+int bw_scatter_answers(const int64_t* src, const int64_t* slot, int64_t n, int64_t* dst, int64_t n_dst,
+                       void* stream);
 
 /* ============================================================ batched version forests
  * Thousands of independent version trees replayed in one pipeline (the reference

@@ -128,9 +128,42 @@ int bw_v7_plan_build(const BwFixture* f, const BwNativeSpec* spec, int32_t block
 int bw_v7_plan_build_declared(const BwFixture* f, const BwDeclared* w, int32_t blocks, BwV7Plan** out);
 void bw_v7_plan_free(BwV7Plan* p);
 
-/* Lowercase hex SHA-256 (64 chars + NUL) and the reference's FNV-1a. */
+/* BWLEV001 event stream ingest (emit_events.cpp:5-8, 21-27, 62-66): the reference's
+ * sequential stream of row deltas, factor sets and queries (16-byte header, 36-byte
+ * records) over a fixture's base rows, compiled into a linear-chain event workload:
+ * chain state i is the stream before its i-th query, keys are endpoint classes over
+ * the stream's distinct query bounds, a factor change expands into one event per
+ * class of the group's live mass.  slot[i] is the i-th query's index in the answer
+ * vector ((state - 1) * q + k; -1 for state-0 queries), n_answers its length.
+ * Returns 2 on bad arguments or allocation failure, 3 on a malformed stream. */
+typedef struct BwStreamWorkload {
+  BwNativeWorkload chain;
+  int64_t* slot;
+  int64_t n_answers;
+  int32_t q;
+} BwStreamWorkload;
+int bw_stream_build(const BwFixture* f, const void* data, size_t bytes, BwStreamWorkload** out);
+void bw_stream_free(BwStreamWorkload* w);
+
+/* Lowercase hex SHA-256 (64 chars + NUL) and the reference's FNV-1a
+   (common.hpp:396-400, sha_fast/sha256.hpp), one-shot and streaming: a digest
+   fed the same bytes in any split gives the one-shot value. */
 void bw_sha256_hex(const void* data, size_t n, char out_hex[65]);
 uint64_t bw_fnv1a(const void* data, size_t n);
+
+typedef struct BwSha256 {
+  uint32_t h[8];
+  uint64_t bytes;      /* bytes fed so far */
+  uint8_t buf[64];     /* pending partial block */
+  uint32_t fill;
+} BwSha256;
+void bw_sha256_init(BwSha256* s);
+void bw_sha256_update(BwSha256* s, const void* data, size_t n);
+void bw_sha256_final(BwSha256* s, char out_hex[65]);
+
+#define BW_FNV1A_BASIS 1469598103934665603ULL
+/* FNV-1a continued over more bytes: start from BW_FNV1A_BASIS. */
+uint64_t bw_fnv1a_update(uint64_t h, const void* data, size_t n);
 
 #ifdef __cplusplus
 }

@@ -158,6 +158,49 @@ def direct_scan_declared(fx: Fixture, decl) -> np.ndarray:
     return ans
 
 
+STREAM_DTYPE = np.dtype([("kind", "<u4"), ("state", "<u4"), ("qidx", "<u4"), ("g", "<i4"), ("w", "<i4"),
+                         ("a", "<i8"), ("b", "<i8")])   # 36 bytes, packed
+
+
+def stream_answers(fixture: bytes, stream: bytes) -> np.ndarray:
+    """The reference's answers for a BWLEV001 event stream (emit_events.cpp:5-8,
+    21-27): replay the records in order over the fixture's base rows, answer each
+    query as the sum over groups of factor x the live amounts with t in [lo, hi)
+    (external/dd_probe/src/main.rs:66-80), and order the answers by (state, qidx)
+    without state 0 (main.rs:245-262).  Wrapping int64 throughout.  A direct
+    restatement over per-group live-mass arrays: Python loops, test sizes only."""
+    import struct
+    assert stream[:8] == b"BWLEV001"
+    (n,) = struct.unpack_from("<Q", stream, 8)
+    assert len(stream) == 16 + 36 * n
+    rec = np.frombuffer(stream, dtype=STREAM_DTYPE, count=n, offset=16)
+    rows, groups = struct.unpack_from("<qi", fixture, 8)
+    base = np.frombuffer(fixture, dtype=np.dtype([("t", "<i8"), ("a", "<i8"), ("g", "<i4"), ("p", "<i4")]),
+                         count=rows, offset=64)
+    mul = [int(x) for x in np.frombuffer(fixture, dtype="<i8", count=groups, offset=64 + 24 * rows)]
+    times = np.unique(np.concatenate([base["t"], rec["a"][rec["kind"] == 0]]))
+    live = np.zeros((groups, times.size), dtype=np.int64)
+    np.add.at(live, (base["g"], np.searchsorted(times, base["t"])), base["a"])
+    M = (1 << 64) - 1
+    out = []
+    with np.errstate(over="ignore"):
+        for r in rec:
+            k = int(r["kind"])
+            if k == 0:
+                live[r["g"], np.searchsorted(times, r["a"])] += np.int64(r["w"]) * r["b"]
+            elif k == 1:
+                mul[int(r["g"])] = int(r["a"])
+            else:
+                lo, hi = np.searchsorted(times, [r["a"], r["b"]])
+                ans = 0
+                for g in range(groups):
+                    ans += mul[g] * int(live[g, lo:hi].sum()) if hi > lo else 0
+                ans &= M
+                out.append((int(r["state"]), int(r["qidx"]), ans - (1 << 64) if ans >> 63 else ans))
+    out.sort()
+    return np.array([a for s, _, a in out if s != 0], dtype=np.int64)
+
+
 def _ev_arrays(parent, events, queries):
     parent = np.ascontiguousarray(parent, dtype=np.int32)
     events = np.ascontiguousarray(events, dtype=EVENT_DTYPE)

@@ -31,6 +31,13 @@ $(OUT)/compiled_$(STATES): $(OUT)/sha_shim.o
 	$(CXX) -std=c++17 -O3 -fopenmp -DBWH_STATES=$(STATES) -DBWH_MAXQ=$(MAXQ) -Ioracle/ref_shim -I$(REF)/src \
 	  $(REF)/src/panel_batch_v7fix.cpp $(OUT)/sha_shim.o $(OUT)/bwo.o -o $@
 
+# The reference's BWLEV001 event-stream emitter (emit_events.cpp), unmodified.
+emit: $(OUT)/emit_events_$(STATES)
+
+$(OUT)/emit_events_$(STATES):
+	mkdir -p $(OUT)
+	$(CXX) -std=c++17 -O2 -DBWH_STATES=$(STATES) -DBWH_MAXQ=$(MAXQ) -I$(REF)/src $(REF)/src/emit_events.cpp -o $@
+
 # The reference's CsrBase rank/range (sparse_engine.hpp:70-102) behind a small harness.
 $(OUT)/csr_ref: oracle/ref_csr.cpp
 	mkdir -p $(OUT)

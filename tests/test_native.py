@@ -59,6 +59,21 @@ def test_host_sha_matches_oracle(bw, oracle_mod):
         assert bw.fnv1a(data[:n]) == oracle_mod.fnv1a(data[:n])
 
 
+def test_streaming_digest_equals_one_shot(bw):
+    """The extract digests chunk by chunk: any split gives the one-shot SHA-256/FNV-1a."""
+    rng = np.random.default_rng(5)
+    data = rng.integers(0, 256, 300_001, dtype=np.uint8).tobytes()
+    for cuts in ([], [1], [63, 64, 65], [55, 56, 57, 120], list(rng.integers(0, len(data), 40))):
+        d = bw.Digest()
+        prev = 0
+        for c in sorted(cuts) + [len(data)]:
+            d.update(data[prev:c])
+            prev = c
+        sha, fnv = d.final()
+        assert sha == bw.sha256_hex(data) and fnv == bw.fnv1a(data)
+    assert bw.Digest().final()[0] == bw.sha256_hex(b"")
+
+
 def test_front_end_rejects_bad_fixture(bw):
     img = bytearray(fixture("check"))
     img[0:8] = b"BWBASE99"

@@ -64,6 +64,17 @@ def test_worker_fixture_and_case_errors_exit_3(bw, tmp_path):
     assert not (tmp_path / "a.json").exists()
 
 
+def test_worker_event_stream_errors(bw, tmp_path):
+    common = ["--answers", tmp_path / "a.bin", "--json", tmp_path / "a.json"]
+    fx = fixture_file(tmp_path)
+    bad = tmp_path / "bad.bwlev"
+    bad.write_bytes(b"BWLEV001" + (3).to_bytes(8, "little") + b"\0" * 10)
+    assert run(bw, tmp_path, "--fixture", fx, "--events", bad, *common).returncode == 3
+    assert run(bw, tmp_path, "--fixture", fx, "--events", tmp_path / "missing.bwlev", *common).returncode == 3
+    assert run(bw, tmp_path, "--fixture", fx, "--events", bad, "--arm", "gpu_v7", *common).returncode == 2
+    assert not (tmp_path / "a.json").exists()
+
+
 # ------------------------------------------------------------------------------ GPU
 def _cases():
     return [c for c in GOLDEN["cases"] if c["fixture"] == "check"]
@@ -104,3 +115,21 @@ def test_worker_unwritable_answers_exit_4(bw, torch_cuda, tmp_path):
             tmp_path / "x.json", scope="per_state")
     assert r.returncode == 4
     assert not (tmp_path / "x.json").exists()
+
+
+STREAMS = json.loads((GOLD / "stream_golden.json").read_text())["cases"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", STREAMS, ids=lambda c: c["file"])
+def test_worker_event_stream_reproduces_golden(bw, torch_cuda, tmp_path, case):
+    fx = fixture_file(tmp_path)
+    ev = tmp_path / "s.bwlev"
+    ev.write_bytes(zlib.decompress((GOLD / case["file"]).read_bytes()))
+    ans, js = tmp_path / "a.bin", tmp_path / "a.json"
+    r = run(bw, tmp_path, "--fixture", fx, "--events", ev, "--answers", ans, "--json", js)
+    assert r.returncode == 0, r.stderr
+    rec = json.loads(js.read_text())
+    assert rec["answers_sha256"] == case["answers_sha256"]
+    assert hashlib.sha256(ans.read_bytes()).hexdigest() == case["answers_sha256"]
+    assert rec["answers_fn"] == case["fnv1a"] and rec["n_answers"] == case["n_answers"]
