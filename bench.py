@@ -376,7 +376,8 @@ def plain_record(args, bw, dev, name: str, scale: float, steps: int, warmup: int
     h_answers = torch.empty(Q, dtype=torch.int64).pin_memory()
     d_parent, d_events, d_queries = h_parent.to(dev), h_events.to(dev), h_queries.to(dev)
     d_answers = torch.empty(Q, dtype=torch.int64, device=dev)
-    plan = bw.Replay(d_parent, w.n_keys, E, Q, blocks=args.blocks, chain=w.chain, timing=True, path=args.path)
+    plan = bw.Replay(d_parent, w.n_keys, E, Q, blocks=args.blocks, chain=w.chain, timing=True, path=args.path,
+                     wide=w.chain and bw.wide_deltas(w.events))
     chain_path = plan.chain_path(d_events)
     stream = torch.cuda.current_stream(dev)
     for i in range(max(1, warmup)):
@@ -562,7 +563,7 @@ def reference_chain_record(args, bw, dev, steps: int) -> dict:
     d_events = torch.from_numpy(w.events.view(np.int64).reshape(-1, 2)).to(dev)
     d_queries = torch.from_numpy(w.queries.view(np.int32).reshape(-1, 3)).to(dev)
     d_answers = torch.empty(Q, dtype=torch.int64, device=dev)
-    plan = bw.Replay(d_parent, w.n_keys, E, Q, chain=True, timing=True)
+    plan = bw.Replay(d_parent, w.n_keys, E, Q, chain=True, timing=True, wide=bw.wide_deltas(w.events))
     chain_path = plan.chain_path(d_events)
     for _ in range(3):
         plan.launch(d_parent, d_events, d_queries, d_answers)

@@ -33,6 +33,7 @@ BW_REPLAY_CHAIN_HINT = 1
 BW_REPLAY_TIMING = 2
 BW_REPLAY_CHAIN_KERNEL = 4
 BW_REPLAY_GENERAL = 8
+BW_REPLAY_WIDE = 16
 PATH_FLAGS = {"auto": 0, "chain": BW_REPLAY_CHAIN_KERNEL, "general": BW_REPLAY_GENERAL}
 STAGES = ["ingest", "linearise", "blocks", "prepare", "carry", "sweep"]
 STATUS_NAMES = {0: "ok", 1: "events not grouped by state", 2: "event key out of range",
@@ -177,7 +178,8 @@ class Replay:
     """Reusable replay plan: holds the device workspace for one input shape."""
 
     def __init__(self, parent, n_keys: int, n_events: int, n_queries: int, *, blocks: int = 0,
-                 chain: bool = False, timing: bool = False, path: str = "auto", device=None):
+                 chain: bool = False, timing: bool = False, path: str = "auto", wide: bool = False,
+                 device=None):
         torch = _torch()
         self.lib = gpu_lib()
         self.device = device or parent.device
@@ -188,7 +190,8 @@ class Replay:
         a.n_events = int(n_events)
         a.n_queries = int(n_queries)
         a.blocks = int(blocks)
-        a.flags = (BW_REPLAY_CHAIN_HINT if chain else 0) | (BW_REPLAY_TIMING if timing else 0) | PATH_FLAGS[path]
+        a.flags = ((BW_REPLAY_CHAIN_HINT if chain else 0) | (BW_REPLAY_TIMING if timing else 0) | PATH_FLAGS[path]
+                   | (BW_REPLAY_WIDE if wide else 0))
         nbytes = C.c_size_t(0)
         _check(self.lib.bw_replay_workspace_size(C.byref(a), C.byref(nbytes)), "workspace size")
         self.workspace = torch.empty(max(int(nbytes.value), 256), dtype=torch.uint8, device=self.device)
@@ -246,13 +249,15 @@ class Replay:
 
 
 def replay(parent, n_keys: int, events, queries, *, blocks: int = 0, chain: bool = False,
-           check: bool = True, path: str = "auto"):
+           check: bool = True, path: str = "auto", wide: bool = False):
     """One replay on the current CUDA stream; returns int64 answers on the device.
     ``path``: "auto" (the chain path for event-heavy chains with small key domains,
     else the general pipeline), "chain" or "general" to force one (chain needs
-    ``chain=True``)."""
+    ``chain=True``).  ``wide``: the chain path keeps an int64 histogram
+    (BW_REPLAY_WIDE) -- for deltas mostly outside (-2^19, 2^19), see wide_deltas()."""
     torch = _torch()
-    r = Replay(parent, n_keys, events.shape[0], queries.shape[0], blocks=blocks, chain=chain, path=path)
+    r = Replay(parent, n_keys, events.shape[0], queries.shape[0], blocks=blocks, chain=chain, path=path,
+               wide=wide)
     answers = torch.empty(queries.shape[0], dtype=torch.int64, device=parent.device)
     r.launch(parent, events, queries, answers)
     if check:
@@ -260,6 +265,18 @@ def replay(parent, n_keys: int, events, queries, *, blocks: int = 0, chain: bool
         if st:
             raise ValueError(f"replay input rejected on the device: {STATUS_NAMES.get(st, st)}")
     return answers
+
+
+def wide_deltas(events) -> bool:
+    """Whether a host event array is better replayed with BW_REPLAY_WIDE: more than
+    one event in 64 carries a delta outside (-2^19, 2^19) (the int32 window's range)."""
+    import numpy as np
+    d = np.asarray(events["delta"] if getattr(events, "dtype", None) is not None and events.dtype.names
+                   else events)
+    if d.size == 0:
+        return False
+    big = np.count_nonzero((d >= (1 << 19)) | (d <= -(1 << 19)))
+    return big * 64 > d.size
 
 
 class _ForestShape:

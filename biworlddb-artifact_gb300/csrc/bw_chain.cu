@@ -31,6 +31,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <mutex>
+#include <type_traits>
 
 #include "bw_gpu.h"
 #include "bw_common.cuh"
@@ -82,12 +83,13 @@ struct SweepSmem {
   size_t ring, H, T, qbuf, qpre, bar, misc, bytes;
 };
 __host__ __device__ inline size_t al16(size_t x) { return (x + 15) & ~size_t(15); }
-__host__ __device__ inline SweepSmem sweep_smem(uint32_t C, int nch, int te, int ns) {
+// hw: bytes of a window entry (4: int32 window, 8: int64 window)
+__host__ __device__ inline SweepSmem sweep_smem(uint32_t C, int nch, int te, int ns, int hw) {
   SweepSmem L;
   size_t o = 0;
   L.ring = o;  o = al16(o + (size_t)ns * te * 16);
-  L.H = o;     o = al16(o + (size_t)C * 4);
-  L.T = o;     o = al16(o + (size_t)nch * 4);
+  L.H = o;     o = al16(o + (size_t)C * hw);
+  L.T = o;     o = al16(o + (size_t)nch * hw);
   L.qbuf = o;  o = al16(o + 2 * (size_t)QB * 16);   // two tiles' query records
   L.qpre = o;  o = al16(o + 32 * 12);                // prefetched window of 32 query records
   L.bar = o;   o = al16(o + (size_t)ns * 8);
@@ -169,6 +171,35 @@ __device__ __forceinline__ int32_t probe_flat(const int32_t* H, uint32_t lo, uin
     const int4 v = *reinterpret_cast<const int4*>(H + k);
     const uint32_t d = k - lo;
     s += (d < w ? v.x : 0) + (d + 1 < w ? v.y : 0) + (d + 2 < w ? v.z : 0) + (d + 3 < w ? v.w : 0);
+  }
+  return s;
+}
+
+// The int64 window's counterparts: lane shares of the sum over [lo, hi) (lo < hi <= C)
+// from 32-key chunk totals plus the partial chunks, or flat 128-bit reads of two
+// keys each (H 16-byte aligned and padded to an even key count).
+__device__ __forceinline__ uint64_t probe_chunks64(const unsigned long long* H, const unsigned long long* T,
+                                                   uint32_t lo, uint32_t hi, int lane) {
+  const uint32_t clo = (lo + 31) >> kChunkShift, chi = hi >> kChunkShift;
+  uint64_t s = 0;
+  if (clo >= chi) {
+    for (uint32_t k = lo + lane; k < hi; k += 32) s += H[k];
+    return s;
+  }
+  const uint32_t a = lo + lane, z = (chi << kChunkShift) + lane;
+  if (a < (clo << kChunkShift)) s += H[a];
+  if (z < hi) s += H[z];
+  for (uint32_t c = clo + lane; c < chi; c += 32) s += T[c];
+  return s;
+}
+__device__ __forceinline__ uint64_t probe_flat64(const unsigned long long* H, uint32_t lo, uint32_t hi, int lane) {
+  const uint32_t w = hi - lo;
+  uint64_t s = 0;
+#pragma unroll 2
+  for (uint32_t k = (lo & ~1u) + 2 * lane; k < hi; k += 64) {
+    const ulonglong2 v = *reinterpret_cast<const ulonglong2*>(H + k);
+    const uint32_t d = k - lo;
+    s += (d < w ? v.x : 0ull) + (d + 1 < w ? v.y : 0ull);
   }
   return s;
 }
@@ -260,6 +291,23 @@ __device__ void find_tile_queries(const ChainParams& p, uint32_t* qpre, int64_t&
   pbase = qcur;
 }
 
+// The same with the int64 window (no folded row: it only fills at the end).
+__device__ __forceinline__ int64_t answer_one64(const ChainParams& p, const unsigned long long* H,
+                                                const unsigned long long* T, const uint4* tile, uint32_t pos,
+                                                uint32_t lo, uint32_t hi, int lane) {
+  lo = min(lo, p.C);
+  hi = min(hi, p.C);
+  if (lo >= hi) return 0;
+  const uint32_t w = hi - lo;
+  uint64_t part = p.nch ? probe_chunks64(H, T, lo, hi, lane) : probe_flat64(H, lo, hi, lane);
+#pragma unroll 4
+  for (uint32_t j = lane; j < pos; j += 32) {
+    const uint4 e = tile[j];
+    if (e.y - lo < w) part += ((uint64_t)e.w << 32) | e.z;
+  }
+  return (int64_t)warp_sum_u64(part);
+}
+
 // Answer of one query by one warp, valid in lane 0: the folded key prefix row
 // (P[hi] - P[lo], when it holds data), the window probe, and the tile's first
 // `pos` events inside [lo, hi) (tile == nullptr: none).
@@ -298,8 +346,8 @@ __device__ __forceinline__ int64_t answer_one(const ChainParams& p, const int32_
 // prefix row: P[k+1] += sum of H[j] + wide[j] over j <= k.  Each thread takes a
 // contiguous key segment; a CTA-wide exclusive scan of the segment sums gives its
 // base.  H, T and the consumed wide entries return to zero.  All threads call it.
-template <int NT>
-__device__ void fold(const ChainParams& p, int32_t* H, int32_t* T, int64_t* P, int64_t* wide, bool rows_live,
+template <int NT, typename HT>
+__device__ void fold(const ChainParams& p, HT* H, HT* T, int64_t* P, int64_t* wide, bool rows_live,
                      bool wide_live, Misc* m) {
   constexpr int NW = NT / 32;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -307,7 +355,7 @@ __device__ void fold(const ChainParams& p, int32_t* H, int32_t* T, int64_t* P, i
   const uint32_t k0 = min(C, (uint32_t)tid * per), k1 = min(C, k0 + per);
   uint64_t s = 0;
   for (uint32_t k = k0; k < k1; ++k) {
-    s += (uint64_t)(int64_t)H[k];
+    s += (uint64_t)(int64_t)H[k];   // sign-extends an int32 window entry
     if (wide_live) s += (uint64_t)__ldcg(wide + k);
   }
   uint64_t incl = s;
@@ -338,17 +386,20 @@ __device__ void fold(const ChainParams& p, int32_t* H, int32_t* T, int64_t* P, i
 
 // Tile geometry: NT threads, EPT events per thread, TL = NT * EPT events per tile
 // (<= 1024, so an int32-safe tile's absolute sum stays below 2^29); MINB CTAs per SM;
-// NS tiles in the shared-memory ring.
-template <int NT, int EPT, int MINB, int NS>
+// NS tiles in the shared-memory ring.  W64: the window is int64 (two 32-bit shared
+// atomics per update, exact modulo 2^64 at any delta size): no window folds, no wide
+// tiles -- the mode for chains whose deltas mostly exceed the int32-safe range.
+template <int NT, int EPT, int MINB, int NS, bool W64>
 __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
   constexpr int NW = NT / 32, QW = NW - 1, TL = NT * EPT;
   static_assert(TL <= TE && NW <= kMaxWarps && NW >= 2, "tile geometry");
   extern __shared__ __align__(128) unsigned char sm[];
   const uint32_t C = p.C;
-  const SweepSmem SL = sweep_smem(C, p.nch, TL, NS);
+  using HT = typename std::conditional<W64, unsigned long long, int32_t>::type;
+  const SweepSmem SL = sweep_smem(C, p.nch, TL, NS, (int)sizeof(HT));
   uint4* ring = reinterpret_cast<uint4*>(sm + SL.ring);
-  int32_t* H = reinterpret_cast<int32_t*>(sm + SL.H);
-  int32_t* T = reinterpret_cast<int32_t*>(sm + SL.T);
+  HT* H = reinterpret_cast<HT*>(sm + SL.H);
+  HT* T = reinterpret_cast<HT*>(sm + SL.T);
   uint32_t* qbuf = reinterpret_cast<uint32_t*>(sm + SL.qbuf);   // [2][QB] uint4, by tile parity
   uint32_t* qpre = reinterpret_cast<uint32_t*>(sm + SL.qpre);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + SL.bar);
@@ -414,7 +465,7 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
       for (int k = 0; k < EPT; ++k) {
         const int idx = tid + k * NT;
         cur[k] = idx < n ? ring[idx] : make_uint4(0, 0, 0, 0);
-        bigp |= !small_delta(cur[k]);
+        if (!W64) bigp |= !small_delta(cur[k]);
       }
       if (warp == QW) find_tile_queries(p, qpre, pbase, qcur, ring, n, qbuf_of(0), m->tq[0], lane);
     }
@@ -451,13 +502,13 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
     }
     // fold the window into the prefix row before it could overflow, and after a
     // wide tile (whose events went to the wide histogram)
-    if (win >= kFoldAt || wide_live) {
+    if (!W64 && (win >= kFoldAt || wide_live)) {
       fold<NT>(p, H, T, P, wrow, rows_live, wide_live, m);
       win = 0;
       rows_live = true;
       wide_live = false;
     }
-    if (big && !wide_init) {
+    if (!W64 && big && !wide_init) {
       for (uint32_t k = tid; k < C; k += NT) wrow[k] = 0;
       wide_init = true;
       __syncthreads();
@@ -493,7 +544,9 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
           hi = r[2];
           pos = tile_pos(tile, n, r[0]);
         }
-        const int64_t a = answer_one(p, H, T, P, rows_live, big != 0, tile, pos, lo, hi, lane);
+        int64_t a;
+        if constexpr (W64) a = answer_one64(p, H, T, tile, pos, lo, hi, lane);
+        else a = answer_one(p, H, T, P, rows_live, big != 0, tile, pos, lo, hi, lane);
         if (lane == 0) p.ans[i] = a;
       }
       __syncthreads();
@@ -511,10 +564,14 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
         bad |= (e.x < prev ? 1u : 0u) | (e.x >= (uint32_t)p.S ? 2u : 0u);
         if (e.y >= C) {
           bad |= 4u;
+        } else if (W64) {
+          const uint64_t d = ((uint64_t)e.w << 32) | e.z;
+          shared_add_u64(reinterpret_cast<unsigned long long*>(&H[e.y]), d);
+          if (p.nch) shared_add_u64(reinterpret_cast<unsigned long long*>(&T[e.y >> kChunkShift]), d);
         } else if (!big) {
           const int32_t d = (int32_t)e.z;
-          atomicAdd(&H[e.y], d);
-          if (p.nch) atomicAdd(&T[e.y >> kChunkShift], d);
+          atomicAdd(reinterpret_cast<int32_t*>(&H[e.y]), d);
+          if (p.nch) atomicAdd(reinterpret_cast<int32_t*>(&T[e.y >> kChunkShift]), d);
           wsum += (uint32_t)(d < 0 ? -d : d);
         } else {
           atomicAdd(reinterpret_cast<unsigned long long*>(wrow + e.y), ((unsigned long long)e.w << 32) | e.z);
@@ -541,7 +598,7 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
         for (int k = 0; k < EPT; ++k) {
           const int idx = tid + k * NT;
           cur[k] = idx < nn ? nt[idx] : make_uint4(0, 0, 0, 0);
-          bigp |= !small_delta(cur[k]);
+          if (!W64) bigp |= !small_delta(cur[k]);
         }
         if (warp == QW && !next_found)
           find_tile_queries(p, qpre, pbase, qcur, nt, nn, qbuf_of(t + 1), m->tq[(t + 1) & 1], lane);
@@ -565,7 +622,7 @@ __global__ void __launch_bounds__(NT, MINB) k_chain_sweep(ChainParams p) {
   }
   // final fold: the block's whole key histogram as a key prefix row
   if (warp == QW && lane == 0) m->tail_q0 = qcur;
-  fold<NT>(p, H, T, P, wrow, rows_live, wide_live, m);
+  fold<NT>(p, H, T, P, wrow, rows_live && !W64, wide_live && !W64, m);
   // last block: the queries after its last event see every event of the chain,
   // all of it now in the prefix row
   if (b == p.B - 1) {
@@ -626,17 +683,18 @@ __global__ void __launch_bounds__(kChainThreads) k_chain_fixup(ChainParams p) {
 struct Geometry {
   int threads, ept, minb, stages;
 };
-constexpr Geometry kGeometries[] = {{128, 4, 5, 3}, {256, 4, 3, 3}, {512, 2, 2, 3}, {256, 4, 4, 2},
-                                     {256, 2, 4, 4}, {512, 2, 2, 2}, {256, 3, 4, 3}};
-constexpr int kNumGeometries = 7;
+constexpr Geometry kGeometries[] = {{128, 4, 5, 3}, {256, 4, 3, 3}, {512, 2, 2, 3}, {256, 4, 4, 2}, {256, 3, 4, 3}};
+constexpr int kNumGeometries = 5;
 
 // BW_CHAIN_GEOMETRY=<index into kGeometries> pins the geometry (tuning runs).
 // Otherwise, when the events fill every CTA with full state blocks, 256 threads
 // with (in this order of preference, measured on byte-dominated chains) 3 events
-// each and a three-tile ring at four CTAs per SM, 4 events and a two-tile ring at
-// three or more, 4 events and a three-tile ring at two or more; else the geometry
-// with the most resident threads per SM (few, short state blocks: wide CTAs finish
-// each sooner).
+// each and a three-tile ring at four CTAs per SM (three with the int64 window), 4
+// events and a two-tile ring at three or more, 4 events and a three-tile ring at two
+// or more; else the geometry with the most resident threads per SM (few, short
+// state blocks: wide CTAs finish each sooner).  Tiles always stay large: smaller
+// tiles shorten the in-tile scans but cost more per tile than they save, even on
+// query-dense chains (measured).
 int geometry_override() {
   static const int g = [] {
     const char* v = std::getenv("BW_CHAIN_GEOMETRY");
@@ -664,18 +722,24 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
   s.C = a->n_keys;
   s.E = a->n_events;
   s.Q = a->n_queries;
-  s.nch = s.C > kFlatKeys ? (int32_t)((s.C + 31) >> 5) : 0;
+  // query-dense chains (more than one query per 64 events) keep chunk totals at any
+  // domain size: their intervals are probed often, and a probe over chunk totals
+  // reads ~width/1024 words per lane instead of ~width/128
+  const bool dense = s.Q * 64 > s.E;
+  s.nch = (s.C > kFlatKeys || dense) ? (int32_t)((s.C + 31) >> 5) : 0;
+  s.w64 = (a->flags & BW_REPLAY_WIDE) && s.C <= kChainMaxKeys64;
+  const int hw = s.w64 ? 8 : 4;
   int pin = geometry_override();
   int fit[kNumGeometries];
   size_t need[kNumGeometries];
   for (int g = 0; g < kNumGeometries; ++g) {
     const Geometry& G = kGeometries[g];
-    need[g] = sweep_smem(s.C, s.nch, G.threads * G.ept, G.stages).bytes;
+    need[g] = sweep_smem(s.C, s.nch, G.threads * G.ept, G.stages, hw).bytes;
     fit[g] = (int)(kSmemPerSM / (need[g] + 1024));
     if (fit[g] > G.minb) fit[g] = G.minb;
   }
   if (pin >= 0 && fit[pin] < 1) pin = -1;
-  if (pin < 0 && fit[6] >= 4 && s.E >= (int64_t)sms * fit[6] * kChainMinBlockEvents) pin = 6;
+  if (pin < 0 && fit[4] >= (s.w64 ? 3 : 4) && s.E >= (int64_t)sms * fit[4] * kChainMinBlockEvents) pin = 4;
   if (pin < 0 && fit[3] >= 3 && s.E >= (int64_t)sms * fit[3] * kChainMinBlockEvents) pin = 3;
   if (pin < 0 && fit[1] >= 2 && s.E >= (int64_t)sms * fit[1] * kChainMinBlockEvents) pin = 1;
   int best = -1, best_threads = 0;
@@ -716,13 +780,13 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
 int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int* kernels) {
   std::call_once(g_attr_once, [] {
     const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    g_attr_err = cudaFuncSetAttribute(k_chain_sweep<128, 4, 5, 3>, A, kSmemLimit);
-    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 4, 3, 3>, A, kSmemLimit);
-    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<512, 2, 2, 3>, A, kSmemLimit);
-    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 4, 4, 2>, A, kSmemLimit);
-    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 2, 4, 4>, A, kSmemLimit);
-    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<512, 2, 2, 2>, A, kSmemLimit);
-    if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(k_chain_sweep<256, 3, 4, 3>, A, kSmemLimit);
+    const void* fns[] = {(const void*)k_chain_sweep<128, 4, 5, 3, false>, (const void*)k_chain_sweep<256, 4, 3, 3, false>,
+                         (const void*)k_chain_sweep<512, 2, 2, 3, false>, (const void*)k_chain_sweep<256, 4, 4, 2, false>,
+                         (const void*)k_chain_sweep<256, 3, 4, 3, false>, (const void*)k_chain_sweep<128, 4, 5, 3, true>,
+                         (const void*)k_chain_sweep<256, 4, 3, 3, true>, (const void*)k_chain_sweep<512, 2, 2, 3, true>,
+                         (const void*)k_chain_sweep<256, 4, 4, 2, true>, (const void*)k_chain_sweep<256, 3, 4, 3, true>};
+    for (const void* f : fns)
+      if (g_attr_err == cudaSuccess) g_attr_err = cudaFuncSetAttribute(f, A, kSmemLimit);
   });
   if (g_attr_err != cudaSuccess) return report(g_attr_err, "chain sweep attribute");
   cudaStream_t st = static_cast<cudaStream_t>(a->stream);
@@ -750,14 +814,17 @@ int chain_enqueue(const ChainSpec& s, const BwReplayArgs* a, EventSet* evs, int*
     for (int i = 0; i <= BW_STAGE_SWEEP; ++i)
       if ((rc = report(cudaEventRecord(evs->ev[i], st), "event record"))) return rc;
   }
-  switch (s.geometry) {
-    case 0: k_chain_sweep<128, 4, 5, 3><<<s.B, 128, s.smem, st>>>(p); break;
-    case 1: k_chain_sweep<256, 4, 3, 3><<<s.B, 256, s.smem, st>>>(p); break;
-    case 2: k_chain_sweep<512, 2, 2, 3><<<s.B, 512, s.smem, st>>>(p); break;
-    case 3: k_chain_sweep<256, 4, 4, 2><<<s.B, 256, s.smem, st>>>(p); break;
-    case 4: k_chain_sweep<256, 2, 4, 4><<<s.B, 256, s.smem, st>>>(p); break;
-    case 5: k_chain_sweep<512, 2, 2, 2><<<s.B, 512, s.smem, st>>>(p); break;
-    default: k_chain_sweep<256, 3, 4, 3><<<s.B, 256, s.smem, st>>>(p); break;
+  switch (s.geometry * 2 + (s.w64 ? 1 : 0)) {
+    case 0: k_chain_sweep<128, 4, 5, 3, false><<<s.B, 128, s.smem, st>>>(p); break;
+    case 1: k_chain_sweep<128, 4, 5, 3, true><<<s.B, 128, s.smem, st>>>(p); break;
+    case 2: k_chain_sweep<256, 4, 3, 3, false><<<s.B, 256, s.smem, st>>>(p); break;
+    case 3: k_chain_sweep<256, 4, 3, 3, true><<<s.B, 256, s.smem, st>>>(p); break;
+    case 4: k_chain_sweep<512, 2, 2, 3, false><<<s.B, 512, s.smem, st>>>(p); break;
+    case 5: k_chain_sweep<512, 2, 2, 3, true><<<s.B, 512, s.smem, st>>>(p); break;
+    case 6: k_chain_sweep<256, 4, 4, 2, false><<<s.B, 256, s.smem, st>>>(p); break;
+    case 7: k_chain_sweep<256, 4, 4, 2, true><<<s.B, 256, s.smem, st>>>(p); break;
+    case 8: k_chain_sweep<256, 3, 4, 3, false><<<s.B, 256, s.smem, st>>>(p); break;
+    default: k_chain_sweep<256, 3, 4, 3, true><<<s.B, 256, s.smem, st>>>(p); break;
   }
   int k = 1;
   if ((rc = report(cudaGetLastError(), "chain sweep launch"))) return rc;

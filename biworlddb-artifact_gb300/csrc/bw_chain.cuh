@@ -23,6 +23,7 @@ constexpr int kChainThreads = 512;                              // largest sweep
 constexpr int kChainTile = 1024;                                // largest tile, events (16 KiB)
 constexpr int kChainQBuf = 64;                                  // query records staged per tile
 constexpr uint32_t kChainMaxKeys = 32768;                       // key domain held in shared memory
+constexpr uint32_t kChainMaxKeys64 = 16384;                     // ... with the int64 window
 constexpr int kChainSegRows = 16;                               // block rows per column-scan segment
 constexpr int64_t kChainMinBlockEvents = 8192;
 
@@ -34,6 +35,7 @@ struct ChainSpec {
   int32_t nch = 1;        // 32-key chunks of the window's chunk totals
   int32_t nseg = 1;       // column-scan segments
   int32_t ctas_per_sm = 1;
+  bool w64 = false;       // int64 window (BW_REPLAY_WIDE)
   int32_t geometry = 2;   // sweep geometry: index, threads per CTA, events per thread
   int32_t threads = 512;
   int32_t ept = 2;

@@ -135,7 +135,13 @@ int run_event_arm(const BwNativeWorkload* w, int32_t blocks, DeviceAnswers& out,
   a.queries = d_q;
   a.answers = d_ans;
   a.blocks = blocks;
-  a.flags = chain ? BW_REPLAY_CHAIN_HINT : 0;
+  // deltas mostly outside the chain path's int32-window range: int64 histogram
+  int64_t n_big = 0;
+  for (int64_t i = 0; i < w->n_events; ++i) {
+    const int64_t d = w->events[i].delta;
+    n_big += (d >= (1 << 19) || d <= -(1 << 19)) ? 1 : 0;
+  }
+  a.flags = chain ? (BW_REPLAY_CHAIN_HINT | (n_big * 64 > w->n_events ? BW_REPLAY_WIDE : 0)) : 0;
   size_t need = 0;
   BW_OR_5(bw_replay_workspace_size(&a, &need), "bw_replay_workspace_size");
   CUDA_OR_5(cudaMalloc(&ws, need ? need : 256));

@@ -218,6 +218,11 @@ typedef struct {
  * force either path instead (tests, benchmarks). */
 #define BW_REPLAY_CHAIN_KERNEL 4
 #define BW_REPLAY_GENERAL 8
+/* Chain path: keep the running key histogram as int64 (exact at any delta size, two
+ * 32-bit shared atomics per update) instead of int32 windows -- for chains whose
+ * deltas mostly lie outside (-2^19, 2^19), e.g. amount x factor products of the
+ * reference-native workloads.  Key domains up to 16,384 keys; ignored above. */
+#define BW_REPLAY_WIDE 16
 
 /* Pipeline stages timed under BW_REPLAY_TIMING, in order (the chain path has only
  * the sweep, which reads the events, and the carry scan with the answer fix-up that

@@ -33,9 +33,9 @@ def chain_case(seed, S, C, E, Q, zipf=1.1, delta="small"):
     return parent, C, ev, qs
 
 
-def run_chain(bw, torch, parent, C, ev, qs, blocks=0, path="chain"):
+def run_chain(bw, torch, parent, C, ev, qs, blocks=0, path="chain", wide=False):
     p, e, q = evgen.to_device(torch, parent, ev, qs)
-    r = bw.Replay(p, C, len(ev), len(qs), blocks=blocks, chain=True, path=path)
+    r = bw.Replay(p, C, len(ev), len(qs), blocks=blocks, chain=True, path=path, wide=wide)
     assert r.chain_path(e), "the chain path was not selected"
     ans = torch.empty(len(qs), dtype=torch.int64, device=p.device)
     r.launch(p, e, q, ans)
@@ -65,6 +65,17 @@ def test_chain_path_matches_oracle(bw, torch_cuda, oracle_mod, seed, S, C, E, Q,
     parent, C, ev, qs = chain_case(seed, S, C, E, Q, zipf, delta)
     want = oracle_mod.ev_blocks(parent, C, ev, qs, blocks=8)
     got, st = run_chain(bw, torch_cuda, parent, C, ev, qs, blocks=blocks)
+    assert st == 0
+    np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("seed,S,C,E,Q,zipf,delta,blocks", [c for c in CASES if c[2] <= 16384])
+def test_chain_path_int64_window_matches_oracle(bw, torch_cuda, oracle_mod, seed, S, C, E, Q, zipf, delta, blocks):
+    """BW_REPLAY_WIDE: the same cases through the int64 histogram (any delta size,
+    no window folds, no wide tiles)."""
+    parent, C, ev, qs = chain_case(seed, S, C, E, Q, zipf, delta)
+    want = oracle_mod.ev_blocks(parent, C, ev, qs, blocks=8)
+    got, st = run_chain(bw, torch_cuda, parent, C, ev, qs, blocks=blocks, wide=True)
     assert st == 0
     np.testing.assert_array_equal(got, want)
 

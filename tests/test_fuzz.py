@@ -129,7 +129,9 @@ def test_gpu_fuzz_replay(bw, torch_cuda, chunk):
         p, e, q = evgen.to_device(torch_cuda, w.parent, w.events, w.queries)
         variants = [dict(), dict(blocks=3)] + ([dict(chain=True), dict(chain=True, blocks=5),
                                                 dict(chain=True, path="chain"),
-                                                dict(chain=True, path="chain", blocks=4)] if w.chain else [])
+                                                dict(chain=True, path="chain", blocks=4),
+                                                dict(chain=True, path="chain", blocks=3, wide=True)]
+                                               if w.chain else [])
         for kw in variants:
             ans = bw.replay(p, w.n_keys, e, q, **kw).cpu().numpy()
             assert bw.sha256_hex(ans.tobytes()) == rec["answers_sha256"], (c.name, kw)

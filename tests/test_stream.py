@@ -88,13 +88,29 @@ def test_stream_rejects_malformed(bw):
     assert n_answers == 0 and len(w.queries) == 0 and len(w.events) > 0
 
 
+def test_wide_delta_rule(bw):
+    """The int64-window hint: more than one delta in 64 outside (-2^19, 2^19)."""
+    ev = np.zeros(640, dtype=[("state", "<u4"), ("key", "<u4"), ("delta", "<i8")])
+    assert not bw.wide_deltas(ev)
+    ev["delta"][:10] = 1 << 19          # 10 of 640: one in 64, not more
+    assert not bw.wide_deltas(ev)
+    ev["delta"][:11] = 1 << 19
+    assert bw.wide_deltas(ev)
+    ev["delta"][:11] = (1 << 19) - 1
+    assert not bw.wide_deltas(ev)
+    ev["delta"][:11] = -(1 << 19)
+    assert bw.wide_deltas(ev)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", SG["cases"], ids=case_id)
 def test_gpu_stream_replay(bw, torch_cuda, case):
     import evgen
     w, slot, n_answers = bw.stream_workload(FIXTURE, stream(case))
     p, e, q = evgen.to_device(torch_cuda, w.parent, w.events, w.queries)
+    assert bw.wide_deltas(w.events)   # amount x factor products: the int64 window's case
     for kw in (dict(chain=True), dict(chain=True, path="chain"), dict(chain=True, path="chain", blocks=7),
+               dict(chain=True, path="chain", wide=True), dict(chain=True, path="chain", blocks=5, wide=True),
                dict(chain=True, path="general"), dict()):
         got = bw.replay(p, w.n_keys, e, q, **kw).cpu().numpy()
         ans = bw.scatter_answers(got, slot, n_answers)
