@@ -85,6 +85,7 @@ struct Declared {
   std::vector<int64_t> ins_t;
   std::vector<int32_t> ins_g;
   std::vector<int64_t> endpoints;
+  std::vector<uint32_t> clo, chi;  // endpoint classes of qlo / qhi (class_of of each bound)
 };
 
 int32_t version_parent(int32_t topology, int32_t v) {
@@ -251,18 +252,57 @@ int validate(const BwFixture& f, const Declared& w, int32_t S) {
   return 0;
 }
 
-// Sorted distinct declared bounds (batch_engine_v7.hpp:362-442 dedupe).
+// Sorted distinct declared bounds (batch_engine_v7.hpp:362-442 dedupe) and the
+// endpoint class of every declared bound.  The bounds are sorted with their
+// positions by an LSD radix sort over 11-bit digits (passes whose digit is the same
+// in every key are skipped); a bound's class, the number of distinct bounds at or
+// below it, is then its rank among the distinct values + 1, so no per-query binary
+// search is needed.
 void collect_endpoints(Declared& w, int32_t S, int32_t q, bool per_state) {
-  w.endpoints.clear();
-  w.endpoints.reserve((size_t)(S - 1) * q * 2);
-  for (int32_t v = 1; v < S; ++v)
-    for (int32_t k = 0; k < q; ++k) {
-      const size_t qi = per_state ? (size_t)v * q + k : (size_t)k;
-      w.endpoints.push_back(w.qlo[qi]);
-      w.endpoints.push_back(w.qhi[qi]);
+  const size_t nq = per_state ? (size_t)S * q : (size_t)q;
+  const size_t lo_q = per_state ? (size_t)q : 0;   // first used slot (state 0 holds none)
+  const size_t n = 2 * (nq - lo_q);
+  std::vector<uint64_t> key(n), key2(n);
+  std::vector<uint32_t> pos(n), pos2(n);
+  for (size_t i = lo_q, j = 0; i < nq; ++i, j += 2) {
+    key[j] = (uint64_t)w.qlo[i] ^ (1ull << 63);   // order-preserving for int64
+    key[j + 1] = (uint64_t)w.qhi[i] ^ (1ull << 63);
+    pos[j] = (uint32_t)(2 * i);
+    pos[j + 1] = (uint32_t)(2 * i + 1);
+  }
+  uint64_t all_or = 0, all_and = ~0ull;
+  for (uint64_t k : key) {
+    all_or |= k;
+    all_and &= k;
+  }
+  std::vector<uint32_t> cnt(1u << 11);
+  for (int sh = 0; sh < 64; sh += 11) {
+    const uint64_t m = (1ull << 11) - 1;
+    if ((((all_or ^ all_and) >> sh) & m) == 0) continue;   // constant digit
+    std::fill(cnt.begin(), cnt.end(), 0u);
+    for (uint64_t k : key) ++cnt[(k >> sh) & m];
+    uint32_t run = 0;
+    for (uint32_t& c : cnt) {
+      const uint32_t t = c;
+      c = run;
+      run += t;
     }
-  std::sort(w.endpoints.begin(), w.endpoints.end());
-  w.endpoints.erase(std::unique(w.endpoints.begin(), w.endpoints.end()), w.endpoints.end());
+    for (size_t i = 0; i < n; ++i) {
+      const uint32_t d = cnt[(key[i] >> sh) & m]++;
+      key2[d] = key[i];
+      pos2[d] = pos[i];
+    }
+    key.swap(key2);
+    pos.swap(pos2);
+  }
+  w.endpoints.clear();
+  w.clo.assign(nq, 0);
+  w.chi.assign(nq, 0);
+  for (size_t i = 0; i < n; ++i) {
+    if (i == 0 || key[i] != key[i - 1]) w.endpoints.push_back((int64_t)(key[i] ^ (1ull << 63)));
+    const uint32_t cls = (uint32_t)w.endpoints.size();   // rank among the distinct bounds + 1
+    (pos[i] & 1 ? w.chi : w.clo)[pos[i] >> 1] = cls;
+  }
 }
 
 // Copy of a caller's explicit workload into the builder's form.
@@ -319,8 +359,21 @@ int build_events(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bo
   std::vector<int64_t> fac(G);
   for (int32_t g = 0; g < G; ++g) fac[g] = f.factor(g);
 
-  std::vector<BwEvent> ev;
-  ev.reserve((size_t)N + 2 * (size_t)S);
+  // upper bound of the event count: base rows, two per row edit, the group support
+  // of every factor edit
+  size_t cap = (size_t)N;
+  for (int32_t v = 1; v < S; ++v) cap += w.edit[v].op == OP_FACTOR ? gm[w.edit[v].g].cls.size() : 2;
+  bool chain = true;
+  for (int32_t v = 1; v < S && chain; ++v) chain = w.parent[v] == v - 1;
+  // a chain's preorder is state order: its events go straight to the output
+  BwEvent* evbuf = new (std::nothrow) BwEvent[cap ? cap : 1];
+  if (!evbuf) return 3;
+  struct EvSink {
+    BwEvent* p;
+    size_t n;
+    void push_back(const BwEvent& e) { p[n++] = e; }
+    size_t size() const { return n; }
+  } ev{evbuf, 0};
   int64_t n_factor = 0;
   // state 0: the base relation weighted by the fixture factors
   for (int64_t i = 0; i < N; ++i) {
@@ -402,9 +455,12 @@ int build_events(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bo
     }
   }
 
-  // group events by state (stable counting sort; chains are already in order)
+  // group events by state (stable counting sort; a chain's are already in order)
   BwNativeWorkload* o = new (std::nothrow) BwNativeWorkload();
-  if (!o) return 3;
+  if (!o) {
+    delete[] evbuf;
+    return 3;
+  }
   o->n_states = S;
   o->n_keys = (uint32_t)ep.size() + 1u;
   o->n_events = (int64_t)ev.size();
@@ -412,19 +468,21 @@ int build_events(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bo
   o->n_factor_events = n_factor;
   o->parent = new int32_t[S];
   std::memcpy(o->parent, w.parent.data(), sizeof(int32_t) * S);
-  o->events = new BwEvent[ev.empty() ? 1 : ev.size()];
-  {
+  if (chain) {
+    o->events = evbuf;
+  } else {
+    o->events = new BwEvent[ev.size() ? ev.size() : 1];
     std::vector<int64_t> off((size_t)S + 1, 0);
-    for (const BwEvent& x : ev) ++off[x.state + 1];
+    for (size_t i = 0; i < ev.size(); ++i) ++off[evbuf[i].state + 1];
     for (int32_t v = 0; v < S; ++v) off[v + 1] += off[v];
-    for (const BwEvent& x : ev) o->events[off[x.state]++] = x;
+    for (size_t i = 0; i < ev.size(); ++i) o->events[off[evbuf[i].state]++] = evbuf[i];
+    delete[] evbuf;
   }
   o->queries = new BwQuery[o->n_queries ? o->n_queries : 1];
   for (int32_t v = 1; v < S; ++v)
     for (int32_t k = 0; k < q; ++k) {
       const size_t qi = per_state ? (size_t)v * q + k : (size_t)k;
-      o->queries[(size_t)(v - 1) * q + k] = {(uint32_t)v, (uint32_t)class_of(w.qlo[qi]),
-                                             (uint32_t)class_of(w.qhi[qi])};
+      o->queries[(size_t)(v - 1) * q + k] = {(uint32_t)v, w.clo[qi], w.chi[qi]};
     }
   *out = o;
   return 0;
@@ -900,8 +958,8 @@ int build_v7(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bool p
   for (int32_t v = 1; v < S; ++v)
     for (int32_t k = 0; k < q; ++k) {
       const size_t qi = per_state ? (size_t)v * q + k : (size_t)k;
-      qlb[(size_t)v * q + k] = class_of(w.qlo[qi]);
-      qhb[(size_t)v * q + k] = class_of(w.qhi[qi]);
+      qlb[(size_t)v * q + k] = (int32_t)w.clo[qi];
+      qhb[(size_t)v * q + k] = (int32_t)w.chi[qi];
     }
 
   BwV7Plan* o = new (std::nothrow) BwV7Plan();
