@@ -941,10 +941,31 @@ def bench_csr(args):
     return 0
 
 
+def bench_reference_chain(args):
+    """``--workload reference_chain``: the reference's own GPU workload alone (its
+    300,000-state chain) through both worker arms and the warm replay, one JSON line."""
+    import torch
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    bw = load_pkg()
+    bw.build()
+    rec = reference_chain_record(args, bw, dev, args.steps)
+    w = rec["warm_replay"]
+    line = {"metric": "bit-exact range-sum answers/s (the reference's 300,000-state chain, warm replay)",
+            "value": w["answers_per_s"], "unit": "answers/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": w["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int64", "data": "synthetic", "config": {"workload": "reference_chain"},
+            **rec}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "reference_chain":
+        return bench_reference_chain(args)
     if args.workload == "csr_lut":
         return bench_csr(args)
     if args.workload == "batched_trees":

@@ -99,7 +99,7 @@ GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch", "gpu
                "bw_forest_launch_timed",
                "bw_serve_create", "bw_serve_reset", "bw_serve_run", "bw_serve_info", "bw_serve_destroy",
                "bw_forest_plan_stats", "bw_key_histogram", "bw_key_prefix", "bw_add_range_carry",
-               "bw_scatter_answers"]
+               "bw_scatter_answers", "bw_native_expand_workspace", "bw_native_expand"]
 
 _gpu = None
 
@@ -599,7 +599,7 @@ HOST_SYMBOLS = ["bw_fixture_open", "bw_fixture_from_memory", "bw_fixture_close",
                 "bw_native_build", "bw_native_free", "bw_native_build_declared", "bw_v7_plan_build",
                 "bw_v7_plan_build_declared", "bw_v7_plan_free", "bw_sha256_hex", "bw_fnv1a",
                 "bw_sha256_init", "bw_sha256_update", "bw_sha256_final", "bw_fnv1a_update",
-                "bw_stream_build", "bw_stream_free"]
+                "bw_stream_build", "bw_stream_free", "bw_native_build_compact", "bw_native_compact_free"]
 
 _host = None
 
@@ -755,6 +755,88 @@ def native_workload_declared(fixture: bytes, decl, name: str = "declared") -> "w
         chain = bool(np.all(par[1:] == np.arange(par.size - 1)))
         return _native_result(L, out, name, chain)
     return _with_fixture(fixture, run)
+
+
+class BwTimeline(C.Structure):
+    _fields_ = [("state", C.c_int32), ("idx", C.c_int32), ("value", C.c_int64), ("out", C.c_int64)]
+
+
+class BwNativeCompact(C.Structure):
+    _fields_ = [("n_states", C.c_int32), ("n_groups", C.c_int32), ("n_keys", C.c_uint32), ("n_events", C.c_int64),
+                ("n_queries", C.c_int64), ("parent", C.c_void_p), ("queries", C.c_void_p), ("n_fixed", C.c_int64),
+                ("fixed", C.c_void_p), ("fixed_pos", C.c_void_p), ("sup_off", C.c_void_p), ("sup_cls", C.c_void_p),
+                ("base_mass", C.c_void_p), ("tl_off", C.c_void_p), ("tl", C.POINTER(BwTimeline))]
+
+
+def native_compact(fixture: bytes, n_states: int, seed: int, factor_period: int, q: int, per_state: bool = True,
+                   factor_pct: int = -1) -> dict:
+    """The compact form of a reference-native chain (bw_native_build_compact) as numpy
+    arrays: verbatim events and their positions, group supports and base masses,
+    per-group timelines (mass updates, factor expansions)."""
+    import numpy as np
+
+    def run(L, fx):
+        L.bw_native_build_compact.argtypes = [C.c_void_p, C.POINTER(BwNativeSpec),
+                                              C.POINTER(C.POINTER(BwNativeCompact))]
+        L.bw_native_compact_free.argtypes = [C.POINTER(BwNativeCompact)]
+        spec = BwNativeSpec(n_states, 0, seed, factor_period, q, int(per_state), factor_pct)
+        out = C.POINTER(BwNativeCompact)()
+        rc = L.bw_native_build_compact(fx, C.byref(spec), C.byref(out))
+        if rc:
+            raise ValueError(f"compact chain build rejected (rc={rc})")
+        try:
+            c = out.contents
+            G = c.n_groups
+
+            def arr(ptr, dtype, n):
+                n = int(n)
+                return np.frombuffer(C.string_at(ptr, np.dtype(dtype).itemsize * n), dtype=dtype).copy() if n else \
+                    np.empty(0, dtype=dtype)
+            sup_off = arr(c.sup_off, np.int64, G + 1)
+            tl_off = arr(c.tl_off, np.int64, G + 1)
+            tl_dt = np.dtype([("state", "<i4"), ("idx", "<i4"), ("value", "<i8"), ("out", "<i8")])
+            return {"n_states": c.n_states, "n_groups": G, "n_keys": int(c.n_keys), "n_events": int(c.n_events),
+                    "parent": arr(c.parent, np.int32, c.n_states),
+                    "queries": arr(c.queries, workloads.QUERY_DTYPE, c.n_queries),
+                    "fixed": arr(c.fixed, workloads.EVENT_DTYPE, c.n_fixed),
+                    "fixed_pos": arr(c.fixed_pos, np.int64, c.n_fixed), "sup_off": sup_off,
+                    "sup_cls": arr(c.sup_cls, np.uint32, sup_off[-1]),
+                    "base_mass": arr(c.base_mass, np.int64, sup_off[-1]), "tl_off": tl_off,
+                    "tl": arr(C.cast(c.tl, C.c_void_p), tl_dt, tl_off[-1])}
+        finally:
+            L.bw_native_compact_free(out)
+    return _with_fixture(fixture, run)
+
+
+def expand_events(compact: dict, device=None):
+    """The compact chain's events on the device (bw_native_expand): an (n_events, 2)
+    int64 tensor, grouped by state."""
+    import numpy as np
+    torch = _torch()
+    L = gpu_lib()
+    L.bw_native_expand_workspace.argtypes = [C.POINTER(BwNativeCompact), C.POINTER(C.c_size_t)]
+    L.bw_native_expand.argtypes = [C.POINTER(BwNativeCompact), C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    keep = {k: np.ascontiguousarray(v) for k, v in compact.items() if isinstance(v, np.ndarray)}
+    c = BwNativeCompact()
+    c.n_states, c.n_groups, c.n_keys = compact["n_states"], compact["n_groups"], compact["n_keys"]
+    c.n_events, c.n_queries = compact["n_events"], len(keep["queries"])
+    c.n_fixed = len(keep["fixed"])
+
+    def ptr(k):
+        return keep[k].ctypes.data if keep[k].size else None
+    c.parent, c.queries, c.fixed, c.fixed_pos = ptr("parent"), ptr("queries"), ptr("fixed"), ptr("fixed_pos")
+    c.sup_off, c.sup_cls, c.base_mass, c.tl_off = ptr("sup_off"), ptr("sup_cls"), ptr("base_mass"), ptr("tl_off")
+    c.tl = C.cast(ptr("tl"), C.POINTER(BwTimeline))
+    need = C.c_size_t(0)
+    _check(L.bw_native_expand_workspace(C.byref(c), C.byref(need)), "bw_native_expand_workspace")
+    dev = device or torch.device("cuda")
+    ws = torch.empty(max(int(need.value), 256), dtype=torch.uint8, device=dev)
+    ev = torch.empty((max(compact["n_events"], 1), 2), dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    _check(L.bw_native_expand(C.byref(c), ev.data_ptr(), ws.data_ptr(), ws.numel(), stream.cuda_stream),
+           "bw_native_expand")
+    stream.synchronize()   # the host arrays are only needed until the copies are done
+    return ev[:compact["n_events"]]
 
 
 class BwStreamWorkload(C.Structure):

@@ -490,6 +490,165 @@ int build_events(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bo
 
 }  // namespace
 
+namespace {
+// The compact form of a chain's event model (see bw_native_build_compact): the same
+// sequential walk as build_events, with the factor expansion left to the device.
+int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bool per_state,
+                  BwNativeCompact** out) {
+  for (int32_t v = 1; v < S; ++v)
+    if (w.parent[v] != v - 1) return 2;
+  const int32_t G = f.G;
+  const int64_t N = f.n, M = N + (int64_t)w.ins_t.size();
+  const std::vector<int64_t>& ep = w.endpoints;
+  auto class_of = [&](int64_t t) {
+    return (int32_t)(std::upper_bound(ep.begin(), ep.end(), t) - ep.begin());
+  };
+  std::vector<RowImage> row((size_t)M);
+  std::vector<std::vector<int32_t>> sup(G);
+  for (int64_t i = 0; i < N; ++i) {
+    row[i] = {1, f.row_g(i), class_of(f.row_t(i)), f.row_amt(i)};
+    if (row[i].g < 0 || row[i].g >= G) return 3;
+    sup[row[i].g].push_back(row[i].c);
+  }
+  for (size_t k = 0; k < w.ins_t.size(); ++k) row[N + k] = {0, w.ins_g[k], class_of(w.ins_t[k]), 0};
+  for (int32_t v = 1; v < S; ++v) {
+    const Edit& e = w.edit[v];
+    if (e.op == OP_INSERT || e.op == OP_MOVE) sup[e.g].push_back(class_of(e.t));
+  }
+  std::vector<GroupMass> gm(G);
+  for (int32_t g = 0; g < G; ++g) {
+    std::sort(sup[g].begin(), sup[g].end());
+    sup[g].erase(std::unique(sup[g].begin(), sup[g].end()), sup[g].end());
+    gm[g].cls.swap(sup[g]);
+    gm[g].mass.assign(gm[g].cls.size(), 0);
+  }
+  std::vector<int64_t> fac(G);
+  for (int32_t g = 0; g < G; ++g) fac[g] = f.factor(g);
+  std::vector<BwEvent> fixed;
+  std::vector<int64_t> fixed_pos;
+  fixed.reserve((size_t)N + 2 * (size_t)S);
+  fixed_pos.reserve((size_t)N + 2 * (size_t)S);
+  int64_t pos = 0;
+  for (int64_t i = 0; i < N; ++i) {   // state 0: the base rows, weighted by the fixture factors
+    const RowImage& r = row[i];
+    GroupMass& m = gm[r.g];
+    m.mass[m.index(r.c)] += (uint64_t)r.amt;
+    const uint64_t d = (uint64_t)r.amt * (uint64_t)fac[r.g];
+    if (d) {
+      fixed.push_back({0u, (uint32_t)r.c, (int64_t)d});
+      fixed_pos.push_back(pos++);
+    }
+  }
+  std::vector<std::vector<BwTimeline>> tl(G);
+  for (int32_t v = 1; v < S; ++v) {
+    const Edit& e = w.edit[v];
+    if (e.op == OP_FACTOR) {
+      const uint64_t ds = (uint64_t)e.val - (uint64_t)fac[e.g];
+      if (ds && !gm[e.g].cls.empty()) {
+        tl[e.g].push_back({v, -1, (int64_t)ds, pos});
+        pos += (int64_t)gm[e.g].cls.size();
+      }
+      fac[e.g] = e.val;
+      continue;
+    }
+    RowImage& r = row[(size_t)e.id];
+    const RowImage old = r;
+    RowImage nw = old;
+    switch (e.op) {
+      case OP_REPLACE: nw.ex = 1; nw.amt = e.val; break;
+      case OP_DELETE: nw.ex = 0; break;
+      default: nw.ex = 1; nw.g = e.g; nw.c = class_of(e.t); nw.amt = e.val; break;  // insert, move
+    }
+    if (old.ex && old.amt != 0) {
+      fixed.push_back({(uint32_t)v, (uint32_t)old.c, (int64_t)((uint64_t)0 - (uint64_t)fac[old.g] * (uint64_t)old.amt)});
+      fixed_pos.push_back(pos++);
+    }
+    if (nw.ex && nw.amt != 0) {
+      fixed.push_back({(uint32_t)v, (uint32_t)nw.c, (int64_t)((uint64_t)fac[nw.g] * (uint64_t)nw.amt)});
+      fixed_pos.push_back(pos++);
+    }
+    if (old.ex) tl[old.g].push_back({v, (int32_t)gm[old.g].index(old.c), (int64_t)((uint64_t)0 - (uint64_t)old.amt), 0});
+    if (nw.ex) tl[nw.g].push_back({v, (int32_t)gm[nw.g].index(nw.c), nw.amt, 0});
+    r = nw;
+  }
+
+  BwNativeCompact* o = new (std::nothrow) BwNativeCompact();
+  if (!o) return 3;
+  o->n_states = S;
+  o->n_groups = G;
+  o->n_keys = (uint32_t)ep.size() + 1u;
+  o->n_events = pos;
+  o->n_queries = (int64_t)(S - 1) * q;
+  o->n_fixed = (int64_t)fixed.size();
+  size_t nsup = 0, ntl = 0;
+  for (int32_t g = 0; g < G; ++g) {
+    nsup += gm[g].cls.size();
+    ntl += tl[g].size();
+  }
+  o->parent = new (std::nothrow) int32_t[S];
+  o->queries = new (std::nothrow) BwQuery[o->n_queries ? o->n_queries : 1];
+  o->fixed = new (std::nothrow) BwEvent[fixed.size() ? fixed.size() : 1];
+  o->fixed_pos = new (std::nothrow) int64_t[fixed.size() ? fixed.size() : 1];
+  o->sup_off = new (std::nothrow) int64_t[G + 1];
+  o->sup_cls = new (std::nothrow) uint32_t[nsup ? nsup : 1];
+  o->base_mass = new (std::nothrow) int64_t[nsup ? nsup : 1];
+  o->tl_off = new (std::nothrow) int64_t[G + 1];
+  o->tl = new (std::nothrow) BwTimeline[ntl ? ntl : 1];
+  if (!o->parent || !o->queries || !o->fixed || !o->fixed_pos || !o->sup_off || !o->sup_cls || !o->base_mass ||
+      !o->tl_off || !o->tl) {
+    bw_native_compact_free(o);
+    return 3;
+  }
+  std::memcpy(o->parent, w.parent.data(), sizeof(int32_t) * S);
+  std::memcpy(o->fixed, fixed.data(), fixed.size() * sizeof(BwEvent));
+  std::memcpy(o->fixed_pos, fixed_pos.data(), fixed_pos.size() * 8);
+  size_t a = 0, b = 0;
+  for (int32_t g = 0; g < G; ++g) {
+    o->sup_off[g] = (int64_t)a;
+    o->tl_off[g] = (int64_t)b;
+    for (size_t i = 0; i < gm[g].cls.size(); ++i, ++a) {
+      o->sup_cls[a] = (uint32_t)gm[g].cls[i];
+      o->base_mass[a] = (int64_t)gm[g].mass[i];   // the walk leaves the state-0 masses as they are
+    }
+    for (const BwTimeline& x : tl[g]) o->tl[b++] = x;
+  }
+  o->sup_off[G] = (int64_t)a;
+  o->tl_off[G] = (int64_t)b;
+  for (int32_t v = 1; v < S; ++v)
+    for (int32_t k = 0; k < q; ++k) {
+      const size_t qi = per_state ? (size_t)v * q + k : (size_t)k;
+      o->queries[(size_t)(v - 1) * q + k] = {(uint32_t)v, w.clo[qi], w.chi[qi]};
+    }
+  *out = o;
+  return 0;
+}
+}  // namespace
+
+extern "C" int bw_native_build_compact(const BwFixture* fx, const BwNativeSpec* sp, BwNativeCompact** out) {
+  if (!fx || !sp || !out || sp->n_states < 2 || sp->q < 1 || sp->topology < 0 || sp->topology > 2)
+    return 2;
+  if (sp->topology != 0) return 2;
+  Declared w;
+  declare(*fx, *sp, w);
+  collect_endpoints(w, sp->n_states, sp->q, sp->per_state != 0);
+  const int rc = validate(*fx, w, sp->n_states);
+  return rc ? rc : build_compact(*fx, w, sp->n_states, sp->q, sp->per_state != 0, out);
+}
+
+extern "C" void bw_native_compact_free(BwNativeCompact* c) {
+  if (!c) return;
+  delete[] c->parent;
+  delete[] c->queries;
+  delete[] c->fixed;
+  delete[] c->fixed_pos;
+  delete[] c->sup_off;
+  delete[] c->sup_cls;
+  delete[] c->base_mass;
+  delete[] c->tl_off;
+  delete[] c->tl;
+  delete c;
+}
+
 extern "C" int bw_native_build(const BwFixture* fx, const BwNativeSpec* sp, BwNativeWorkload** out) {
   if (!fx || !sp || !out || sp->n_states < 2 || sp->q < 1 || sp->topology < 0 || sp->topology > 2)
     return 2;

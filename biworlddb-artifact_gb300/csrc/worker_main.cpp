@@ -107,17 +107,23 @@ int upload(T** dst, const T* src, size_t n) {
 }
 
 // The event-model replay of a declared workload (any topology).
-int run_event_arm(const BwNativeWorkload* w, int32_t blocks, DeviceAnswers& out, Timings& tm) {
+// wide: the chain path's int64 histogram (deltas mostly outside the int32 window);
+// d_events: events already on the device (the device-side chain setup), else they
+// are uploaded from w->events.
+int run_event_arm(const BwNativeWorkload* w, int32_t blocks, bool wide, BwEvent* d_events, DeviceAnswers& out,
+                  Timings& tm) {
   const auto u0 = clk::now();
   int32_t* d_parent = nullptr;
-  BwEvent* d_ev = nullptr;
+  BwEvent* d_ev = d_events;
   BwQuery* d_q = nullptr;
   int64_t* d_ans = nullptr;
   void* ws = nullptr;
   int rc = upload(&d_parent, w->parent, (size_t)w->n_states);
   out.owned.push_back(d_parent);
-  if (!rc) rc = upload(&d_ev, w->events, (size_t)w->n_events);
-  out.owned.push_back(d_ev);
+  if (!rc && !d_ev) {
+    rc = upload(&d_ev, w->events, (size_t)w->n_events);
+    out.owned.push_back(d_ev);
+  }
   if (!rc) rc = upload(&d_q, w->queries, (size_t)w->n_queries);
   out.owned.push_back(d_q);
   if (rc) return rc;
@@ -135,13 +141,7 @@ int run_event_arm(const BwNativeWorkload* w, int32_t blocks, DeviceAnswers& out,
   a.queries = d_q;
   a.answers = d_ans;
   a.blocks = blocks;
-  // deltas mostly outside the chain path's int32-window range: int64 histogram
-  int64_t n_big = 0;
-  for (int64_t i = 0; i < w->n_events; ++i) {
-    const int64_t d = w->events[i].delta;
-    n_big += (d >= (1 << 19) || d <= -(1 << 19)) ? 1 : 0;
-  }
-  a.flags = chain ? (BW_REPLAY_CHAIN_HINT | (n_big * 64 > w->n_events ? BW_REPLAY_WIDE : 0)) : 0;
+  a.flags = chain ? (BW_REPLAY_CHAIN_HINT | (wide ? BW_REPLAY_WIDE : 0)) : 0;
   size_t need = 0;
   BW_OR_5(bw_replay_workspace_size(&a, &need), "bw_replay_workspace_size");
   CUDA_OR_5(cudaMalloc(&ws, need ? need : 256));
@@ -178,6 +178,14 @@ int run_event_arm(const BwNativeWorkload* w, int32_t blocks, DeviceAnswers& out,
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return 0;
+}
+
+// More than one delta in 64 outside (-2^19, 2^19): the chain path's int32 windows
+// would take the wide-tile route most of the time, so its int64 histogram is used.
+bool wide_deltas(const BwEvent* ev, int64_t n) {
+  int64_t big = 0;
+  for (int64_t i = 0; i < n; ++i) big += (ev[i].delta >= (1 << 19) || ev[i].delta <= -(1 << 19)) ? 1 : 0;
+  return big * 64 > n;
 }
 
 // The gpu_v7.h drop-in path on the reference's v7 chain plan.
@@ -428,6 +436,19 @@ int main(int argc, char** argv) {
   BwNativeWorkload* w = nullptr;
   BwV7Plan* plan = nullptr;
   BwStreamWorkload* sw = nullptr;
+  BwNativeCompact* cp = nullptr;   // device-side chain setup
+  BwNativeWorkload cw{};           // its chain view (events on the device)
+  BwEvent* d_events = nullptr;
+  void* d_xws = nullptr;
+  bool wide = false;
+  const char* dev_setup = std::getenv("BWH_DEVICE_SETUP");
+  const bool device_setup = arm == "gb300" && events_path.empty() && topology == 0 &&
+                            !(dev_setup && std::strcmp(dev_setup, "0") == 0);
+  if (device_setup) {   // the CUDA context is process start-up, not a workload phase
+    CUDA_OR_5(cudaSetDevice(0));
+    CUDA_OR_5(cudaFree(nullptr));
+  }
+  const auto t1s = clk::now();
   if (!events_path.empty()) {
     std::ifstream in(events_path, std::ios::binary);
     const std::vector<char> img((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
@@ -442,6 +463,28 @@ int main(int argc, char** argv) {
     w = &sw->chain;
     q = sw->q;
     if (q > 0) states = (int32_t)(sw->n_answers / q) + 1;
+  } else if (device_setup) {
+    // chain setup on the device: compact form on the host, factor expansion on the GPU
+    if (bw_native_build_compact(fx, &spec, &cp)) {
+      std::fprintf(stderr, "workload build failed (unsupported case)\n");
+      return 3;
+    }
+    size_t xbytes = 0;
+    BW_OR_5(bw_native_expand_workspace(cp, &xbytes), "bw_native_expand_workspace");
+    CUDA_OR_5(cudaMalloc(&d_xws, xbytes ? xbytes : 256));
+    CUDA_OR_5(cudaMalloc(&d_events, (size_t)(cp->n_events ? cp->n_events : 1) * sizeof(BwEvent)));
+    BW_OR_5(bw_native_expand(cp, d_events, d_xws, xbytes ? xbytes : 256, nullptr), "bw_native_expand");
+    CUDA_OR_5(cudaDeviceSynchronize());
+    CUDA_OR_5(cudaFree(d_xws));
+    d_xws = nullptr;
+    cw.n_states = cp->n_states;
+    cw.n_keys = cp->n_keys;
+    cw.n_events = cp->n_events;
+    cw.n_queries = cp->n_queries;
+    cw.parent = cp->parent;
+    cw.queries = cp->queries;
+    w = &cw;
+    wide = wide_deltas(cp->fixed, cp->n_fixed);
   } else if (arm == "gb300") {
     if (bw_native_build(fx, &spec, &w)) {
       std::fprintf(stderr, "workload build failed (unsupported case)\n");
@@ -461,7 +504,9 @@ int main(int argc, char** argv) {
   DeviceAnswers da;
   Timings tm;
   const auto te0 = clk::now();
-  const int rc = arm == "gb300" ? run_event_arm(w, blocks, da, tm) : run_v7_arm(plan, da, tm);
+  if (w && !cp) wide = wide_deltas(w->events, w->n_events);
+  if (d_events) da.owned.push_back(d_events);
+  const int rc = arm == "gb300" ? run_event_arm(w, blocks, wide, d_events, da, tm) : run_v7_arm(plan, da, tm);
   if (rc) return rc;
   if (sw) {   // chain answers (stream order) -> the (state, k) answer vector
     int64_t *d_slot = nullptr, *d_out = nullptr;
@@ -495,12 +540,13 @@ int main(int argc, char** argv) {
   for (void* b : da.owned) cudaFree(b);
   da.owned.clear();
   if (sw) bw_stream_free(sw);
+  else if (cp) bw_native_compact_free(cp);
   else if (w) bw_native_free(w);
   if (plan) bw_v7_plan_free(plan);
   bw_fixture_close(fx);
   const auto t5 = clk::now();
 
-  const int64_t load_ns = ns_between(t0, t1), setup_ns = ns_between(t1, t2), execute_ns = ns_between(te0, t3),
+  const int64_t load_ns = ns_between(t0, t1), setup_ns = ns_between(t1s, t2), execute_ns = ns_between(te0, t3),
                 extract_ns = ns_between(t3, t4), cleanup_ns = ns_between(t4, t5);
   const int64_t full_ns = load_ns + setup_ns + execute_ns + extract_ns + cleanup_ns;
   const int64_t kernel_total = tm.kernel + tm.carry + tm.combine;

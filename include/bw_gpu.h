@@ -315,6 +315,47 @@ int bw_add_range_carry(const BwQuery* queries, int64_t n, uint32_t n_keys, const
 int bw_scatter_answers(const int64_t* src, const int64_t* slot, int64_t n, int64_t* dst, int64_t n_dst,
                        void* stream);
 
+/* ============================================================ chain setup on the device
+ * The factor expansion of a reference-native chain (the bulk of its events: a factor
+ * edit of group g becomes one event per class of g's support) built on the GPU.
+ * The host compiles the chain into this compact form (bw_native_build_compact,
+ * include/bw_host.h): the events that are copied verbatim (base rows and row edits)
+ * with their output positions, every group's support and base mass, and per group
+ * the timeline of its mass updates and factor expansions in state order.  The
+ * device applies a group's updates between expansions (they commute) and writes
+ * each expansion (state, class, ds * mass) at its output range. */
+typedef struct {
+  int32_t state;
+  int32_t idx;        /* support index of a mass update; -1 for an expansion */
+  int64_t value;      /* mass delta, or the expansion's factor delta ds */
+  int64_t out;        /* expansion: output position of its first event */
+} BwTimeline;
+
+typedef struct {
+  int32_t n_states, n_groups;
+  uint32_t n_keys;
+  int64_t n_events;       /* events the expansion writes in all */
+  int64_t n_queries;
+  int32_t* parent;        /* n_states (a chain) */
+  BwQuery* queries;       /* n_queries, reference answer order */
+  int64_t n_fixed;
+  BwEvent* fixed;         /* events copied verbatim ... */
+  int64_t* fixed_pos;     /* ... to these output positions */
+  int64_t* sup_off;       /* n_groups + 1 */
+  uint32_t* sup_cls;      /* group g's classes: sup_cls[sup_off[g] .. sup_off[g+1]) */
+  int64_t* base_mass;     /* parallel to sup_cls */
+  int64_t* tl_off;        /* n_groups + 1 */
+  BwTimeline* tl;         /* group g's timeline: tl[tl_off[g] .. tl_off[g+1]) */
+} BwNativeCompact;
+
+/* Device scratch for bw_native_expand (the compact arrays and per-group masses). */
+int bw_native_expand_workspace(const BwNativeCompact* c, size_t* bytes);
+/* Upload the compact form (host arrays) into `workspace` and write all n_events
+ * events, grouped by state, to `events` (device).  Enqueued on `stream`; the host
+ * arrays must stay valid until the stream reaches this point. */
+int bw_native_expand(const BwNativeCompact* c, BwEvent* events, void* workspace, size_t workspace_bytes,
+                     void* stream);
+
 /* ============================================================ batched version forests
  * Thousands of independent version trees replayed in one pipeline (the reference
  * replays one chain per worker process, panel_batch_gpu.cpp:182-214, and its

@@ -64,6 +64,13 @@ typedef struct {          /* host arrays owned by the library */
 int bw_native_build(const BwFixture* f, const BwNativeSpec* spec, BwNativeWorkload** out);
 void bw_native_free(BwNativeWorkload* w);
 
+/* The same declared workload for a chain (topology 0) in the compact form whose
+ * factor expansion the device performs (bw_native_expand, include/bw_gpu.h): the
+ * expanded event list equals bw_native_build's apart from extra zero-delta events
+ * (classes whose mass is zero at the factor edit).  2 for a tree. */
+int bw_native_build_compact(const BwFixture* f, const BwNativeSpec* spec, BwNativeCompact** out);
+void bw_native_compact_free(BwNativeCompact* c);
+
 /* An explicit declared workload: the reference's Workload (common.hpp:177-212) as a
  * caller fills it directly, e.g. the reference's randomized branching fuzz
  * (fuzz_fullpath.cpp:196-283), instead of drawing it from (topology, seed, factor
