@@ -652,7 +652,7 @@ class Digest:
     FNV_BASIS = 1469598103934665603
 
     def __init__(self):
-        self._state = C.create_string_buffer(8 * 4 + 8 + 64 + 8)   # BwSha256, padded
+        self._state = C.create_string_buffer(256)   # a BwSha256 (128 bytes), with room to spare
         host_lib().bw_sha256_init(self._state)
         self._fnv = self.FNV_BASIS
 

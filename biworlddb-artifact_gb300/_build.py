@@ -90,10 +90,10 @@ def build(force: bool = False, verbose: bool = False) -> None:
     if gpu_objs:
         subprocess.run([nvcc, *ARCH, "-shared", "-o", str(GPU_LIB), *map(str, gpu_objs)], check=True)
     if host_objs:
-        subprocess.run(["g++", "-shared", "-fopenmp", "-o", str(HOST_LIB), *map(str, host_objs)],
+        subprocess.run(["g++", "-shared", "-fopenmp", "-o", str(HOST_LIB), *map(str, host_objs), "-ldl"],
                        check=True)
         # the worker: host objects linked in, the CUDA library by rpath
         subprocess.run([nvcc, *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fopenmp,-ffp-contract=off",
                         "-I", str(INCLUDE), "-I", str(CSRC), str(CSRC / "worker_main.cpp"), *map(str, host_objs),
-                        "-L", str(PKG), "-lbwgpu", "-lgomp", f"-Xlinker=-rpath,{PKG}", "-o", str(WORKER)],
+                        "-L", str(PKG), "-lbwgpu", "-lgomp", "-ldl", f"-Xlinker=-rpath,{PKG}", "-o", str(WORKER)],
                        check=True)

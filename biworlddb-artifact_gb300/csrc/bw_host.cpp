@@ -8,6 +8,7 @@
 // so factor edits expand to exactly the deltas the reference's executor adds.
 #include "bw_host.h"
 
+#include <dlfcn.h>
 #include <fcntl.h>
 #include <sys/mman.h>
 #include <sys/stat.h>
@@ -884,20 +885,80 @@ const Sha256Consts& sha_consts() {
   return c;
 }
 inline uint32_t rotr(uint32_t x, int n) { return (x >> n) | (x << (32 - n)); }
+inline uint32_t big_sigma0(uint32_t x) { return rotr(x, 2) ^ rotr(x, 13) ^ rotr(x, 22); }
+inline uint32_t big_sigma1(uint32_t x) { return rotr(x, 6) ^ rotr(x, 11) ^ rotr(x, 25); }
+inline uint32_t small_sigma0(uint32_t x) { return rotr(x, 7) ^ rotr(x, 18) ^ (x >> 3); }
+inline uint32_t small_sigma1(uint32_t x) { return rotr(x, 17) ^ rotr(x, 19) ^ (x >> 10); }
+// One FIPS 180-4 round: the working variables are renamed instead of moved (the
+// callers rotate the argument order), t1 lands in d and t1 + t2 in h.
+#define BW_SHA_ROUND(a, b, c, d, e, f, g, h, i)                                           \
+  do {                                                                                    \
+    const uint32_t t1 = h + big_sigma1(e) + (g ^ (e & (f ^ g))) + K[i] + w[(i) & 15];    \
+    d += t1;                                                                              \
+    h = t1 + big_sigma0(a) + ((a & b) | (c & (a | b)));                                   \
+  } while (0)
+// The message schedule kept as a rolling window of 16 words.
 void sha_compress(uint32_t h[8], const uint8_t* p, const uint32_t* K) {
-  uint32_t w[64];
+  uint32_t w[16];
   for (int i = 0; i < 16; ++i)
     w[i] = ((uint32_t)p[4 * i] << 24) | ((uint32_t)p[4 * i + 1] << 16) | ((uint32_t)p[4 * i + 2] << 8) | p[4 * i + 3];
-  for (int i = 16; i < 64; ++i)
-    w[i] = w[i - 16] + (rotr(w[i - 15], 7) ^ rotr(w[i - 15], 18) ^ (w[i - 15] >> 3)) + w[i - 7] +
-           (rotr(w[i - 2], 17) ^ rotr(w[i - 2], 19) ^ (w[i - 2] >> 10));
   uint32_t a = h[0], b = h[1], c = h[2], d = h[3], e = h[4], f = h[5], g = h[6], hh = h[7];
-  for (int i = 0; i < 64; ++i) {
-    const uint32_t t1 = hh + (rotr(e, 6) ^ rotr(e, 11) ^ rotr(e, 25)) + ((e & f) ^ (~e & g)) + K[i] + w[i];
-    const uint32_t t2 = (rotr(a, 2) ^ rotr(a, 13) ^ rotr(a, 22)) + ((a & b) ^ (a & c) ^ (b & c));
-    hh = g; g = f; f = e; e = d + t1; d = c; c = b; b = a; a = t1 + t2;
+  for (int i = 0; i < 64; i += 8) {
+    if (i >= 16)
+      for (int j = i; j < i + 8; ++j)
+        w[j & 15] += small_sigma1(w[(j - 2) & 15]) + w[(j - 7) & 15] + small_sigma0(w[(j - 15) & 15]);
+    BW_SHA_ROUND(a, b, c, d, e, f, g, hh, i + 0);
+    BW_SHA_ROUND(hh, a, b, c, d, e, f, g, i + 1);
+    BW_SHA_ROUND(g, hh, a, b, c, d, e, f, i + 2);
+    BW_SHA_ROUND(f, g, hh, a, b, c, d, e, i + 3);
+    BW_SHA_ROUND(e, f, g, hh, a, b, c, d, i + 4);
+    BW_SHA_ROUND(d, e, f, g, hh, a, b, c, i + 5);
+    BW_SHA_ROUND(c, d, e, f, g, hh, a, b, i + 6);
+    BW_SHA_ROUND(b, c, d, e, f, g, hh, a, i + 7);
   }
   h[0] += a; h[1] += b; h[2] += c; h[3] += d; h[4] += e; h[5] += f; h[6] += g; h[7] += hh;
+}
+#undef BW_SHA_ROUND
+}  // namespace
+
+// The platform's SHA-256 through OpenSSL's EVP interface, found at run time
+// (dlopen, no header or link dependency), as the reference's extract phase uses
+// OpenSSL's SHA256 (sha_fast.hpp:1-40); BW_SHA=sw, or no libcrypto, selects the
+// portable implementation above.  Both give the same digest.
+namespace {
+struct Evp {
+  void* (*ctx_new)() = nullptr;
+  void (*ctx_free)(void*) = nullptr;
+  const void* (*sha256)() = nullptr;
+  int (*init)(void*, const void*, void*) = nullptr;
+  int (*update)(void*, const void*, size_t) = nullptr;
+  int (*final_)(void*, unsigned char*, unsigned int*) = nullptr;
+  bool ok = false;
+};
+const Evp& evp() {
+  static const Evp e = [] {
+    Evp x;
+    const char* mode = std::getenv("BW_SHA");
+    if (mode && std::strcmp(mode, "sw") == 0) return x;
+    void* h = dlopen("libcrypto.so.3", RTLD_NOW | RTLD_LOCAL);
+    if (!h) h = dlopen("libcrypto.so", RTLD_NOW | RTLD_LOCAL);
+    if (!h) return x;
+    x.ctx_new = reinterpret_cast<void* (*)()>(dlsym(h, "EVP_MD_CTX_new"));
+    x.ctx_free = reinterpret_cast<void (*)(void*)>(dlsym(h, "EVP_MD_CTX_free"));
+    x.sha256 = reinterpret_cast<const void* (*)()>(dlsym(h, "EVP_sha256"));
+    x.init = reinterpret_cast<int (*)(void*, const void*, void*)>(dlsym(h, "EVP_DigestInit_ex"));
+    x.update = reinterpret_cast<int (*)(void*, const void*, size_t)>(dlsym(h, "EVP_DigestUpdate"));
+    x.final_ = reinterpret_cast<int (*)(void*, unsigned char*, unsigned int*)>(dlsym(h, "EVP_DigestFinal_ex"));
+    x.ok = x.ctx_new && x.ctx_free && x.sha256 && x.init && x.update && x.final_;
+    return x;
+  }();
+  return e;
+}
+void sha_hex(const uint32_t h[8], char out_hex[65]) {
+  static const char* hx = "0123456789abcdef";
+  for (int i = 0; i < 8; ++i)
+    for (int j = 0; j < 8; ++j) out_hex[8 * i + j] = hx[(h[i] >> (28 - 4 * j)) & 15];
+  out_hex[64] = 0;
 }
 }  // namespace
 
@@ -905,9 +966,27 @@ extern "C" void bw_sha256_init(BwSha256* s) {
   std::memcpy(s->h, sha_consts().h0, sizeof(s->h));
   s->bytes = 0;
   s->fill = 0;
+  s->hw = nullptr;
+  const Evp& e = evp();
+  if (e.ok) {
+    void* ctx = e.ctx_new();
+    if (ctx && e.init(ctx, e.sha256(), nullptr) == 1) s->hw = ctx;
+    else if (ctx) e.ctx_free(ctx);
+  }
 }
 
 extern "C" void bw_sha256_update(BwSha256* s, const void* data, size_t n) {
+  if (s->hw) {
+    s->bytes += n;
+    if (n && evp().update(s->hw, data, n) == 1) return;
+    if (!n) return;
+    // the platform digest failed mid-stream: no way to resume it in software
+    evp().ctx_free(s->hw);
+    s->hw = nullptr;
+    s->fill = 0xffffffffu;   // poisoned: final reports an all-zero digest
+    return;
+  }
+  if (s->fill == 0xffffffffu) return;
   const uint32_t* K = sha_consts().k;
   const uint8_t* p = static_cast<const uint8_t*>(data);
   s->bytes += n;
@@ -927,6 +1006,25 @@ extern "C" void bw_sha256_update(BwSha256* s, const void* data, size_t n) {
 }
 
 extern "C" void bw_sha256_final(BwSha256* s, char out_hex[65]) {
+  if (s->hw) {
+    unsigned char md[32];
+    unsigned int len = 0;
+    const bool ok = evp().final_(s->hw, md, &len) == 1 && len == 32;
+    evp().ctx_free(s->hw);
+    s->hw = nullptr;
+    uint32_t h[8] = {0};
+    if (ok)
+      for (int i = 0; i < 8; ++i)
+        h[i] = ((uint32_t)md[4 * i] << 24) | ((uint32_t)md[4 * i + 1] << 16) | ((uint32_t)md[4 * i + 2] << 8) |
+               md[4 * i + 3];
+    sha_hex(h, out_hex);
+    return;
+  }
+  if (s->fill == 0xffffffffu) {
+    const uint32_t z[8] = {0};
+    sha_hex(z, out_hex);
+    return;
+  }
   const uint32_t* K = sha_consts().k;
   uint8_t tail[128] = {0};
   const size_t rem = s->fill;
@@ -937,10 +1035,7 @@ extern "C" void bw_sha256_final(BwSha256* s, char out_hex[65]) {
   for (int i = 0; i < 8; ++i) tail[tl - 1 - i] = (uint8_t)(bits >> (8 * i));
   sha_compress(s->h, tail, K);
   if (tl == 128) sha_compress(s->h, tail + 64, K);
-  static const char* hx = "0123456789abcdef";
-  for (int i = 0; i < 8; ++i)
-    for (int j = 0; j < 8; ++j) out_hex[8 * i + j] = hx[(s->h[i] >> (28 - 4 * j)) & 15];
-  out_hex[64] = 0;
+  sha_hex(s->h, out_hex);
 }
 
 extern "C" void bw_sha256_hex(const void* data, size_t n, char out_hex[65]) {

@@ -163,6 +163,8 @@ typedef struct BwSha256 {
   uint64_t bytes;      /* bytes fed so far */
   uint8_t buf[64];     /* pending partial block */
   uint32_t fill;
+  void* hw;            /* the platform digest in use (OpenSSL EVP, found at run time), else NULL;
+                          bw_sha256_final releases it.  BW_SHA=sw forces the portable code. */
 } BwSha256;
 void bw_sha256_init(BwSha256* s);
 void bw_sha256_update(BwSha256* s, const void* data, size_t n);

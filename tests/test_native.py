@@ -74,6 +74,27 @@ def test_streaming_digest_equals_one_shot(bw):
     assert bw.Digest().final()[0] == bw.sha256_hex(b"")
 
 
+def test_platform_and_portable_sha_agree(bw, tmp_path):
+    """The digest uses the platform SHA-256 (OpenSSL EVP, found at run time) unless
+    BW_SHA=sw selects the portable FIPS 180-4 code: both give hashlib's digest."""
+    import hashlib
+    import os
+    import subprocess
+    import sys
+    data = np.random.default_rng(9).integers(0, 256, 1_000_003, dtype=np.uint8).tobytes()
+    (tmp_path / "d.bin").write_bytes(data)
+    code = ("import importlib, sys; sys.path.insert(0, sys.argv[1]); "
+            "bw = importlib.import_module('biworlddb-artifact_gb300'); "
+            "d = bw.Digest(); b = open(sys.argv[2], 'rb').read(); d.update(b[:777]); d.update(b[777:]); "
+            "print(bw.sha256_hex(b), d.final()[0])")
+    root = str(Path(__file__).resolve().parent.parent)
+    for mode in ("sw", "hw"):
+        env = dict(os.environ, BW_SHA=mode)
+        out = subprocess.run([sys.executable, "-c", code, root, str(tmp_path / "d.bin")], env=env,
+                             capture_output=True, text=True, check=True).stdout.split()
+        assert out == [hashlib.sha256(data).hexdigest()] * 2, mode
+
+
 def test_front_end_rejects_bad_fixture(bw):
     img = bytearray(fixture("check"))
     img[0:8] = b"BWBASE99"
