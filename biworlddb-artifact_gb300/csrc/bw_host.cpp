@@ -124,6 +124,8 @@ void declare(const BwFixture& f, const BwNativeSpec& sp, Declared& w) {
   if (sp.per_state) {
     w.qlo.assign((size_t)S * q, 0);
     w.qhi.assign((size_t)S * q, 0);
+    // every state's ranges come from their own seed: independent, drawn in parallel
+#pragma omp parallel for schedule(static)
     for (int32_t v = 1; v < S; ++v) {
       Rng r(seed * 1000000007ULL + topo * 65537ULL + fp * 131ULL + (uint64_t)v * 2654435761ULL + 17ULL);
       nested(r, tmin, tmax, q, &w.qlo[(size_t)v * q], &w.qhi[(size_t)v * q]);
@@ -276,22 +278,37 @@ void collect_endpoints(Declared& w, int32_t S, int32_t q, bool per_state) {
     all_or |= k;
     all_and &= k;
   }
-  std::vector<uint32_t> cnt(1u << 11);
-  for (int sh = 0; sh < 64; sh += 11) {
-    const uint64_t m = (1ull << 11) - 1;
+  // each pass: per-part digit histograms, their exclusive scan in (digit, part)
+  // order, then a stable scatter of every part from its own offsets (parts are
+  // contiguous key ranges, so the order within a digit is preserved)
+  constexpr int kBits = 11, kDigits = 1 << kBits;
+  const int parts = n < (1u << 16) ? 1 : 16;
+  std::vector<uint32_t> cnt((size_t)parts * kDigits);
+  for (int sh = 0; sh < 64; sh += kBits) {
+    const uint64_t m = kDigits - 1;
     if ((((all_or ^ all_and) >> sh) & m) == 0) continue;   // constant digit
     std::fill(cnt.begin(), cnt.end(), 0u);
-    for (uint64_t k : key) ++cnt[(k >> sh) & m];
-    uint32_t run = 0;
-    for (uint32_t& c : cnt) {
-      const uint32_t t = c;
-      c = run;
-      run += t;
+#pragma omp parallel for schedule(static) num_threads(parts)
+    for (int t = 0; t < parts; ++t) {
+      uint32_t* c = &cnt[(size_t)t * kDigits];
+      for (size_t i = n * t / parts; i < n * (t + 1) / parts; ++i) ++c[(key[i] >> sh) & m];
     }
-    for (size_t i = 0; i < n; ++i) {
-      const uint32_t d = cnt[(key[i] >> sh) & m]++;
-      key2[d] = key[i];
-      pos2[d] = pos[i];
+    uint32_t run = 0;
+    for (int d = 0; d < kDigits; ++d)
+      for (int t = 0; t < parts; ++t) {
+        uint32_t& c = cnt[(size_t)t * kDigits + d];
+        const uint32_t x = c;
+        c = run;
+        run += x;
+      }
+#pragma omp parallel for schedule(static) num_threads(parts)
+    for (int t = 0; t < parts; ++t) {
+      uint32_t* c = &cnt[(size_t)t * kDigits];
+      for (size_t i = n * t / parts; i < n * (t + 1) / parts; ++i) {
+        const uint32_t d = c[(key[i] >> sh) & m]++;
+        key2[d] = key[i];
+        pos2[d] = pos[i];
+      }
     }
     key.swap(key2);
     pos.swap(pos2);
@@ -338,19 +355,28 @@ int build_events(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bo
   };
 
   // row images and group supports
+  // endpoint classes of every row and edit time, found in parallel up front (the
+  // binary searches over the endpoint array are the walk's main cost otherwise)
+  std::vector<int32_t> ecls((size_t)S, 0);
   std::vector<RowImage> row((size_t)M);
+#pragma omp parallel for schedule(static)
+  for (int32_t v = 1; v < S; ++v)
+    if (w.edit[v].op == OP_INSERT || w.edit[v].op == OP_MOVE) ecls[v] = class_of(w.edit[v].t);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) row[i] = {1, f.row_g(i), class_of(f.row_t(i)), f.row_amt(i)};
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < (int64_t)w.ins_t.size(); ++k) row[N + k] = {0, w.ins_g[k], class_of(w.ins_t[k]), 0};
   std::vector<std::vector<int32_t>> sup(G);
   for (int64_t i = 0; i < N; ++i) {
-    row[i] = {1, f.row_g(i), class_of(f.row_t(i)), f.row_amt(i)};
     if (row[i].g < 0 || row[i].g >= G) return 3;
     sup[row[i].g].push_back(row[i].c);
   }
-  for (size_t k = 0; k < w.ins_t.size(); ++k) row[N + k] = {0, w.ins_g[k], class_of(w.ins_t[k]), 0};
   for (int32_t v = 1; v < S; ++v) {
     const Edit& e = w.edit[v];
-    if (e.op == OP_INSERT || e.op == OP_MOVE) sup[e.g].push_back(class_of(e.t));
+    if (e.op == OP_INSERT || e.op == OP_MOVE) sup[e.g].push_back(ecls[v]);
   }
   std::vector<GroupMass> gm(G);
+#pragma omp parallel for schedule(dynamic)
   for (int32_t g = 0; g < G; ++g) {
     std::sort(sup[g].begin(), sup[g].end());
     sup[g].erase(std::unique(sup[g].begin(), sup[g].end()), sup[g].end());
@@ -427,7 +453,7 @@ int build_events(const BwFixture& f, const Declared& w, int32_t S, int32_t q, bo
         switch (e.op) {
           case OP_REPLACE: nw.ex = 1; nw.amt = e.val; break;
           case OP_DELETE: nw.ex = 0; break;
-          default: nw.ex = 1; nw.g = e.g; nw.c = class_of(e.t); nw.amt = e.val; break;  // insert, move
+          default: nw.ex = 1; nw.g = e.g; nw.c = ecls[c]; nw.amt = e.val; break;  // insert, move
         }
         if (old.ex && old.amt != 0)
           ev.push_back({(uint32_t)c, (uint32_t)old.c,
@@ -504,19 +530,28 @@ int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, b
   auto class_of = [&](int64_t t) {
     return (int32_t)(std::upper_bound(ep.begin(), ep.end(), t) - ep.begin());
   };
+  // endpoint classes of every row and edit time, found in parallel up front (the
+  // binary searches over the endpoint array are the walk's main cost otherwise)
+  std::vector<int32_t> ecls((size_t)S, 0);
   std::vector<RowImage> row((size_t)M);
+#pragma omp parallel for schedule(static)
+  for (int32_t v = 1; v < S; ++v)
+    if (w.edit[v].op == OP_INSERT || w.edit[v].op == OP_MOVE) ecls[v] = class_of(w.edit[v].t);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < N; ++i) row[i] = {1, f.row_g(i), class_of(f.row_t(i)), f.row_amt(i)};
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < (int64_t)w.ins_t.size(); ++k) row[N + k] = {0, w.ins_g[k], class_of(w.ins_t[k]), 0};
   std::vector<std::vector<int32_t>> sup(G);
   for (int64_t i = 0; i < N; ++i) {
-    row[i] = {1, f.row_g(i), class_of(f.row_t(i)), f.row_amt(i)};
     if (row[i].g < 0 || row[i].g >= G) return 3;
     sup[row[i].g].push_back(row[i].c);
   }
-  for (size_t k = 0; k < w.ins_t.size(); ++k) row[N + k] = {0, w.ins_g[k], class_of(w.ins_t[k]), 0};
   for (int32_t v = 1; v < S; ++v) {
     const Edit& e = w.edit[v];
-    if (e.op == OP_INSERT || e.op == OP_MOVE) sup[e.g].push_back(class_of(e.t));
+    if (e.op == OP_INSERT || e.op == OP_MOVE) sup[e.g].push_back(ecls[v]);
   }
   std::vector<GroupMass> gm(G);
+#pragma omp parallel for schedule(dynamic)
   for (int32_t g = 0; g < G; ++g) {
     std::sort(sup[g].begin(), sup[g].end());
     sup[g].erase(std::unique(sup[g].begin(), sup[g].end()), sup[g].end());
@@ -558,7 +593,7 @@ int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, b
     switch (e.op) {
       case OP_REPLACE: nw.ex = 1; nw.amt = e.val; break;
       case OP_DELETE: nw.ex = 0; break;
-      default: nw.ex = 1; nw.g = e.g; nw.c = class_of(e.t); nw.amt = e.val; break;  // insert, move
+      default: nw.ex = 1; nw.g = e.g; nw.c = ecls[v]; nw.amt = e.val; break;  // insert, move
     }
     if (old.ex && old.amt != 0) {
       fixed.push_back({(uint32_t)v, (uint32_t)old.c, (int64_t)((uint64_t)0 - (uint64_t)fac[old.g] * (uint64_t)old.amt)});
