@@ -99,7 +99,8 @@ GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch", "gpu
                "bw_forest_launch_timed",
                "bw_serve_create", "bw_serve_reset", "bw_serve_run", "bw_serve_info", "bw_serve_destroy",
                "bw_forest_plan_stats", "bw_key_histogram", "bw_key_prefix", "bw_add_range_carry",
-               "bw_scatter_answers", "bw_native_expand_workspace", "bw_native_expand"]
+               "bw_scatter_answers", "bw_native_expand_workspace", "bw_native_expand",
+               "bw_group_workspace_size", "bw_group_events", "bw_group_queries", "bw_group_status"]
 
 _gpu = None
 
@@ -837,6 +838,55 @@ def expand_events(compact: dict, device=None):
            "bw_native_expand")
     stream.synchronize()   # the host arrays are only needed until the copies are done
     return ev[:compact["n_events"]]
+
+
+def group_by_state(n_states: int, events=None, queries=None, check: bool = True):
+    """Group device event and/or query arrays by state (bw_group_events,
+    bw_group_queries): a stable radix sort on the state.  Returns (events, queries,
+    order): the grouped copies and, for queries, order[i] = the input index of grouped
+    query i (scatter_device_answers puts answers back in input order)."""
+    torch = _torch()
+    L = gpu_lib()
+    L.bw_group_workspace_size.argtypes = [C.c_int64, C.c_int32, C.POINTER(C.c_size_t)]
+    L.bw_group_events.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    L.bw_group_queries.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_size_t, C.c_void_p]
+    L.bw_group_status.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    out_e = out_q = order = None
+    for kind, arr in (("events", events), ("queries", queries)):
+        if arr is None:
+            continue
+        n = int(arr.shape[0])
+        need = C.c_size_t(0)
+        _check(L.bw_group_workspace_size(n, int(kind == "queries"), C.byref(need)), "bw_group_workspace_size")
+        ws = torch.empty(max(int(need.value), 256), dtype=torch.uint8, device=arr.device)
+        stream = torch.cuda.current_stream(arr.device).cuda_stream
+        if kind == "events":
+            out_e = torch.empty_like(arr)
+            _check(L.bw_group_events(arr.data_ptr(), n, int(n_states), out_e.data_ptr(), ws.data_ptr(), ws.numel(),
+                                     stream), "bw_group_events")
+        else:
+            out_q = torch.empty_like(arr)
+            order = torch.empty(max(n, 1), dtype=torch.int64, device=arr.device)[:n]
+            _check(L.bw_group_queries(arr.data_ptr(), n, int(n_states), out_q.data_ptr(), order.data_ptr(),
+                                      ws.data_ptr(), ws.numel(), stream), "bw_group_queries")
+        if check and n:
+            st = C.c_int32(0)
+            _check(L.bw_group_status(ws.data_ptr(), C.byref(st)), "bw_group_status")
+            if st.value:
+                raise ValueError(f"{kind} rejected on the device: {STATUS_NAMES.get(st.value, st.value)}")
+    return out_e, out_q, order
+
+
+def scatter_device_answers(answers, slot, n_out: int):
+    """out[slot[i]] = answers[i] on the device (bw_scatter_answers)."""
+    torch = _torch()
+    L = gpu_lib()
+    L.bw_scatter_answers.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
+    out = torch.zeros(max(n_out, 1), dtype=torch.int64, device=answers.device)[:n_out]
+    _check(L.bw_scatter_answers(answers.data_ptr(), slot.data_ptr(), int(answers.numel()), out.data_ptr(), n_out,
+                                torch.cuda.current_stream(answers.device).cuda_stream), "bw_scatter_answers")
+    return out
 
 
 class BwStreamWorkload(C.Structure):

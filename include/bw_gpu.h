@@ -315,6 +315,22 @@ int bw_add_range_carry(const BwQuery* queries, int64_t n, uint32_t n_keys, const
 int bw_scatter_answers(const int64_t* src, const int64_t* slot, int64_t n, int64_t* dst, int64_t n_dst,
                        void* stream);
 
+/* ============================================================ grouping by state
+ * The replay takes events and queries grouped by state (non-decreasing).  Arrays in
+ * another order are grouped on the device by a stable radix sort on the state (8
+ * bits per pass over the bits n_states needs).  bw_group_queries also writes
+ * order[i] = the input index of output query i, so the answers of the grouped
+ * queries go back to input order with bw_scatter_answers(answers, order, ...).  The
+ * first pass checks every state against n_states: bw_group_status then reads
+ * BW_STATUS_STATE_RANGE (synchronises).  Events must be 16-byte aligned; the input
+ * and output arrays must differ. */
+int bw_group_workspace_size(int64_t n, int32_t queries, size_t* bytes);
+int bw_group_events(const BwEvent* in, int64_t n, int32_t n_states, BwEvent* out, void* workspace,
+                    size_t workspace_bytes, void* stream);
+int bw_group_queries(const BwQuery* in, int64_t n, int32_t n_states, BwQuery* out, int64_t* order,
+                     void* workspace, size_t workspace_bytes, void* stream);
+int bw_group_status(const void* workspace, int32_t* status);
+
 /* ============================================================ chain setup on the device
  * The factor expansion of a reference-native chain (the bulk of its events: a factor
  * edit of group g becomes one event per class of g's support) built on the GPU.
