@@ -16,6 +16,9 @@ roofline, e2e and CPU baseline:
   65,536 keys) on the general pipeline;
 * ``csr_lut``: the sparse-key CSR rank-LUT (10M u64 keys, 100M point and range
   lookups, LUT budgets 64/256/1024 MiB);
+* ``csr_versioned``: config 3's versioned dimension -- the csr_lut keys, events and
+  lookups on a 100,000-state chain with forks: rank index, rank mapping and two
+  replays over the 10M-rank domain per step;
 * ``reference_chain``: the reference's own published GPU workload -- a 300,000-state
   chain, seed 7, factor period 37, q=2, per-state ranges, on the synthetic 100k-row
   fixture -- through the worker binary (both arms: the event replay and the
@@ -507,6 +510,82 @@ def csr_record(args, bw, dev, steps: int, warmup: int, scale: float = 1.0) -> di
             "gpu_launches": 3 * 3 * steps}
 
 
+def csr_versioned_record(args, bw, dev, steps: int, scale: float = 1.0) -> dict:
+    """Config 3's versioned dimension: the csr_lut keys, events and lookups on a
+    100,000-state chain with forks.  Per step: the keys' rank index (bw_csr_build),
+    events and lookups mapped to ranks (bw_csr_events, bw_csr_queries), and one
+    replay over the 10M-rank domain for the point lookups and one for the range
+    lookups.  Checked against the oracle on 100,000 sampled lookups of each kind."""
+    import torch
+    oracle = oracle_mod()
+    t_gen = time.perf_counter()
+    w = bw.workloads.csr_versioned(args.seed, scale)
+    gen_s = time.perf_counter() - t_gen
+    S, E, L = len(w.parent), len(w.ev_key), len(w.pt_key)
+
+    def t(a, dt):
+        return torch.from_numpy(np.ascontiguousarray(a).view(dt)).to(dev)
+    p = torch.from_numpy(w.parent).to(dev)
+    es, ek, ed = t(w.ev_state, np.int32), t(w.ev_key, np.int64), t(w.ev_delta, np.int64)
+    ps, pk = t(w.pt_state, np.int32), t(w.pt_key, np.int64)
+    rs, rl, rh = t(w.rg_state, np.int32), t(w.rg_lo, np.int64), t(w.rg_hi, np.int64)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1, ev2, ev3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+    times = []
+    for i in range(1 + steps):
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        idx = bw.CsrIndex(ek, ed, key_bits=w.key_bits)
+        ev_r = idx.events(es, ek, ed)
+        q_pt, q_rg = idx.queries(ps, pk), idx.queries(rs, rl, rh)
+        ev1.record(stream)
+        a_pt = bw.replay(p, max(1, idx.count()), ev_r, q_pt, check=False)
+        ev2.record(stream)
+        a_rg = bw.replay(p, max(1, idx.count()), ev_r, q_rg, check=False)
+        ev3.record(stream)
+        torch.cuda.synchronize()
+        if i:
+            times.append((ev0.elapsed_time(ev1), ev1.elapsed_time(ev2), ev2.elapsed_time(ev3)))
+    idx_ms, pt_ms, rg_ms = (statistics.median(x) for x in zip(*times))
+    # oracle on sampled lookups (ranks on the host, preorder replay over the rank domain)
+    rng = np.random.default_rng(11)
+    keys = np.unique(w.ev_key)
+    evo = np.empty(E, dtype=bw.workloads.EVENT_DTYPE)
+    evo["state"], evo["key"], evo["delta"] = w.ev_state, np.searchsorted(keys, w.ev_key), w.ev_delta
+    sp, sr = np.sort(rng.choice(L, 100_000, replace=False)), np.sort(rng.choice(L, 100_000, replace=False))
+    qo = np.empty(200_000, dtype=bw.workloads.QUERY_DTYPE)
+    r = np.searchsorted(keys, w.pt_key[sp])
+    pres = (r < len(keys)) & (keys[np.minimum(r, len(keys) - 1)] == w.pt_key[sp])
+    qo["state"][:100_000], qo["lo"][:100_000], qo["hi"][:100_000] = w.pt_state[sp], np.where(pres, r, 0), \
+        np.where(pres, r + 1, 0)
+    qo["state"][100_000:] = w.rg_state[sr]
+    qo["lo"][100_000:], qo["hi"][100_000:] = np.searchsorted(keys, w.rg_lo[sr]), np.searchsorted(keys, w.rg_hi[sr])
+    t_cpu = time.perf_counter()
+    want_pt = oracle.ev_sweep(w.parent, len(keys), evo, qo[:100_000])
+    want_rg = oracle.ev_sweep(w.parent, len(keys), evo, qo[100_000:])
+    cpu_s = time.perf_counter() - t_cpu
+    if not (np.array_equal(a_pt.cpu().numpy()[sp], want_pt) and np.array_equal(a_rg.cpu().numpy()[sr], want_rg)):
+        raise SystemExit("csr_versioned: GPU answers differ from the oracle")
+    peak, peak_kind = measured_peaks()
+    step_ms = idx_ms + pt_ms + rg_ms
+    sweep_bytes = 16 * E + 20 * L
+    return {"value": 2 * L / (step_ms / 1e3), "unit": "lookups/s", "ms_per_step": step_ms, "steps": steps,
+            "config": {"workload": "csr_versioned", "states": S, "events": E, "distinct_keys": int(w.n_keys),
+                       "point_lookups": L, "range_lookups": L, "topology": "tree (chain with forks, p=0.9)",
+                       "key_universe_bits": w.key_bits, "l2": "inputs larger than L2 (no flush needed)"},
+            "phases_ms": {"index_and_rank_mapping": idx_ms, "point_replay": pt_ms, "range_replay": rg_ms},
+            "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": sweep_bytes / (pt_ms / 1e3) / 1e9,
+                         "peak": peak, "unit": "GB/s", "frac": sweep_bytes / (pt_ms / 1e3) / 1e9 / peak,
+                         "peak_kind": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": sweep_bytes,
+                         "note": "whole point replay over the rank domain; a 10M-key domain takes several rank "
+                                 "slices per block, each sweeping the block's events again"},
+            "cpu_baseline": {"value": 200_000 / cpu_s, "unit": "lookups/s", "cores": 1, "kind": "port",
+                             "sample": f"preorder replay of all {E} events answering 200,000 sampled lookups "
+                                       f"({cpu_s:.1f} s)"},
+            "exact": "100,000 sampled point and 100,000 range lookups against the oracle",
+            "setup": {"generate_s": gen_s}}
+
+
 # the reference's published GPU numbers for its own workload (300,000-state chain,
 # seed 7, factor period 37, q=2, per-state ranges; RTX 4090 + EPYC 9554)
 REFERENCE_PUBLISHED = {
@@ -811,6 +890,10 @@ def bench_batched(args):
         subs["csr_lut"]["wall_s"] = time.perf_counter() - t_sub
         torch.cuda.empty_cache()
         t_sub = time.perf_counter()
+        subs["csr_versioned"] = csr_versioned_record(args, bw, dev, min(args.sub_steps, 2))
+        subs["csr_versioned"]["wall_s"] = time.perf_counter() - t_sub
+        torch.cuda.empty_cache()
+        t_sub = time.perf_counter()
         subs["reference_chain"] = reference_chain_record(args, bw, dev, args.sub_steps)
         subs["reference_chain"]["wall_s"] = time.perf_counter() - t_sub
         torch.cuda.empty_cache()
@@ -941,6 +1024,21 @@ def bench_csr(args):
     return 0
 
 
+def bench_csr_versioned(args):
+    """``--workload csr_versioned``: config 3's versioned dimension alone, one line."""
+    import torch
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    bw = load_pkg()
+    bw.build()
+    rec = csr_versioned_record(args, bw, dev, args.steps, args.scale)
+    line = {"metric": "exact versioned sparse-key lookups/s (CSR ranks + version-tree replay)", "n_gpus": 1,
+            "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic", **rec}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def bench_reference_chain(args):
     """``--workload reference_chain``: the reference's own GPU workload alone (its
     300,000-state chain) through both worker arms and the warm replay, one JSON line."""
@@ -966,6 +1064,8 @@ def main():
         return reference_arm(args)
     if args.workload == "reference_chain":
         return bench_reference_chain(args)
+    if args.workload == "csr_versioned":
+        return bench_csr_versioned(args)
     if args.workload == "csr_lut":
         return bench_csr(args)
     if args.workload == "batched_trees":

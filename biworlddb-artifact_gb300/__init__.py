@@ -100,7 +100,8 @@ GPU_SYMBOLS = ["gpu_v7_launch", "gpu_combine_launch", "bw_v7_carry_launch", "gpu
                "bw_serve_create", "bw_serve_reset", "bw_serve_run", "bw_serve_info", "bw_serve_destroy",
                "bw_forest_plan_stats", "bw_key_histogram", "bw_key_prefix", "bw_add_range_carry",
                "bw_scatter_answers", "bw_native_expand_workspace", "bw_native_expand",
-               "bw_group_workspace_size", "bw_group_events", "bw_group_queries", "bw_group_status"]
+               "bw_group_workspace_size", "bw_group_events", "bw_group_queries", "bw_group_status",
+               "bw_csr_events", "bw_csr_queries"]
 
 _gpu = None
 
@@ -889,6 +890,20 @@ def scatter_device_answers(answers, slot, n_out: int):
     return out
 
 
+def versioned_sparse_replay(parent, ev_state, ev_key, ev_delta, q_state, lo, hi=None, *, key_bits: int = 40,
+                            lut_budget_bytes: int = 64 << 20, index=None, path: str = "auto"):
+    """A version tree over sparse u64 keys (config 3's versioned dimension): the keys'
+    CSR rank index on the device (bw_csr_build, or `index`), events and lookups mapped
+    to ranks there (bw_csr_events, bw_csr_queries), then the replay over the rank
+    domain.  Point lookups when hi is None, else range lookups over [lo, hi).
+    Returns (answers, index)."""
+    idx = index if index is not None else CsrIndex(ev_key, ev_delta, key_bits=key_bits,
+                                                   lut_budget_bytes=lut_budget_bytes)
+    ev = idx.events(ev_state, ev_key, ev_delta)
+    qs = idx.queries(q_state, lo, hi)
+    return replay(parent, max(1, idx.count()), ev, qs, path=path), idx
+
+
 class BwStreamWorkload(C.Structure):
     _fields_ = [("chain", BwNativeWorkload), ("slot", C.c_void_p), ("n_answers", C.c_int64), ("q", C.c_int32)]
 
@@ -1270,4 +1285,34 @@ class CsrIndex:
         st = torch.cuda.current_stream(self.device).cuda_stream
         _check(gpu_lib().bw_csr_range(C.byref(self.idx), bounds.data_ptr() if n else None, n,
                                       out.data_ptr() if n else None, st), "bw_csr_range")
+        return out
+
+    def events(self, states, keys, deltas):
+        """Event records over the index's ranks (bw_csr_events): an (n, 2) int64 tensor
+        of {u32 state, u32 rank, i64 delta}; states u32-valued int32, keys u64 as int64."""
+        torch = _torch()
+        L = gpu_lib()
+        L.bw_csr_events.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                    C.c_void_p]
+        n = int(keys.numel())
+        out = torch.empty((max(n, 1), 2), dtype=torch.int64, device=self.device)[:n]
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        _check(L.bw_csr_events(C.byref(self.idx), states.data_ptr() if n else None, keys.data_ptr() if n else None,
+                               deltas.data_ptr() if n else None, n, out.data_ptr() if n else None, st),
+               "bw_csr_events")
+        return out
+
+    def queries(self, states, lo, hi=None):
+        """Query records over rank intervals (bw_csr_queries): point lookups of lo
+        (hi None) or range lookups over keys [lo, hi); an (n, 3) int32 tensor."""
+        torch = _torch()
+        L = gpu_lib()
+        L.bw_csr_queries.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                     C.c_void_p]
+        n = int(lo.numel())
+        out = torch.empty((max(n, 1), 3), dtype=torch.int32, device=self.device)[:n]
+        st = torch.cuda.current_stream(self.device).cuda_stream
+        _check(L.bw_csr_queries(C.byref(self.idx), states.data_ptr() if n else None, lo.data_ptr() if n else None,
+                                hi.data_ptr() if (n and hi is not None) else None, n,
+                                out.data_ptr() if n else None, st), "bw_csr_queries")
         return out

@@ -246,6 +246,44 @@ __global__ void k_csr_range(BwCsr x, const uint64_t* __restrict__ bounds, int64_
   }
 }
 
+// Versioned sparse keys (the event model over the index's ranks): event records
+// keyed by the rank of their u64 key (a key missing from the index gets rank m, which
+// the replay reports as out of range), and query records over rank intervals -- a
+// point lookup of a present key is [rank, rank + 1), of an absent one empty; a range
+// lookup [lo, hi) over keys is [rank(lo), rank(hi)) over ranks.
+__global__ void k_csr_events(BwCsr x, const uint32_t* __restrict__ states, const uint64_t* __restrict__ keys,
+                             const int64_t* __restrict__ deltas, int64_t n, BwEvent* __restrict__ out) {
+  const int64_t m = *x.count;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    bool pr;
+    const int64_t r = csr_rank(x, m, keys[i], pr);
+    BwEvent e;
+    e.state = states[i];
+    e.key = (uint32_t)(pr ? r : m);
+    e.delta = deltas[i];
+    out[i] = e;
+  }
+}
+__global__ void k_csr_queries(BwCsr x, const uint32_t* __restrict__ states, const uint64_t* __restrict__ lo,
+                              const uint64_t* __restrict__ hi, int64_t n, BwQuery* __restrict__ out) {
+  const int64_t m = *x.count;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    bool pr;
+    const int64_t a = csr_rank(x, m, lo[i], pr);
+    BwQuery q;
+    q.state = states[i];
+    if (!hi) {
+      q.lo = pr ? (uint32_t)a : 0u;
+      q.hi = pr ? (uint32_t)a + 1u : 0u;
+    } else {
+      bool pb;
+      q.lo = (uint32_t)a;
+      q.hi = (uint32_t)csr_rank(x, m, hi[i], pb);
+    }
+    out[i] = q;
+  }
+}
+
 struct CsrLayout {
   int32_t shift = 0, passes = 0;
   int64_t nb = 0, ntiles = 0;
@@ -418,4 +456,20 @@ extern "C" int bw_csr_status(const BwCsr* idx, int32_t* status) {
   int rc = report(cudaDeviceSynchronize(), "synchronise");
   if (rc) return rc;
   return report(cudaMemcpy(status, idx->status, 4, cudaMemcpyDeviceToHost), "status read");
+}
+
+extern "C" int bw_csr_events(const BwCsr* idx, const uint32_t* states, const uint64_t* keys, const int64_t* deltas,
+                             int64_t n, BwEvent* out, void* stream) {
+  if (check_index(idx) || n < 0 || (n > 0 && (!states || !keys || !deltas || !out))) return BW_EINVAL;
+  if (n == 0) return 0;
+  k_csr_events<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(*idx, states, keys, deltas, n, out);
+  return report(cudaGetLastError(), "k_csr_events");
+}
+
+extern "C" int bw_csr_queries(const BwCsr* idx, const uint32_t* states, const uint64_t* lo, const uint64_t* hi,
+                              int64_t n, BwQuery* out, void* stream) {
+  if (check_index(idx) || n < 0 || (n > 0 && (!states || !lo || !out))) return BW_EINVAL;
+  if (n == 0) return 0;
+  k_csr_queries<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(*idx, states, lo, hi, n, out);
+  return report(cudaGetLastError(), "k_csr_queries");
 }

@@ -30,6 +30,9 @@ configured workloads:
 * ``csr_lut`` (sparse-key rank index): 10,000,000 distinct u64 keys over
   [0, 2^40), 20,000,000 (key, delta) events on them, 100,000,000 point and
   100,000,000 range lookups, half present keys and half absent.
+* ``csr_versioned`` (config 3's versioned dimension): the same keys, events and
+  lookups on a 100,000-state chain with forks (extend with p=0.9, else fork from a
+  uniform earlier state), events and lookups at uniform states.
 
 Events and queries are produced grouped by state (a commit log appends each
 version's events when the version is created; answers come back state-major, as
@@ -137,6 +140,8 @@ CONFIGS = {"plain_chain": plain_chain, "trip_tree": trip_tree}
 def make(name: str, seed: int = 0, scale: float = 1.0):
     if name == "csr_lut":
         return csr_lut(seed=seed, scale=scale)
+    if name == "csr_versioned":
+        return csr_versioned(seed=seed, scale=scale)
     if name == "batched_trees":
         return batched_trees(seed=seed, scale=scale)
     return CONFIGS[name](seed=seed, scale=scale)
@@ -290,6 +295,43 @@ def csr_lut(seed: int = 0, scale: float = 1.0, lookups: int | None = None) -> Cs
     a, b = mixed(L), mixed(L)
     ranges = np.stack([np.minimum(a, b), np.maximum(a, b)], axis=1)
     return CsrWorkload("csr_lut", bits, int(K), keys, amounts, point, ranges)
+
+
+@dataclass
+class CsrVersioned:
+    """Config 3's versioned dimension: a version tree over sparse u64 keys.  Events
+    (grouped by state) carry u64 keys; lookups are point and range lookups at states
+    (grouped by state).  Answers are the usual root-path range sums over the keys."""
+    name: str
+    key_bits: int
+    n_keys: int
+    parent: np.ndarray
+    ev_state: np.ndarray      # u32, non-decreasing
+    ev_key: np.ndarray        # u64
+    ev_delta: np.ndarray      # i64
+    pt_state: np.ndarray      # u32, non-decreasing
+    pt_key: np.ndarray        # u64
+    rg_state: np.ndarray      # u32, non-decreasing
+    rg_lo: np.ndarray         # u64
+    rg_hi: np.ndarray         # u64
+
+
+def csr_versioned(seed: int = 0, scale: float = 1.0, lookups: int | None = None) -> CsrVersioned:
+    """The csr_lut keys, events and lookups (10M distinct u64 keys, 20M events, 100M
+    point and 100M range lookups, half present and half absent) on a 100,000-state
+    chain with forks (each state extends its parent with p=0.9, else forks from a
+    uniform earlier state), events and lookups at uniform states."""
+    base = csr_lut(seed, scale, lookups)
+    rng = np.random.default_rng(seed + 1)
+    S = max(2, int(100_000 * scale))
+    parent = _fork_tree(rng, S, 0.9)
+    E, L = len(base.keys), len(base.point)
+
+    def states(n):
+        return np.sort(rng.integers(0, S, size=n)).astype(np.uint32)
+    return CsrVersioned("csr_versioned", base.key_bits, base.n_distinct, parent, states(E), base.keys,
+                        base.amounts, states(L), base.point, states(L), base.ranges[:, 0].copy(),
+                        base.ranges[:, 1].copy())
 
 
 @dataclass

@@ -563,6 +563,18 @@ int bw_csr_point(const BwCsr* idx, const uint64_t* keys, int64_t n, int64_t* out
 int bw_csr_range(const BwCsr* idx, const uint64_t* bounds, int64_t n, int64_t* out, void* stream);
 /* Synchronise the device and read the build's status word (0 = valid input). */
 int bw_csr_status(const BwCsr* idx, int32_t* status);
+/* Versioned sparse keys: the event model over the index's ranks, so a version tree
+ * whose events carry u64 keys (config 3's chain-with-forks over sparse keys) replays
+ * with bw_replay_launch at n_keys = the index's key count.  bw_csr_events: out[i] =
+ * (states[i], rank of keys[i], deltas[i]); a key missing from the index gets rank m
+ * (the replay then reports BW_STATUS_EVENT_KEY_RANGE).  bw_csr_queries: hi == NULL,
+ * point lookups -- (states[i], rank, rank + 1) for a present lo[i], an empty interval
+ * for an absent one; else range lookups over keys [lo[i], hi[i]) -- (states[i],
+ * rank(lo[i]), rank(hi[i])), empty when hi <= lo.  rank = index keys below the key. */
+int bw_csr_events(const BwCsr* idx, const uint32_t* states, const uint64_t* keys, const int64_t* deltas,
+                  int64_t n, BwEvent* out, void* stream);
+int bw_csr_queries(const BwCsr* idx, const uint32_t* states, const uint64_t* lo, const uint64_t* hi,
+                   int64_t n, BwQuery* out, void* stream);
 
 /* Library/device information: SM count of the current device and the library's
  * compile-time architecture tag (e.g. 1030 for sm_103a). */
