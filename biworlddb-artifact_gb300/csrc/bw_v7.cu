@@ -11,7 +11,9 @@
 //  * The dense block leaf delta lives directly in the caller's dV row (global
 //    memory), so shared memory holds only the Fenwick tree and the factor vector
 //    and the class domain can reach ~28k classes instead of ~6k.
-//  * The next node is prefetched into registers while the current one is applied.
+//  * Runs of up to 32 nodes without a factor edit are applied as one batch (warp 0,
+//    one lane per node), and each of their queries subtracts the batch's later
+//    updates below its bound: two barriers per batch instead of two per node.
 //  * One kernel body serves the 56-byte node (gpu_v7.h), the 40-byte compact node
 //    (gpu_v7b.h, gpu_session.h) and the session form, whose Fenwick tree and leaf
 //    live in caller-owned global memory (any class domain).
@@ -25,7 +27,8 @@
 namespace bw {
 
 constexpr int kV7Threads = 512;
-constexpr int kV7SmemLimit = 232448 - 1024;
+constexpr int kV7Batch = 32;                  // nodes per batch (one warp's lanes)
+constexpr int kV7SmemLimit = 232448 - 2048;   // dynamic shared memory; the batch arrays are static
 
 // One plan for the three node encodings of the drop-in ABIs (gpu_v7.h, gpu_v7b.h,
 // gpu_session.h): the kernel argument.
@@ -95,60 +98,78 @@ __global__ void __launch_bounds__(kV7Threads) k_v7_block(V7Run a) {
   const Node* nodes = static_cast<const Node*>(a.nodes);
   const int v0 = a.v0[b], v1 = a.v1[b];
   const int64_t* need = a.need_off + (size_t)b * G;
-  Node nxt;
-  if (v0 < v1) nxt = nodes[v0];
-  for (int v = v0; v < v1; ++v) {
-    const NodeView p = view_node(nxt);
-    if (v + 1 < v1) nxt = nodes[v + 1];
-    if (p.kind == 1) {
-      // lane 0 removes the old row image, lane 1 adds the new one (distinct
-      // leaf/devbuf cells unless old == new, which the atomics tolerate)
-      if (tid < 32) {
-        const bool is_old = tid == 0, is_new = tid == 1;
-        bool act = false;
-        uint32_t c1 = 0;
-        uint64_t w = 0;
-        if (is_old && p.ex_old && p.amt_old != 0) {
-          act = true;
-          c1 = (uint32_t)p.c_old + 1u;
-          w = (uint64_t)0 - (uint64_t)fac[p.g_old] * (uint64_t)p.amt_old;
-          atomicAdd(reinterpret_cast<unsigned long long*>(leaf + c1), (unsigned long long)w);
-          const int64_t off = need[p.g_old];
-          if (off >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(a.devbuf + off + p.ti_old),
-                                  (unsigned long long)((uint64_t)0 - (uint64_t)p.amt_old));
-        } else if (is_new && p.ex_new && p.amt_new != 0) {
-          act = true;
-          c1 = (uint32_t)p.c_new + 1u;
-          w = (uint64_t)fac[p.g_new] * (uint64_t)p.amt_new;
-          atomicAdd(reinterpret_cast<unsigned long long*>(leaf + c1), (unsigned long long)w);
-          const int64_t off = need[p.g_new];
-          if (off >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(a.devbuf + off + p.ti_new),
-                                  (unsigned long long)p.amt_new);
+  // A run of up to 32 consecutive nodes without a factor edit is one batch: warp 0
+  // applies all of their row updates at once (the Fenwick sums commute), then every
+  // query of node j reads the Fenwick prefix and takes back the updates of the
+  // batch's later nodes that fall below its bound.  Two barriers per batch instead of
+  // two per node; a factor edit is a batch of its own.
+  __shared__ uint32_t upd_c1[2 * kV7Batch];   // 1-based class of each update, or ~0u for none
+  __shared__ unsigned long long upd_w[2 * kV7Batch];
+  __shared__ int batch_len;
+  for (int v = v0; v < v1;) {
+    if (tid < 32) {
+      const int i = v + tid;
+      const bool in = tid < kV7Batch && i < v1;
+      NodeView p{};
+      if (in) p = view_node(nodes[i]);
+      const unsigned fac_mask = __ballot_sync(0xffffffffu, in && p.kind == 2);
+      const unsigned in_mask = __ballot_sync(0xffffffffu, in);
+      // a leading factor edit forms a batch of one; else the run before the first one
+      const int k = (fac_mask & 1u) ? 1 : (fac_mask ? __ffs(fac_mask) - 1 : __popc(in_mask));
+      if (tid == 0) batch_len = k;
+      if (!(fac_mask & 1u) && tid < k) {
+        uint32_t c_old = ~0u, c_new = ~0u;
+        uint64_t w_old = 0, w_new = 0;
+        if (p.kind == 1) {
+          if (p.ex_old && p.amt_old != 0) {
+            c_old = (uint32_t)p.c_old + 1u;
+            w_old = (uint64_t)0 - (uint64_t)fac[p.g_old] * (uint64_t)p.amt_old;
+            atomicAdd(reinterpret_cast<unsigned long long*>(leaf + c_old), (unsigned long long)w_old);
+            const int64_t off = need[p.g_old];
+            if (off >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(a.devbuf + off + p.ti_old),
+                                    (unsigned long long)((uint64_t)0 - (uint64_t)p.amt_old));
+            fen_add<GLOBAL>(fen, (uint32_t)ncls, c_old, w_old);
+          }
+          if (p.ex_new && p.amt_new != 0) {
+            c_new = (uint32_t)p.c_new + 1u;
+            w_new = (uint64_t)fac[p.g_new] * (uint64_t)p.amt_new;
+            atomicAdd(reinterpret_cast<unsigned long long*>(leaf + c_new), (unsigned long long)w_new);
+            const int64_t off = need[p.g_new];
+            if (off >= 0) atomicAdd(reinterpret_cast<unsigned long long*>(a.devbuf + off + p.ti_new),
+                                    (unsigned long long)p.amt_new);
+            fen_add<GLOBAL>(fen, (uint32_t)ncls, c_new, w_new);
+          }
         }
-        if (act) fen_add<GLOBAL>(fen, (uint32_t)ncls, c1, w);
+        upd_c1[2 * tid] = c_old;
+        upd_w[2 * tid] = w_old;
+        upd_c1[2 * tid + 1] = c_new;
+        upd_w[2 * tid + 1] = w_new;
       }
-      __syncthreads();
-    } else if (p.kind == 2) {
-      const int g = p.g_old;
+    }
+    __syncthreads();
+    const int k = batch_len;
+    const NodeView f = view_node(nodes[v]);
+    if (k == 1 && f.kind == 2) {
+      const int g = f.g_old;
       const int row = a.g2row[g];
       const int64_t off = need[g];
-      const uint64_t ds = (uint64_t)p.fac_val - (uint64_t)p.fac_prev;
+      const uint64_t ds = (uint64_t)f.fac_val - (uint64_t)f.fac_prev;
       if (row >= 0 && off >= 0 && ds != 0) {
         const int kb = a.ms_off[row], ke = a.ms_off[row + 1];
         for (int k0 = kb; k0 < ke; k0 += nt) {
-          const int k = k0 + tid;
+          const int kk = k0 + tid;
           bool act = false;
           uint32_t c1 = 0;
           uint64_t d = 0;
-          if (k < ke) {
-            const int di = a.ms_dev[k];
+          if (kk < ke) {
+            const int di = a.ms_dev[kk];
             // devbuf and leaf cells are also updated by global atomics (row edits),
             // which do not update L1: read them from L2
             const uint64_t dev = di >= 0 ? (uint64_t)__ldcg(a.devbuf + off + di) : 0;
-            d = ds * ((uint64_t)a.ms_base[k] + dev);
+            d = ds * ((uint64_t)a.ms_base[kk] + dev);
             if (d != 0) {
               act = true;
-              c1 = (uint32_t)a.ms_cls[k] + 1u;
+              c1 = (uint32_t)a.ms_cls[kk] + 1u;
               leaf[c1] = (int64_t)((uint64_t)__ldcg(leaf + c1) + d);  // support classes are distinct
             }
           }
@@ -156,15 +177,26 @@ __global__ void __launch_bounds__(kV7Threads) k_v7_block(V7Run a) {
         }
       }
       __syncthreads();
-      if (tid == 0) fac[g] = p.fac_val;
-      __syncthreads();
-    }
-    for (int e = tid; e < 2 * q; e += nt) {
-      const int kk = e >> 1;
-      const int idx = (e & 1) ? a.qhb[(size_t)v * q + kk] : a.qlb[(size_t)v * q + kk];
-      a.lvals[(size_t)(v - 1) * (size_t)(2 * q) + e] = (int64_t)fen_prefix<GLOBAL>(fen, (uint32_t)idx);
+      if (tid == 0) fac[g] = f.fac_val;
+      for (int e = tid; e < 2 * q; e += nt) {
+        const int idx = (e & 1) ? a.qhb[(size_t)v * q + (e >> 1)] : a.qlb[(size_t)v * q + (e >> 1)];
+        a.lvals[(size_t)(v - 1) * (size_t)(2 * q) + e] = (int64_t)fen_prefix<GLOBAL>(fen, (uint32_t)idx);
+      }
+    } else {
+      // queries of the batch's nodes: the prefix after the whole batch, less the later
+      // nodes' updates at or below the bound
+      for (int e = tid; e < k * 2 * q; e += nt) {
+        const int j = e / (2 * q), r = e - j * (2 * q);
+        const int vv = v + j;
+        const int idx = (r & 1) ? a.qhb[(size_t)vv * q + (r >> 1)] : a.qlb[(size_t)vv * q + (r >> 1)];
+        uint64_t val = fen_prefix<GLOBAL>(fen, (uint32_t)idx);
+        for (int u = 2 * (j + 1); u < 2 * k; ++u)
+          if (upd_c1[u] <= (uint32_t)idx) val -= upd_w[u];
+        a.lvals[(size_t)(vv - 1) * (size_t)(2 * q) + r] = (int64_t)val;
+      }
     }
     __syncthreads();
+    v += k;
   }
   if (GLOBAL && a.dV)   // the session form also reports the block's leaf delta in dV
     for (int i = tid; i < Cpfx; i += nt) a.dV[(size_t)b * Cpfx + i] = __ldcg(leaf + i);
