@@ -27,6 +27,7 @@
 // place: row b becomes the key prefix of the events of blocks 0 .. b-1.
 // Fix-up (k_chain_fixup): every query of block b >= 1 adds row[hi] - row[lo].
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -691,8 +692,9 @@ constexpr int kNumGeometries = 5;
 // with (in this order of preference, measured on byte-dominated chains) 3 events
 // each and a three-tile ring at four CTAs per SM (three with the int64 window), 4
 // events and a two-tile ring at three or more, 4 events and a three-tile ring at two
-// or more; else the geometry with the most resident threads per SM (few, short
-// state blocks: wide CTAs finish each sooner).  Tiles always stay large: smaller
+// or more; else (few, short state blocks) 512 threads x 2 events, whose wide CTAs
+// finish each block soonest, with one block per SM while every block keeps at least
+// 2,048 events.  Tiles always stay large: smaller
 // tiles shorten the in-tile scans but cost more per tile than they save, even on
 // query-dense chains (measured).
 int geometry_override() {
@@ -742,6 +744,10 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
   if (pin < 0 && fit[4] >= (s.w64 ? 3 : 4) && s.E >= (int64_t)sms * fit[4] * kChainMinBlockEvents) pin = 4;
   if (pin < 0 && fit[3] >= 3 && s.E >= (int64_t)sms * fit[3] * kChainMinBlockEvents) pin = 3;
   if (pin < 0 && fit[1] >= 2 && s.E >= (int64_t)sms * fit[1] * kChainMinBlockEvents) pin = 1;
+  // too few events to fill the GPU with full blocks: the widest CTA (512 threads)
+  // finishes each short block soonest (measured on the 1M-event plain chain)
+  const bool few = pin < 0;
+  if (few && fit[2] >= 1) pin = 2;
   int best = -1, best_threads = 0;
   for (int g = 0; g < kNumGeometries; ++g) {
     const Geometry& G = kGeometries[g];
@@ -760,6 +766,8 @@ int chain_spec(const BwReplayArgs* a, int sms, ChainSpec& s) {
   }
   if (best < 0) return BW_EINVAL;
   int64_t B = a->blocks > 0 ? a->blocks : (s.E + kChainMinBlockEvents - 1) / kChainMinBlockEvents;
+  // few events: one block per SM when every block still gets 2,048 events or more
+  if (a->blocks <= 0 && few && B < sms) B = std::min<int64_t>(sms, std::max<int64_t>(B, s.E / 2048));
   const int64_t cap = (int64_t)sms * s.ctas_per_sm;
   if (a->blocks <= 0 && B > cap) B = cap;
   if (B > s.E) B = s.E;
