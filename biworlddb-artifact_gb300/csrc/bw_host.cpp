@@ -195,6 +195,7 @@ struct RowImage {
   uint8_t ex;
   int32_t g, c;
   int64_t amt;
+  int32_t si = 0;   // index of class c in group g's support (the compact builder keeps it)
 };
 
 }  // namespace
@@ -558,6 +559,20 @@ int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, b
     gm[g].cls.swap(sup[g]);
     gm[g].mass.assign(gm[g].cls.size(), 0);
   }
+  // support positions of every row's and every insert/move edit's class, in parallel:
+  // the walk below then needs no search
+  std::vector<int32_t> esi((size_t)S, 0);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < M; ++i) {
+    const std::vector<int32_t>& cl = gm[row[i].g].cls;
+    row[i].si = (int32_t)(std::lower_bound(cl.begin(), cl.end(), row[i].c) - cl.begin());
+  }
+#pragma omp parallel for schedule(static)
+  for (int32_t v = 1; v < S; ++v)
+    if (w.edit[v].op == OP_INSERT || w.edit[v].op == OP_MOVE) {
+      const std::vector<int32_t>& cl = gm[w.edit[v].g].cls;
+      esi[v] = (int32_t)(std::lower_bound(cl.begin(), cl.end(), ecls[v]) - cl.begin());
+    }
   std::vector<int64_t> fac(G);
   for (int32_t g = 0; g < G; ++g) fac[g] = f.factor(g);
   std::vector<BwEvent> fixed;
@@ -567,21 +582,28 @@ int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, b
   int64_t pos = 0;
   for (int64_t i = 0; i < N; ++i) {   // state 0: the base rows, weighted by the fixture factors
     const RowImage& r = row[i];
-    GroupMass& m = gm[r.g];
-    m.mass[m.index(r.c)] += (uint64_t)r.amt;
+    gm[r.g].mass[r.si] += (uint64_t)r.amt;
     const uint64_t d = (uint64_t)r.amt * (uint64_t)fac[r.g];
     if (d) {
       fixed.push_back({0u, (uint32_t)r.c, (int64_t)d});
       fixed_pos.push_back(pos++);
     }
   }
-  std::vector<std::vector<BwTimeline>> tl(G);
+  // timeline records in walk (state) order with their groups; grouped afterwards
+  std::vector<BwTimeline> tlf;
+  std::vector<int32_t> tlg;
+  tlf.reserve(2 * (size_t)S);
+  tlg.reserve(2 * (size_t)S);
+  auto tl_push = [&](int32_t g, const BwTimeline& x) {
+    tlf.push_back(x);
+    tlg.push_back(g);
+  };
   for (int32_t v = 1; v < S; ++v) {
     const Edit& e = w.edit[v];
     if (e.op == OP_FACTOR) {
       const uint64_t ds = (uint64_t)e.val - (uint64_t)fac[e.g];
       if (ds && !gm[e.g].cls.empty()) {
-        tl[e.g].push_back({v, -1, (int64_t)ds, pos});
+        tl_push(e.g, {v, -1, (int64_t)ds, pos});
         pos += (int64_t)gm[e.g].cls.size();
       }
       fac[e.g] = e.val;
@@ -593,7 +615,7 @@ int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, b
     switch (e.op) {
       case OP_REPLACE: nw.ex = 1; nw.amt = e.val; break;
       case OP_DELETE: nw.ex = 0; break;
-      default: nw.ex = 1; nw.g = e.g; nw.c = ecls[v]; nw.amt = e.val; break;  // insert, move
+      default: nw.ex = 1; nw.g = e.g; nw.c = ecls[v]; nw.si = esi[v]; nw.amt = e.val; break;  // insert, move
     }
     if (old.ex && old.amt != 0) {
       fixed.push_back({(uint32_t)v, (uint32_t)old.c, (int64_t)((uint64_t)0 - (uint64_t)fac[old.g] * (uint64_t)old.amt)});
@@ -603,8 +625,8 @@ int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, b
       fixed.push_back({(uint32_t)v, (uint32_t)nw.c, (int64_t)((uint64_t)fac[nw.g] * (uint64_t)nw.amt)});
       fixed_pos.push_back(pos++);
     }
-    if (old.ex) tl[old.g].push_back({v, (int32_t)gm[old.g].index(old.c), (int64_t)((uint64_t)0 - (uint64_t)old.amt), 0});
-    if (nw.ex) tl[nw.g].push_back({v, (int32_t)gm[nw.g].index(nw.c), nw.amt, 0});
+    if (old.ex) tl_push(old.g, {v, old.si, (int64_t)((uint64_t)0 - (uint64_t)old.amt), 0});
+    if (nw.ex) tl_push(nw.g, {v, nw.si, nw.amt, 0});
     r = nw;
   }
 
@@ -616,11 +638,9 @@ int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, b
   o->n_events = pos;
   o->n_queries = (int64_t)(S - 1) * q;
   o->n_fixed = (int64_t)fixed.size();
-  size_t nsup = 0, ntl = 0;
-  for (int32_t g = 0; g < G; ++g) {
-    nsup += gm[g].cls.size();
-    ntl += tl[g].size();
-  }
+  size_t nsup = 0;
+  const size_t ntl = tlf.size();
+  for (int32_t g = 0; g < G; ++g) nsup += gm[g].cls.size();
   o->parent = new (std::nothrow) int32_t[S];
   o->queries = new (std::nothrow) BwQuery[o->n_queries ? o->n_queries : 1];
   o->fixed = new (std::nothrow) BwEvent[fixed.size() ? fixed.size() : 1];
@@ -638,18 +658,23 @@ int build_compact(const BwFixture& f, const Declared& w, int32_t S, int32_t q, b
   std::memcpy(o->parent, w.parent.data(), sizeof(int32_t) * S);
   std::memcpy(o->fixed, fixed.data(), fixed.size() * sizeof(BwEvent));
   std::memcpy(o->fixed_pos, fixed_pos.data(), fixed_pos.size() * 8);
-  size_t a = 0, b = 0;
+  size_t a = 0;
   for (int32_t g = 0; g < G; ++g) {
     o->sup_off[g] = (int64_t)a;
-    o->tl_off[g] = (int64_t)b;
     for (size_t i = 0; i < gm[g].cls.size(); ++i, ++a) {
       o->sup_cls[a] = (uint32_t)gm[g].cls[i];
       o->base_mass[a] = (int64_t)gm[g].mass[i];   // the walk leaves the state-0 masses as they are
     }
-    for (const BwTimeline& x : tl[g]) o->tl[b++] = x;
   }
   o->sup_off[G] = (int64_t)a;
-  o->tl_off[G] = (int64_t)b;
+  // timelines grouped by group, state order kept (stable counting sort)
+  for (int32_t g = 0; g <= G; ++g) o->tl_off[g] = 0;
+  for (int32_t g : tlg) ++o->tl_off[g + 1];
+  for (int32_t g = 0; g < G; ++g) o->tl_off[g + 1] += o->tl_off[g];
+  {
+    std::vector<int64_t> at(o->tl_off, o->tl_off + G);
+    for (size_t i = 0; i < ntl; ++i) o->tl[at[tlg[i]]++] = tlf[i];
+  }
   for (int32_t v = 1; v < S; ++v)
     for (int32_t k = 0; k < q; ++k) {
       const size_t qi = per_state ? (size_t)v * q + k : (size_t)k;
