@@ -69,6 +69,15 @@ struct Rng {
   }
   uint32_t bounded(uint32_t n) { return n ? (uint32_t)(next() % n) : 0u; }
   int64_t range(int64_t lo, int64_t hi) { return hi <= lo ? lo : lo + (int64_t)(next() % (uint64_t)(hi - lo)); }
+  // Counter property (batch_engine_v7c.hpp:244-249): the k-th draw (0-based) of a
+  // generator started at state s0 is mix(s0 + (k + 1) * gamma), independent of the
+  // draws before it.
+  static uint64_t at(uint64_t s0, uint64_t k) {
+    uint64_t z = s0 + (k + 1) * 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+  }
 };
 
 enum : uint8_t { OP_REPLACE = 0, OP_INSERT = 1, OP_DELETE = 2, OP_MOVE = 3, OP_FACTOR = 4 };
@@ -140,11 +149,18 @@ void declare(const BwFixture& f, const BwNativeSpec& sp, Declared& w) {
   w.parent.resize(S);
   for (int32_t v = 0; v < S; ++v) w.parent[v] = version_parent(sp.topology, v);
   w.edit.assign(S, Edit{});
+  // The edit stream in two phases, bit-identical to drawing it sequentially (the
+  // reference's v7c split, batch_engine_v7c.hpp:332-408): a cheap sequential pass
+  // decides every state's op, its insert slot and the index of its first draw; the
+  // edits are then materialised in parallel from the counter property.
+  const uint64_t s0 = rng.s;
+  std::vector<uint32_t> draw0((size_t)S, 0), ins_slot((size_t)S, 0);
   std::vector<int64_t> gfactor(G, 1000);
-  int32_t next_group = 0;
+  int32_t next_group = 0, n_ins = 0;
+  uint64_t k = 0;
   for (int32_t v = 1; v < S; ++v) {
     Edit& e = w.edit[v];
-    const bool factor_step = sp.factor_pct >= 0 ? rng.bounded(100) < (uint32_t)sp.factor_pct
+    const bool factor_step = sp.factor_pct >= 0 ? (uint32_t)(Rng::at(s0, k++) % 100u) < (uint32_t)sp.factor_pct
                                                 : (sp.factor_period > 0 && v % sp.factor_period == 0);
     if (factor_step) {
       const int32_t g = next_group++ % G;
@@ -154,29 +170,48 @@ void declare(const BwFixture& f, const BwNativeSpec& sp, Declared& w) {
       e.op = OP_FACTOR; e.g = g; e.val = nf;
       continue;
     }
-    const uint32_t roll = rng.bounded(100);
-    if (roll < 55) {
-      e.op = OP_REPLACE;
-      e.id = rng.range(0, N);
-      e.val = f.row_amt(e.id) + rng.range(-100000, 100000);
-    } else if (roll < 75) {
-      e.op = OP_INSERT;
-      e.id = N + (int64_t)w.ins_t.size();
-      e.t = rng.range(tmin, tmax + 1);
-      e.g = (int32_t)rng.bounded((uint32_t)G);
-      const int64_t base_amt = f.row_amt(rng.bounded((uint32_t)N));
-      e.val = base_amt + rng.range(-100000, 100000);
-      w.ins_t.push_back(e.t);
-      w.ins_g.push_back(e.g);
-    } else if (roll < 90) {
-      e.op = OP_DELETE;
-      e.id = rng.range(0, N);
-    } else {
-      e.op = OP_MOVE;
-      e.id = rng.range(0, N);
-      e.t = rng.range(tmin, tmax + 1);
-      e.g = (int32_t)rng.bounded((uint32_t)G);
-      e.val = f.row_amt(e.id) + rng.range(-100000, 100000);
+    const uint32_t roll = (uint32_t)(Rng::at(s0, k++) % 100u);
+    draw0[v] = (uint32_t)k;
+    if (roll < 55) { e.op = OP_REPLACE; k += 2; }
+    else if (roll < 75) { e.op = OP_INSERT; ins_slot[v] = (uint32_t)n_ins++; k += 4; }
+    else if (roll < 90) { e.op = OP_DELETE; k += 1; }
+    else { e.op = OP_MOVE; k += 4; }
+  }
+  w.ins_t.assign((size_t)n_ins, 0);
+  w.ins_g.assign((size_t)n_ins, 0);
+  auto range_at = [&](uint64_t kk, int64_t lo, int64_t hi) {
+    return hi <= lo ? lo : lo + (int64_t)(Rng::at(s0, kk) % (uint64_t)(hi - lo));
+  };
+  auto bounded_at = [&](uint64_t kk, uint32_t n) { return n ? (uint32_t)(Rng::at(s0, kk) % n) : 0u; };
+#pragma omp parallel for schedule(static)
+  for (int32_t v = 1; v < S; ++v) {
+    Edit& e = w.edit[v];
+    if (e.op == OP_FACTOR) continue;
+    uint64_t kk = draw0[v];
+    switch (e.op) {
+      case OP_REPLACE:
+        e.id = range_at(kk++, 0, N);
+        e.val = f.row_amt(e.id) + range_at(kk++, -100000, 100000);
+        break;
+      case OP_INSERT: {
+        e.id = N + (int64_t)ins_slot[v];
+        e.t = range_at(kk++, tmin, tmax + 1);
+        e.g = (int32_t)bounded_at(kk++, (uint32_t)G);
+        const int64_t base_amt = f.row_amt(bounded_at(kk++, (uint32_t)N));
+        e.val = base_amt + range_at(kk++, -100000, 100000);
+        w.ins_t[ins_slot[v]] = e.t;
+        w.ins_g[ins_slot[v]] = e.g;
+        break;
+      }
+      case OP_DELETE:
+        e.id = range_at(kk++, 0, N);
+        break;
+      default:   // move
+        e.id = range_at(kk++, 0, N);
+        e.t = range_at(kk++, tmin, tmax + 1);
+        e.g = (int32_t)bounded_at(kk++, (uint32_t)G);
+        e.val = f.row_amt(e.id) + range_at(kk++, -100000, 100000);
+        break;
     }
   }
 }

@@ -59,6 +59,18 @@ def test_host_sha_matches_oracle(bw, oracle_mod):
         assert bw.fnv1a(data[:n]) == oracle_mod.fnv1a(data[:n])
 
 
+@pytest.mark.parametrize("topology,factor_pct", [(0, 30), (1, 10), (2, 0), (0, 100)])
+def test_counter_based_edits_match_sequential_oracle(bw, oracle_mod, topology, factor_pct):
+    """The declared edit stream drawn in two phases (sequential op pass, parallel
+    materialisation from the counter property) equals the sequential draw order of
+    the oracle's make_workload restatement, on the BWH_FACTOR_PCT path too."""
+    fx = fixture("check")
+    w = bw.native_workload(fx, 257, topology, 13, 4, 2, True, factor_pct)
+    want = oracle_mod.direct_scan(oracle_mod.Fixture(fx), 257, topology, 13, 4, 2, True, factor_pct)
+    got = oracle_mod.ev_sweep(w.parent, w.n_keys, w.events, w.queries)
+    np.testing.assert_array_equal(got, want)
+
+
 def test_streaming_digest_equals_one_shot(bw):
     """The extract digests chunk by chunk: any split gives the one-shot SHA-256/FNV-1a."""
     rng = np.random.default_rng(5)
