@@ -47,7 +47,7 @@ Tuning to_tuning(const BwForestTuning* t) {
 int plan_spec(const BwForestShape* sh, const BwForestTuning* tu, PipeSpec& spec) {
   if (!sh || sh->n_trees < 1 || !sh->state_off || !sh->event_off || !sh->query_off || !sh->n_keys) return BW_EINVAL;
   if (tu && (tu->ctas_per_sm < 0 || tu->ctas_per_sm > 2 || tu->block_work < 0 || tu->slice_ranks < 0 ||
-             tu->tile < 0 || tu->tile > 5))
+             tu->tile < 0 || tu->tile > kTileMaxId))
     return BW_EINVAL;
   int sms = 0;
   int rc = sms_of_device(&sms);
@@ -218,7 +218,7 @@ extern "C" int bw_forest_plan_stats(const BwForestShape* sh, const BwForestTunin
   if (!sh || sh->n_trees < 1 || !sh->state_off || !sh->event_off || !sh->query_off || !sh->n_keys || sms < 1)
     return BW_EINVAL;
   if (tu && (tu->ctas_per_sm < 0 || tu->ctas_per_sm > 2 || tu->block_work < 0 || tu->slice_ranks < 0 ||
-             tu->tile < 0 || tu->tile > 5))
+             tu->tile < 0 || tu->tile > kTileMaxId))
     return BW_EINVAL;
   PipeSpec s;
   const int rc = pipe_spec_forest(sh->n_trees, sh->state_off, sh->event_off, sh->query_off, sh->n_keys, to_tuning(tu),
@@ -297,7 +297,7 @@ extern "C" int bw_forest_autotune(const BwForestShape* shape, const int32_t* par
     if ((rc = trial(c))) break;
   if (!rc && best_t >= 0.f) {   // the other tile geometries at the best block work
     const BwForestTuning base = *best;
-    for (int32_t tile = 1; tile <= 5 && !rc; ++tile) {
+    for (int32_t tile = 1; tile <= kTileMaxId && !rc; ++tile) {
       if (tile == base.tile) continue;
       BwForestTuning x = base;
       x.tile = tile;

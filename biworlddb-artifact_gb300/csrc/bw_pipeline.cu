@@ -2039,13 +2039,21 @@ static inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 static size_t sweep_budget(int ctas_per_sm) { return (size_t)(kSmemPerSM / ctas_per_sm) - 3072; }
 
 static void finish_spec(PipeSpec& s, const Tuning& tune) {
-  s.tile = tune.tile >= kTileNarrowId && tune.tile <= kTileSpec512Id ? tune.tile
+  s.tile = tune.tile >= kTileNarrowId && tune.tile <= kTileMaxId ? tune.tile
            : (s.Q * 8 >= s.E ? kTileNarrowId : kTileWideId);
   if (s.tile >= kTileNarrow512Id) s.ctas_per_sm = 1;   // a 512-thread CTA takes the SM's registers
   const int32_t nw = words_of(s.Cmax);
   const size_t bud = sweep_budget(s.ctas_per_sm);
   switch (s.tile) {
     case kTileWideId: s.SL = sweep_layout<TileWide>(nw, bud); break;
+    case kTileEulerId:
+      // the prepare pass cuts slices for the Euler sweep's window; the TileNarrow512
+      // layout (same capacities or less) stays valid for the k_sweep fallback taken
+      // when the events are not 16-byte aligned
+      s.SL = sweep_layout<TileNarrow512>(nw, bud);
+      s.SL.cap32 = std::min<uint32_t>(s.SL.cap32, kEsCap32);
+      s.SL.cap64 = std::min<uint32_t>(s.SL.cap64, kEsCap64);
+      break;
     case kTileNarrow512Id: s.SL = sweep_layout<TileNarrow512>(nw, bud); break;
     case kTileWide512Id: s.SL = sweep_layout<TileWide512>(nw, bud); break;
     case kTileSpec512Id: s.SL = sweep_layout<TileSpec512>(nw, bud); break;
@@ -2267,6 +2275,7 @@ static int ensure_attrs() {
   if ((rc = report(cudaFuncSetAttribute(k_sweep<TileWide512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         kSmemLimit - 1024), "smem attr")))
     return rc;
+  if ((rc = report((cudaError_t)esweep_attrs(), "smem attr"))) return rc;
   if (dev >= 0 && dev < 64) done[dev] = true;
   return 0;
 }
@@ -2426,7 +2435,23 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
     sp.bits = pp.bits; sp.rlut = pp.rlut; sp.slices = pp.slices; sp.nslices = pp.nslices; sp.carry = pp.carry;
     sp.answers = answers; sp.status = status; sp.bmode = bmode; sp.ticket = misc + M_SWEEP_TICKET;
     const int sgrid = std::min(B, s.ctas_per_sm * s.sms);
+    const bool ev16 = (reinterpret_cast<uintptr_t>(events) & 15u) == 0;
+    if (s.tile == kTileEulerId && ev16) {
+      EsParams ep;
+      ep.ev = reinterpret_cast<const uint4*>(events); ep.qs = queries; ep.desc = desc; ep.blocks = blocks;
+      ep.order = order; ep.B = B; ep.cap32 = SL.cap32; ep.cap64 = SL.cap64;
+      ep.bits = pp.bits; ep.rlut = pp.rlut; ep.slices = pp.slices; ep.nslices = pp.nslices; ep.carry = pp.carry;
+      ep.answers = answers; ep.status = status; ep.bmode = bmode; ep.ticket = misc + M_SWEEP_TICKET;
+      if ((rc = report((cudaError_t)esweep_launch(ep, std::min(B, s.sms), st), "k_esweep"))) return rc;
+      ++kernels;
+      if ((rc = mark(6))) return rc;
+      if (kernels_out) *kernels_out = kernels;
+      return 0;
+    }
     switch (s.tile) {
+      case kTileEulerId:   // events not 16-byte aligned: the same slices through k_sweep
+        k_sweep<TileNarrow512><<<sgrid, TileNarrow512::kThreads, SL.bytes, st>>>(sp, SL);
+        break;
       case kTileWideId: k_sweep<TileWide><<<sgrid, TileWide::kThreads, SL.bytes, st>>>(sp, SL); break;
       case kTileNarrow512Id:
         k_sweep<TileNarrow512><<<sgrid, TileNarrow512::kThreads, SL.bytes, st>>>(sp, SL);

@@ -79,7 +79,14 @@ using TileWide = TileCfg<4, 1, 64, 256, 256, true, true>;          // event-heav
 using TileNarrow512 = TileCfg<2, 1, 128, 512, 512, false, true>;   // 16 warps (one CTA per SM), own staging, flat
 using TileWide512 = TileCfg<2, 1, 64, 256, 512, true, true>;
 using TileSpec512 = TileCfg<1, 1, 64, 512, 512, false, true, true>;   // 15 replay warps + 1 staging warp
-enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4, kTileSpec512Id = 5 };
+// kTileEulerId: the Euler-tile sweep of bw_esweep.cu (bulk-copied signed event tiles,
+// flat window, a producer warp; one CTA per SM) instead of k_sweep.
+enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4, kTileSpec512Id = 5,
+       kTileEulerId = 6 };
+constexpr int kTileMaxId = 6;
+// Window capacity of the Euler-tile sweep: int32 entries, or int64 ones in the same bytes.
+constexpr uint32_t kEsCap32 = 32768;
+constexpr uint32_t kEsCap64 = 16384;
 
 // ------------------------------------------------------------------ records
 struct StepDesc {        // one Euler step, 16 bytes
@@ -242,6 +249,29 @@ int pipe_bind(const PipeSpec& spec, void* workspace, cudaStream_t st);
 // Enqueue the whole pipeline (kernels and memsets only: capturable in a CUDA graph).
 int pipe_enqueue(const PipeSpec& spec, void* workspace, const int32_t* parent, const BwEvent* events,
                  const BwQuery* queries, int64_t* answers, cudaStream_t st, EventSet* timing, int* kernels);
+// Euler-tile sweep (bw_esweep.cu): the inputs of k_sweep, the rank capacities the
+// prepare pass cut the slices with, events as 16-byte records (16-byte aligned).
+struct EsParams {
+  const uint4* ev;
+  const BwQuery* qs;
+  const StepDesc* desc;
+  const BlockTab* blocks;
+  const int32_t* order;   // queue order (NULL: identity)
+  int32_t B;
+  uint32_t cap32, cap64;
+  const uint64_t* bits;
+  const uint32_t* rlut;
+  const Slice* slices;
+  const int32_t* nslices;
+  const int64_t* carry;
+  int64_t* answers;
+  int32_t* status;
+  const int32_t* bmode;
+  int32_t* ticket;
+};
+int esweep_attrs();   // one-time shared-memory opt-in (cudaError_t as int)
+int esweep_launch(const EsParams& p, int grid, cudaStream_t st);
+
 // Device address of the status word inside a workspace laid out for `spec`.
 const int32_t* pipe_status_word(const PipeSpec& spec, const void* workspace);
 int report(cudaError_t e, const char* what);

@@ -49,6 +49,11 @@ def run_forest(bw, torch, F, tuning=None):
     (9, 40, {"tile": 4, "block_work": 65536}),           # wide tiles on 512 threads
     (10, 40, {"tile": 5}),                               # one staging warp + 15 replay warps
     (13, 60, {"tile": 5, "block_work": 65536, "slice_ranks": 512}),
+    (14, 60, {"tile": 6}),                               # Euler-tile sweep (bulk-copied signed tiles)
+    (15, 40, {"tile": 6, "block_work": 65536}),
+    (16, 60, {"tile": 6, "block_work": 65536, "slice_ranks": 512}),   # several slices per block
+    (17, 25, {"tile": 6, "block_work": 20000}),          # > 16 carry rows per tree
+    (18, 120, {"tile": 6, "slice_ranks": 2048}),
 ])
 def test_forest_matches_oracle(bw, torch_cuda, oracle_mod, seed, T, tuning):
     rng = np.random.default_rng(seed)
@@ -58,7 +63,7 @@ def test_forest_matches_oracle(bw, torch_cuda, oracle_mod, seed, T, tuning):
     np.testing.assert_array_equal(got, want)
 
 
-@pytest.mark.parametrize("tile", [0, 5])
+@pytest.mark.parametrize("tile", [0, 5, 6])
 def test_forest_wrapping_deltas(bw, torch_cuda, oracle_mod, tile):
     rng = np.random.default_rng(11)
     F = make_forest(rng, 30, max_states=800, big=True)
@@ -66,7 +71,7 @@ def test_forest_wrapping_deltas(bw, torch_cuda, oracle_mod, tile):
                                   oracle_mod.ev_forest(*F))
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5, 6])
 def test_forest_heavy_states_all_tiles(bw, torch_cuda, oracle_mod, tile):
     """States with more events and more queries than one sweep tile stages, in
     query-dense and query-sparse trees, under every tile geometry (single-probe and
@@ -169,7 +174,8 @@ def test_forest_shape_errors(bw, torch_cuda):
         bw.Forest([0, 3], [0, 2], [0, 1], [0])           # empty key domain
 
 
-@pytest.mark.parametrize("tuning", [None, {"tile": 3}, {"tile": 4, "block_work": 200000}, {"tile": 5}])
+@pytest.mark.parametrize("tuning", [None, {"tile": 3}, {"tile": 4, "block_work": 200000}, {"tile": 5},
+                                    {"tile": 6}, {"tile": 6, "block_work": 200000}])
 def test_one_tree_forest_equals_plain(bw, torch_cuda, tuning):
     """A forest of one tree is the plain replay (its uploaded tables, not the
     plain path's per-launch ones)."""

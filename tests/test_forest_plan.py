@@ -22,7 +22,7 @@ def test_every_tree_has_a_block(bw, forest):
     assert st["blocks"] == forest.n_trees and st["carry_bytes"] == 0
 
 
-@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("ctas", [1, 2])
 def test_block_work_monotone_and_carry_budget(bw, forest, tile, ctas):
     prev = None
@@ -43,7 +43,7 @@ def test_carry_budget_caps_huge_domains(bw):
 
 def test_unknown_tile_refused(bw, forest):
     with pytest.raises(RuntimeError):
-        bw.forest_plan_stats(*args(forest), tuning={"tile": 6})
+        bw.forest_plan_stats(*args(forest), tuning={"tile": 7})
 
 
 def test_malformed_shapes_refused(bw):
