@@ -34,7 +34,8 @@ record as the line (``--scale`` multiplies the sizes).
 * e2e: the same through the public API with pinned host buffers: every step
   copies parent/events/queries host->device and the answers device->host.
 * roofline: the dominant kernel -- the chain sweep (k_chain_sweep) on chains, the
-  tree sweep (k_sweep) otherwise -- with its algorithmic bytes (16 per event
+  Euler-tile tree sweep (k_esweep) on forests, the tree sweep (k_sweep) on single
+  trees -- with its algorithmic bytes (16 per event
   record, 12 per query record, 8 per answer) over its mean launch time (CUDA
   events on the launch stream), against the measured HBM copy bandwidth.
 * cpu_baseline: the oracle's restatement of the reference's CPU path on the box's
@@ -842,6 +843,7 @@ def bench_batched(args):
 
     peak, peak_kind = measured_peaks()
     sweep_bytes = 16 * E + 20 * Q
+    sweep_kernel = "k_esweep" if int(info["tuning"].get("tile", 0)) == 6 else "k_sweep"   # tile 6: Euler-tile sweep
     top = max(stage_ms, key=stage_ms.get)
     achieved = sweep_bytes / (stage_ms["sweep"] / 1e3) / 1e9
     value = ws * Q / (ms / 1e3)
@@ -858,9 +860,9 @@ def bench_batched(args):
                   "launches_per_step": T, "kernels_per_step": plain_kernels // max(1, args.plain_steps),
                   "form": "one bw_replay_launch per tree, sequential on one stream"},
         "batched_vs_plain": value / plain_value if plain_value else None,
-        "roofline": {"bound": "hbm", "kernel": "k_sweep", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": sweep_kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
-                     "traffic": profiled_traffic("k_sweep", w.name),
+                     "traffic": profiled_traffic(sweep_kernel, w.name),
                      "algorithmic_bytes_per_launch": sweep_bytes, "mean_launch_ms": stage_ms["sweep"]},
         "pipeline": {"stages_ms": stage_ms, "dominant_stage": top,
                      "whole_step_gbs": w.algorithmic_bytes / (ms / 1e3) / 1e9,

@@ -52,7 +52,7 @@ constexpr int kEsStages = 3;
 constexpr int kEsQB = 64;                  // queries per tile
 constexpr int kEsQW = kEsQB / kEsNWC;      // queries per consumer warp per tile
 constexpr uint32_t kEsFlat = 4096;         // windows up to this size keep no chunk totals
-constexpr int kEsRing = 128;               // producer's descriptor ring (steps)
+constexpr int kEsRing = 256;               // planner's descriptor ring (steps)
 constexpr uint32_t kEsWaitLimit = 1u << 22;
 constexpr uint32_t kFull = 0xffffffffu;
 
@@ -65,7 +65,7 @@ struct EsCtl {
 
 // Dynamic shared memory (all regions 16-byte aligned).
 struct EsSmem {
-  size_t H, T, bits, rl, stage, q, meta, bar, ctl, ring, plan, pmeta, bytes;
+  size_t H, T, bits, rl, stage, pack, q, meta, bar, ctl, ring, plan, pmeta, bytes;
 };
 __host__ __device__ constexpr size_t es_al(size_t x) { return (x + 15) & ~size_t(15); }
 __host__ __device__ constexpr EsSmem es_smem() {
@@ -76,12 +76,13 @@ __host__ __device__ constexpr EsSmem es_smem() {
   L.bits = o;  o = es_al(o + (size_t)kWinWords * 8);
   L.rl = o;    o = es_al(o + ((size_t)kWinWords + 2) * 2);          // slice-local ranks, uint16
   L.stage = o; o = es_al(o + (size_t)kEsStages * kEsTile * 16);
+  L.pack = o;  o = es_al(o + (size_t)kEsTile * 8);                   // the tile as signed (key, int32 delta)
   L.q = o;     o = es_al(o + (size_t)kEsStages * kEsQB * 16);
   L.meta = o;  o = es_al(o + (size_t)kEsStages * sizeof(EsMeta));
   L.bar = o;   o = es_al(o + (size_t)2 * kEsStages * 8);
   L.ctl = o;   o = es_al(o + sizeof(EsCtl));
   L.ring = o;  o = es_al(o + (size_t)kEsRing * 16);
-  L.plan = o;  o = es_al(o + (size_t)2 * 32 * 16);                  // two batch plans
+  L.plan = o;  o = es_al(o + (size_t)2 * 64 * 16);                  // two batch plans
   L.pmeta = o; o = es_al(o + (size_t)2 * 16);
   L.bytes = o;
   return L;
@@ -168,17 +169,16 @@ struct EsPass {
 
 // ------------------------------------------------------------------ producer
 // Two warps: the planner walks the descriptors and cuts the tiles; the issuer merges
-// copy groups and issues the copies.  They hand 32-step batch plans over through two
-// shared plan buffers, each guarded by a pair of named barriers (plan b written:
-// kBarPlanFull + b; plan b read: kBarPlanFree + b; 64 threads each).
+// copy groups and issues the copies.  A batch is 64 consecutive steps, two per lane
+// (lane l: steps 2l and 2l + 1).  Batch plans go from the planner to the issuer
+// through two shared plan buffers, each guarded by a pair of named barriers (plan b
+// written: kBarPlanFull + b; plan b read: kBarPlanFree + b; 64 threads each).
 constexpr int kBarPlanFull = 2;
 constexpr int kBarPlanFree = 4;
+constexpr int kEsBatch = 64;
 __device__ __forceinline__ void pbar_arrive(int id) { asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory"); }
 __device__ __forceinline__ void pbar_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
 
-// One lane's part of a batch plan: its step's taken events [src, src + te) with their
-// sign, its taken queries [q0, q0 + tq) and their first slot xq in the batch, the front
-// slot of an enter step's first event and the exit events of the tile before it.
 struct EsPlanMeta {
   uint32_t nq;     // queries of the tile before the batch | after it << 16
   uint32_t flags;  // 1: the batch ends its tile, 2: it ends the pass
@@ -188,26 +188,38 @@ constexpr uint32_t kPlanTileEnd = 1, kPlanPassEnd = 2;
 
 // The planner's cursor: step ct with its first coe events and coq queries already
 // taken; the descriptors of steps below wb have been requested into the ring (slot
-// u % kEsRing), 32 steps per cp.async group, up to 96 steps ahead of the cursor.
+// u % kEsRing), 32 steps per cp.async group, up to kEsRing - kEsBatch steps ahead.
 struct EsCursor {
   int32_t ct, coe, coq, wb;
 };
 __device__ __forceinline__ void es_ring_request(const EsParams& p, uint4* ring, EsCursor& c, int32_t t1, int lane) {
-  while (c.wb < t1 && c.wb < c.ct + 96) {
+  while (c.wb < t1 && c.wb < c.ct + (kEsRing - kEsBatch)) {
     const int32_t u = c.wb + lane;
     if (u < t1) cp_async16(ring + (u & (kEsRing - 1)), p.desc + u);
     asm volatile("cp.async.commit_group;" ::: "memory");
     c.wb += 32;
   }
 }
-// Wait until the descriptors of steps [ct, ct + 32) have landed (the groups of later
-// steps may stay in flight), then make them visible to the whole warp.
+// Wait until the descriptors of steps [ct, ct + kEsBatch) have landed (the groups of
+// later steps may stay in flight), then make them visible to the whole warp.
 __device__ __forceinline__ void es_ring_ready(const EsCursor& c, int32_t t0) {
-  const int32_t later = (c.wb - t0) / 32 - (c.ct + 31 - t0) / 32 - 1;   // groups past step ct + 31
-  if (later >= 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
+  const int32_t later = (c.wb - t0) / 32 - (c.ct + kEsBatch - 1 - t0) / 32 - 1;   // groups past the batch
+  if (later >= 5) asm volatile("cp.async.wait_group 5;" ::: "memory");
+  else if (later == 4) asm volatile("cp.async.wait_group 4;" ::: "memory");
+  else if (later == 3) asm volatile("cp.async.wait_group 3;" ::: "memory");
+  else if (later == 2) asm volatile("cp.async.wait_group 2;" ::: "memory");
   else if (later == 1) asm volatile("cp.async.wait_group 1;" ::: "memory");
   else asm volatile("cp.async.wait_group 0;" ::: "memory");
   __syncwarp();
+}
+
+// One step's part of a batch plan: events [src, src + te) of sign ex, queries
+// [q0, q0 + tq) with their first slot xq in the batch, the front slot of an enter
+// step's first event and the exit events of the tile before the step.
+__device__ __forceinline__ uint4 es_rec(uint32_t src, uint32_t q0, int32_t te, bool ex, int32_t tq, int32_t xq,
+                                        int32_t fpos, int32_t boff) {
+  return make_uint4(src, q0, (uint32_t)te | (ex ? 1u << 11 : 0u) | ((uint32_t)tq << 12) | ((uint32_t)xq << 19),
+                    (uint32_t)fpos | ((uint32_t)boff << 16));
 }
 
 // Planner: every batch of the pass, tiles cut at kEsTile events or kEsQB queries.
@@ -221,75 +233,92 @@ __device__ void es_plan(const EsParams& p, const EsPass& ps, uint4* ring, uint4*
   uint32_t pb = 0;                  // batches planned in this pass
   for (;;) {
     const bool stop = *reinterpret_cast<const volatile int32_t*>(&ctl->abort) != 0;
-    uint4 rec = make_uint4(0, 0, 0, 0);
+    uint4 rec0 = make_uint4(0, 0, 0, 0), rec1 = rec0;
     uint32_t flags = 0, nq0 = (uint32_t)nq;
     if (stop) {
       flags = kPlanTileEnd | kPlanPassEnd;
     } else {
       es_ring_request(p, ring, c, t1, lane);
       es_ring_ready(c, ps.t0);
-      const int32_t u = c.ct + lane;
-      const bool valid = u < t1;
-      const uint4 dv = ring[u & (kEsRing - 1)];   // StepDesc {e0, q0, ne, nq}
-      const int32_t dnq = (int32_t)dv.w;
-      const bool ex = dnq < 0;
-      int32_t ne = valid ? (int32_t)dv.z : 0, qn = valid && dnq > 0 ? dnq : 0;
-      uint32_t src = dv.x, q0 = dv.y;
+      const int32_t u0 = c.ct + 2 * lane, u1 = u0 + 1;
+      const bool v0 = u0 < t1, v1 = u1 < t1;
+      const uint4 d0 = ring[u0 & (kEsRing - 1)], d1 = ring[u1 & (kEsRing - 1)];   // StepDesc {e0, q0, ne, nq}
+      const bool ex0 = (int32_t)d0.w < 0, ex1 = (int32_t)d1.w < 0;
+      int32_t ne0 = v0 ? (int32_t)d0.z : 0, qn0 = v0 && (int32_t)d0.w > 0 ? (int32_t)d0.w : 0;
+      const int32_t ne1 = v1 ? (int32_t)d1.z : 0, qn1 = v1 && (int32_t)d1.w > 0 ? (int32_t)d1.w : 0;
+      uint32_t src0 = d0.x, qa0 = d0.y;
       if (lane == 0) {
-        ne -= c.coe; src += (uint32_t)c.coe;
-        qn -= c.coq; q0 += (uint32_t)c.coq;
+        ne0 -= c.coe; src0 += (uint32_t)c.coe;
+        qn0 -= c.coq; qa0 += (uint32_t)c.coq;
       }
-      // packed scans of the counts, each clamped below the tile limits (a lane that
-      // fits has exact counts; the first one that does not is the only one cut):
-      // events | queries << 16, and exit events
-      const uint32_t cne = (uint32_t)min(ne, 2047), cqn = (uint32_t)min(qn, 127);
-      uint32_t pk = cne | (cqn << 16), px = ex ? cne : 0u;
+      // counts clamped below the tile limits (a step that fits has exact counts; the
+      // first one that does not is the only one cut), summed per lane (saturating: a
+      // lane past the cut is never used), then scanned over the lanes
+      const int32_t c0 = min(ne0, kEsTile + 1), c1 = min(ne1, kEsTile + 1);
+      const int32_t cq0 = min(qn0, kEsQB + 1), cq1 = min(qn1, kEsQB + 1);
+      const uint32_t pe = (uint32_t)min(c0 + c1, 2047), pq = (uint32_t)min(cq0 + cq1, 127);
+      const uint32_t pxv = (uint32_t)min((ex0 ? c0 : 0) + (ex1 ? c1 : 0), 2047);
+      uint32_t sa = pe | (pq << 16), sx = pxv;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(kFull, pk, o), yx = __shfl_up_sync(kFull, px, o);
-        if (lane >= o) { pk += y; px += yx; }
+        const uint32_t y = __shfl_up_sync(kFull, sa, o), yx = __shfl_up_sync(kFull, sx, o);
+        if (lane >= o) { sa += y; sx += yx; }
       }
-      const int32_t xe = (int32_t)(pk & 0xffffu) - (int32_t)cne, xq = (int32_t)(pk >> 16) - (int32_t)cqn;
-      const int32_t xx = (int32_t)px - (ex ? (int32_t)cne : 0);   // exit events before the lane
+      const int32_t xe = (int32_t)(sa & 0xffffu) - (int32_t)pe;   // events before the lane's pair
+      const int32_t xq = (int32_t)(sa >> 16) - (int32_t)pq;       // queries before it
+      const int32_t xx = (int32_t)sx - (int32_t)pxv;              // exit events before it
       const int32_t room_e = kEsTile - nf - nb, room_q = kEsQB - nq;
-      // lanes below k take their whole step (events and queries); lane k takes what fits
-      const uint32_t fm = __ballot_sync(kFull, valid && xe + (int32_t)cne <= room_e && xq + (int32_t)cqn <= room_q);
-      const int k = fm == kFull ? 32 : __ffs(~fm) - 1;
-      int32_t te = 0, tq = 0;
-      if (lane < k) {
-        te = ne; tq = qn;
-      } else if (lane == k && valid) {
-        te = min(ne, room_e - xe);
-        tq = te == ne ? min(qn, room_q - xq) : 0;
+      const bool f0 = v0 && xe + c0 <= room_e && xq + cq0 <= room_q;
+      const bool f1 = f0 && v1 && xe + c0 + c1 <= room_e && xq + cq0 + cq1 <= room_q;
+      // K: the first step of the batch that is not taken whole (64: none)
+      const uint32_t m1 = __ballot_sync(kFull, !f1);
+      int K = 64;
+      if (m1) {
+        const int L = __ffs(m1) - 1;
+        K = 2 * L + (__shfl_sync(kFull, f0 ? 1 : 0, L) ? 1 : 0);
       }
-      const int32_t fpos = nf + (xe - xx);   // front slot of an enter lane's first event
-      const int32_t boff = nb + xx;          // exit events of the tile before an exit lane's
-      rec.x = src;
-      rec.y = q0;
-      rec.z = (uint32_t)te | (ex ? 1u << 11 : 0u) | ((uint32_t)tq << 12) | ((uint32_t)xq << 19);
-      rec.w = (uint32_t)fpos | ((uint32_t)boff << 16);
-      const uint32_t tt = (uint32_t)te | ((uint32_t)tq << 16);   // te <= kEsTile, tq <= kEsQB
+      int32_t te0 = 0, tq0 = 0, te1 = 0, tq1 = 0;
+      const int s0i = 2 * lane, s1i = s0i + 1;
+      if (s0i < K) {
+        te0 = ne0; tq0 = qn0;
+      } else if (s0i == K && v0) {
+        te0 = min(ne0, room_e - xe);
+        tq0 = te0 == ne0 ? min(qn0, room_q - xq) : 0;
+      }
+      if (s1i < K) {
+        te1 = ne1; tq1 = qn1;
+      } else if (s1i == K && v1) {
+        te1 = min(ne1, room_e - xe - c0);
+        tq1 = te1 == ne1 ? min(qn1, room_q - xq - cq0) : 0;
+      }
+      const int32_t fpos0 = nf + (xe - xx), boff0 = nb + xx;
+      const int32_t fpos1 = fpos0 + (ex0 ? 0 : te0), boff1 = boff0 + (ex0 ? te0 : 0);
+      rec0 = es_rec(src0, qa0, te0, ex0, tq0, xq, fpos0, boff0);
+      rec1 = es_rec(d1.x, d1.y, te1, ex1, tq1, xq + tq0, fpos1, boff1);
+      const uint32_t tt = (uint32_t)(te0 + te1) | ((uint32_t)(tq0 + tq1) << 16);   // <= kEsTile, kEsQB
       const uint32_t sum = __reduce_add_sync(kFull, tt);
-      const uint32_t xsum = __reduce_add_sync(kFull, ex ? (uint32_t)te : 0u);
+      const uint32_t xsum = __reduce_add_sync(kFull, (uint32_t)((ex0 ? te0 : 0) + (ex1 ? te1 : 0)));
       nb += (int32_t)xsum;
       nf += (int32_t)(sum & 0xffffu) - (int32_t)xsum;
       nq += (int32_t)(sum >> 16);
-      if (k == 32) {
-        c.ct += 32; c.coe = 0; c.coq = 0;
-      } else if (c.ct + k >= t1) {
+      if (K == 64) {
+        c.ct += 64; c.coe = 0; c.coq = 0;
+      } else if (c.ct + K >= t1) {
         c.ct = t1; c.coe = 0; c.coq = 0;
       } else {
-        const uint32_t kt = __shfl_sync(kFull, tt, k);
-        c.coe = (k == 0 ? c.coe : 0) + (int32_t)(kt & 0xffffu);
-        c.coq = (k == 0 ? c.coq : 0) + (int32_t)(kt >> 16);
-        c.ct += k;
+        const uint32_t kt = __shfl_sync(kFull, (K & 1) ? ((uint32_t)te1 | ((uint32_t)tq1 << 16))
+                                                       : ((uint32_t)te0 | ((uint32_t)tq0 << 16)), K >> 1);
+        c.coe = (K == 0 ? c.coe : 0) + (int32_t)(kt & 0xffffu);
+        c.coq = (K == 0 ? c.coq : 0) + (int32_t)(kt >> 16);
+        c.ct += K;
       }
       if (c.ct >= t1) flags = kPlanTileEnd | kPlanPassEnd;
       else if (nf + nb >= kEsTile || nq >= kEsQB) flags = kPlanTileEnd;
     }
     const int b = (int)(pb & 1u);
     if (pb >= 2) pbar_sync(kBarPlanFree + b);   // the issuer has read this buffer's last plan
-    plan[b * 32 + lane] = rec;
+    plan[b * kEsBatch + 2 * lane] = rec0;
+    plan[b * kEsBatch + 2 * lane + 1] = rec1;
     if (lane == 0) {
       EsPlanMeta m;
       m.nq = nq0 | ((uint32_t)nq << 16); m.flags = flags; m.nf = (uint32_t)nf; m.nb = (uint32_t)nb;
@@ -303,6 +332,15 @@ __device__ void es_plan(const EsParams& p, const EsPass& ps, uint4* ring, uint4*
   // balance the free barriers of the last (up to) two plans
   for (uint32_t q = pb > 2 ? pb - 2 : 0; q < pb; ++q) pbar_sync(kBarPlanFree + (int)(q & 1u));
   asm volatile("cp.async.wait_all;" ::: "memory");   // ring copies of this pass landed
+}
+
+// Next copy-group break after batch position i = 2 * lane + w (0..63; 64 if none):
+// break bits b0 (even positions, one per lane) and b1 (odd positions).
+__device__ __forceinline__ int es_next_break(uint32_t b0, uint32_t b1, int lane, int w) {
+  const uint32_t hi0 = lane + 1 < 32 ? (b0 & (kFull << (lane + 1))) : 0u;                 // even positions > 2 lane
+  const uint32_t hi1 = w == 0 ? (b1 & (kFull << lane)) : (lane + 1 < 32 ? (b1 & (kFull << (lane + 1))) : 0u);
+  const int e = hi0 ? 2 * (__ffs(hi0) - 1) : 64, o = hi1 ? 2 * (__ffs(hi1) - 1) + 1 : 64;
+  return e < o ? e : o;
 }
 
 // Issuer: turns the plans of a pass into stage copies, query records and stage
@@ -332,7 +370,7 @@ __device__ bool es_issue(const EsParams& p, unsigned char* sm, const uint4* plan
     }
     const int b = (int)(pb & 1u);
     pbar_sync(kBarPlanFull + b);
-    const uint4 rec = plan[b * 32 + lane];
+    const uint4 r0 = plan[b * kEsBatch + 2 * lane], r1 = plan[b * kEsBatch + 2 * lane + 1];
     const EsPlanMeta m = pmeta[b];
     pbar_arrive(kBarPlanFree + b);
     ++pb;
@@ -340,41 +378,56 @@ __device__ bool es_issue(const EsParams& p, unsigned char* sm, const uint4* plan
       uint4* sg = stages + (size_t)st * kEsTile;
       uint4* ql = qls + (size_t)st * kEsQB;
       uint64_t* fb = &full[st];
-      const uint32_t a = rec.x, te = rec.z & 0x7ffu, tq = (rec.z >> 12) & 0x7fu, xq = rec.z >> 19;
-      const bool ex = (rec.z >> 11) & 1u;
-      const int32_t fpos = (int32_t)(rec.w & 0xffffu), boff = (int32_t)(rec.w >> 16);
-      const uint32_t z = a + te, tx = te | (ex ? 0x80000000u : 0u);
-      // copy groups: a lane joins the previous lane's group when both take events of
-      // the same sign from adjacent ranges (ascending: a run of enters; descending: a
-      // run of exits, whose order inside the group does not matter -- no query sits
-      // between exits).  An enter group lands at [fpos, fpos + n) in step order, an
-      // exit group at [kEsTile - boff - n, kEsTile - boff).
-      const uint32_t pa = __shfl_up_sync(kFull, a, 1), pz = __shfl_up_sync(kFull, z, 1);
-      const uint32_t ptx = __shfl_up_sync(kFull, tx, 1);
-      const bool merge = lane > 0 && te > 0 && (ptx & 0x7fffffffu) != 0 && (ptx >> 31) == (tx >> 31) &&
-                         (pz == a || (ex && z == pa));
-      const bool head = te > 0 && !merge;
-      const uint32_t brk = __ballot_sync(kFull, head || te == 0);
-      const uint32_t after = lane == 31 ? 0u : (brk & (kFull << (lane + 1)));
-      const int lastl = after ? __ffs(after) - 2 : 31;
-      const uint32_t la = __shfl_sync(kFull, a, lastl), lz = __shfl_sync(kFull, z, lastl);
-      const uint32_t bytes = __reduce_add_sync(kFull, te) * 16u;
+      const uint32_t te0 = r0.z & 0x7ffu, te1 = r1.z & 0x7ffu;
+      const bool ex0 = (r0.z >> 11) & 1u, ex1 = (r1.z >> 11) & 1u;
+      const uint32_t a0 = r0.x, z0 = a0 + te0, a1 = r1.x, z1 = a1 + te1;
+      // copy groups in step order: a step joins the previous step's group when both
+      // take events of the same sign from adjacent ranges (ascending: a run of enters;
+      // descending: a run of exits, whose order inside the group does not matter -- no
+      // query sits between exits).  An enter group lands at [fpos, fpos + n) in step
+      // order, an exit group at [kEsTile - boff - n, kEsTile - boff).
+      const uint32_t pa = __shfl_up_sync(kFull, a1, 1), pz = __shfl_up_sync(kFull, z1, 1);
+      const uint32_t ptx = __shfl_up_sync(kFull, te1 | (ex1 ? 0x80000000u : 0u), 1);
+      const bool mg0 = lane > 0 && te0 > 0 && (ptx & 0x7fffffffu) != 0 && (ptx >> 31) == (ex0 ? 1u : 0u) &&
+                       (pz == a0 || (ex0 && z0 == pa));
+      const bool mg1 = te1 > 0 && te0 > 0 && ex0 == ex1 && (z0 == a1 || (ex1 && z1 == a0));
+      const bool h0 = te0 > 0 && !mg0, h1 = te1 > 0 && !mg1;
+      const uint32_t b0 = __ballot_sync(kFull, h0 || te0 == 0), b1 = __ballot_sync(kFull, h1 || te1 == 0);
+      // the last member of each head's group: the step before the next break
+      const int l0 = es_next_break(b0, b1, lane, 0) - 1, l1 = es_next_break(b0, b1, lane, 1) - 1;
+      const uint32_t x0a = __shfl_sync(kFull, a0, l0 >> 1), x0b = __shfl_sync(kFull, a1, l0 >> 1);
+      const uint32_t y0a = __shfl_sync(kFull, z0, l0 >> 1), y0b = __shfl_sync(kFull, z1, l0 >> 1);
+      const uint32_t x1a = __shfl_sync(kFull, a0, l1 >> 1), x1b = __shfl_sync(kFull, a1, l1 >> 1);
+      const uint32_t y1a = __shfl_sync(kFull, z0, l1 >> 1), y1b = __shfl_sync(kFull, z1, l1 >> 1);
+      const uint32_t la0 = (l0 & 1) ? x0b : x0a, lz0 = (l0 & 1) ? y0b : y0a;
+      const uint32_t la1 = (l1 & 1) ? x1b : x1a, lz1 = (l1 & 1) ? y1b : y1a;
+      const uint32_t bytes = __reduce_add_sync(kFull, te0 + te1) * 16u;
       if (lane == 0 && bytes) mbar_expect(fb, bytes);   // the batch's bytes, before its copies
       __syncwarp();
-      if (head) {
-        const uint32_t s0 = a < la ? a : la, s1 = z > lz ? z : lz, n = s1 - s0;
-        const int32_t slot = ex ? kEsTile - boff - (int32_t)n : fpos;
+      if (h0) {
+        const uint32_t s0 = a0 < la0 ? a0 : la0, s1 = z0 > lz0 ? z0 : lz0, n = s1 - s0;
+        const int32_t slot = ex0 ? kEsTile - (int32_t)(r0.w >> 16) - (int32_t)n : (int32_t)(r0.w & 0xffffu);
+        bulk_copy(sg + slot, p.ev + s0, n * 16u, fb);
+      }
+      if (h1) {
+        const uint32_t s0 = a1 < la1 ? a1 : la1, s1 = z1 > lz1 ? z1 : lz1, n = s1 - s0;
+        const int32_t slot = ex1 ? kEsTile - (int32_t)(r1.w >> 16) - (int32_t)n : (int32_t)(r1.w & 0xffffu);
         bulk_copy(sg + slot, p.ev + s0, n * 16u, fb);
       }
       // queries of an enter step: after all of its events; bounds by cp.async
-      for (uint32_t r = 0; r < tq; ++r) {
-        const uint32_t* qr = reinterpret_cast<const uint32_t*>(p.qs + (rec.y + r));
-        uint4* e = ql + ((m.nq & 0xffffu) + xq + r);
-        cp_async4(&e->x, qr + 1);
-        cp_async4(&e->y, qr + 2);
-        e->z = (uint32_t)(fpos + (int32_t)te) | ((uint32_t)boff << 16);
-        e->w = rec.y + r;
-        qcopies = true;
+#pragma unroll
+      for (int w = 0; w < 2; ++w) {
+        const uint4 rr = w ? r1 : r0;
+        const uint32_t te = rr.z & 0x7ffu, tq = (rr.z >> 12) & 0x7fu, xq = rr.z >> 19;
+        for (uint32_t r = 0; r < tq; ++r) {
+          const uint32_t* qr = reinterpret_cast<const uint32_t*>(p.qs + (rr.y + r));
+          uint4* e = ql + ((m.nq & 0xffffu) + xq + r);
+          cp_async4(&e->x, qr + 1);
+          cp_async4(&e->y, qr + 2);
+          e->z = ((rr.w & 0xffffu) + te) | (rr.w & 0xffff0000u);
+          e->w = rr.y + r;
+          qcopies = true;
+        }
       }
       if (m.flags & kPlanTileEnd) {
         if (lane == 0) {
@@ -449,6 +502,18 @@ __device__ __forceinline__ HT es_scan(const uint4* tile, uint32_t j0, uint32_t j
   return s;
 }
 
+// Lane share of the signed delta sum of packed events [j0, j1) with keys in [a, a + w).
+__device__ __forceinline__ int32_t es_scan_packed(const uint2* pk, uint32_t j0, uint32_t j1, uint32_t a, uint32_t w,
+                                                  int lane) {
+  int32_t s = 0;
+#pragma unroll 4
+  for (uint32_t j = j0 + lane; j < j1; j += 32) {
+    const uint2 e = pk[j];
+    if (e.x - a < w) s += (int32_t)e.y;
+  }
+  return s;
+}
+
 // One pass of the consumers over the tiles of a pass.  Returns false on a lost wait.
 template <typename HT>
 __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* sm, uint32_t& cnt, uint32_t& bad) {
@@ -458,6 +523,7 @@ __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* s
   const uint64_t* bits = reinterpret_cast<const uint64_t*>(sm + L.bits);
   const uint16_t* rl = reinterpret_cast<const uint16_t*>(sm + L.rl);
   const uint4* stages = reinterpret_cast<const uint4*>(sm + L.stage);
+  uint2* packed = reinterpret_cast<uint2*>(sm + L.pack);
   const uint4* qls = reinterpret_cast<const uint4*>(sm + L.q);
   const EsMeta* metas = reinterpret_cast<const EsMeta*>(sm + L.meta);
   uint64_t* full = reinterpret_cast<uint64_t*>(sm + L.bar);
@@ -492,8 +558,27 @@ __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* s
       const int j = tid + k * kEsNC;
       it[k] = (j < m.nf || j >= back) ? tile[j] : make_uint4(0, 0, 0, 0);
     }
+    // this warp's query records (the stage may be refilled once every warp released it)
+    uint4 qr[kEsQW];
+#pragma unroll
+    for (int r = 0; r < kEsQW; ++r) {
+      const int qi = warp + r * kEsNWC;
+      qr[r] = qi < m.nq ? qls[(size_t)s * kEsQB + qi] : make_uint4(0, 0, 0, 0);
+    }
+    // int32 windows: the tile as signed (key, delta) pairs for the in-tile scans, so
+    // the stage is released before them (int64 windows scan the stage itself)
+    if constexpr (sizeof(HT) == 4) {
+      if (m.nq > 0) {
+#pragma unroll
+        for (int k = 0; k < kEsEPT; ++k) {
+          const int j = tid + k * kEsNC;
+          if (j < m.nf || j >= back) packed[j] = make_uint2(it[k].y, j >= back ? 0u - it[k].z : it[k].z);
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+    }
     if (m.nq > 0) {
-      const uint4* ql = qls + (size_t)s * kEsQB;
       // probes of this warp's queries against the window before the tile; lane shares
       // stay in registers across the barrier, with both ends of the carried row
       HT part[kEsQW];
@@ -504,7 +589,7 @@ __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* s
         carry[r] = 0;
         const int qi = warp + r * kEsNWC;
         if (qi < m.nq) {
-          const uint4 q = ql[qi];
+          const uint4 q = qr[r];
           const uint32_t lo = q.x, hi = q.y;
           if (ps.first && ps.crow && lo < hi && lane < 2) carry[r] = (uint64_t)__ldcg(ps.crow + (lane ? hi : lo));
           const uint32_t a = lo > klo ? lo : klo, z = hi < khi ? hi : khi;
@@ -520,13 +605,18 @@ __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* s
       for (int r = 0; r < kEsQW; ++r) {
         const int qi = warp + r * kEsNWC;
         if (qi < m.nq) {
-          const uint4 q = ql[qi];
+          const uint4 q = qr[r];
           const uint32_t lo = q.x, hi = q.y, pe = q.z & 0xffffu, px = q.z >> 16;
           const uint32_t a = lo > klo ? lo : klo, z = hi < khi ? hi : khi;
           HT v = part[r];
           if (a < z) {
-            v += es_scan<HT>(tile, 0, pe, a, z - a, lane);
-            v -= es_scan<HT>(tile, (uint32_t)(kEsTile - (int32_t)px), (uint32_t)kEsTile, a, z - a, lane);
+            if constexpr (sizeof(HT) == 4) {
+              v += es_scan_packed(packed, 0, pe, a, z - a, lane) +
+                   es_scan_packed(packed, (uint32_t)(kEsTile - (int32_t)px), (uint32_t)kEsTile, a, z - a, lane);
+            } else {
+              v += es_scan<HT>(tile, 0, pe, a, z - a, lane);
+              v -= es_scan<HT>(tile, (uint32_t)(kEsTile - (int32_t)px), (uint32_t)kEsTile, a, z - a, lane);
+            }
           }
           uint64_t total;
           if constexpr (sizeof(HT) == 4) {
@@ -550,8 +640,10 @@ __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* s
         }
       }
     }
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);   // this warp no longer reads the stage
+    if constexpr (sizeof(HT) == 8) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);   // this warp no longer reads the stage
+    }
     // apply: front slots add, back slots subtract
 #pragma unroll
     for (int k = 0; k < kEsEPT; ++k) {

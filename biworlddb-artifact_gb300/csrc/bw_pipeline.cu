@@ -2038,9 +2038,11 @@ static inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
 static size_t sweep_budget(int ctas_per_sm) { return (size_t)(kSmemPerSM / ctas_per_sm) - 3072; }
 
-static void finish_spec(PipeSpec& s, const Tuning& tune) {
+// Default sweep: the Euler-tile sweep for forests (measured fastest on batched
+// uneven trees), else by the query/event ratio.
+static void finish_spec(PipeSpec& s, const Tuning& tune, bool forest) {
   s.tile = tune.tile >= kTileNarrowId && tune.tile <= kTileMaxId ? tune.tile
-           : (s.Q * 8 >= s.E ? kTileNarrowId : kTileWideId);
+           : forest ? kTileEulerId : (s.Q * 8 >= s.E ? kTileNarrowId : kTileWideId);
   if (s.tile >= kTileNarrow512Id) s.ctas_per_sm = 1;   // a 512-thread CTA takes the SM's registers
   const int32_t nw = words_of(s.Cmax);
   const size_t bud = sweep_budget(s.ctas_per_sm);
@@ -2099,7 +2101,7 @@ int pipe_spec_one(int32_t S, uint32_t C, int64_t E, int64_t Q, int32_t blocks, b
   s.gsum_words = groups > 1 ? groups * width : 0;
   s.n_units = (int32_t)(groups * ((width + kCarryChunk - 1) / kCarryChunk));
   s.ctas_per_sm = tune.ctas_per_sm > 0 ? tune.ctas_per_sm : (B >= 2 * sms ? 2 : 1);
-  finish_spec(s, tune);
+  finish_spec(s, tune, false);
   return 0;
 }
 
@@ -2122,7 +2124,7 @@ int pipe_spec_forest(int32_t T, const int64_t* soff, const int64_t* eoff, const 
     s.Smax = std::max<int32_t>(s.Smax, (int32_t)ns);
   }
   s.ctas_per_sm = tune.ctas_per_sm > 0 ? tune.ctas_per_sm : 2;
-  finish_spec(s, tune);   // the sweep layout depends only on the domains and the tuning
+  finish_spec(s, tune, true);   // the sweep layout depends only on the domains and the tuning
   int64_t target = tune.block_work > 0 ? tune.block_work
                                        : std::max<int64_t>(65536, Wtot / (4 * (int64_t)s.ctas_per_sm * sms));
   std::vector<int32_t> nb(T);

@@ -84,9 +84,11 @@ using TileSpec512 = TileCfg<1, 1, 64, 512, 512, false, true, true>;   // 15 repl
 enum { kTileAuto = 0, kTileNarrowId = 1, kTileWideId = 2, kTileNarrow512Id = 3, kTileWide512Id = 4, kTileSpec512Id = 5,
        kTileEulerId = 6 };
 constexpr int kTileMaxId = 6;
-// Window capacity of the Euler-tile sweep: int32 entries, or int64 ones in the same bytes.
-constexpr uint32_t kEsCap32 = 32768;
-constexpr uint32_t kEsCap64 = 16384;
+// Window capacity of the Euler-tile sweep: int32 entries, or int64 ones in the same
+// bytes (the prepare pass cuts its rank slices with the k_sweep window's capacities,
+// 27,904 and 13,824 entries, which both fit).
+constexpr uint32_t kEsCap32 = 27904;
+constexpr uint32_t kEsCap64 = 13952;
 
 // ------------------------------------------------------------------ records
 struct StepDesc {        // one Euler step, 16 bytes

@@ -402,9 +402,9 @@ typedef struct {
                            query, 64 steps), 3 and 4 the same tiles on 512 threads (one
                            CTA per SM), 5 the 512-thread tile with one warp staging
                            tiles for the other fifteen, 6 the Euler-tile sweep (a
-                           producer warp bulk-copies signed event tiles for sixteen
-                           consumer warps over a flat shared-memory window; one CTA
-                           per SM); 0 = by the query/event ratio */
+                           planner and an issuer warp bulk-copy signed event tiles for
+                           sixteen consumer warps over a flat shared-memory window; one
+                           CTA per SM); 0 = 6 */
   int32_t reserved;
 } BwForestTuning;
 
