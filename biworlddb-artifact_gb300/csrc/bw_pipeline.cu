@@ -2049,9 +2049,8 @@ static void finish_spec(PipeSpec& s, const Tuning& tune, bool forest) {
   switch (s.tile) {
     case kTileWideId: s.SL = sweep_layout<TileWide>(nw, bud); break;
     case kTileEulerId:
-      // the prepare pass cuts slices for the Euler sweep's window; the TileNarrow512
-      // layout (same capacities or less) stays valid for the k_sweep fallback taken
-      // when the events are not 16-byte aligned
+      // the prepare pass cuts slices for the Euler sweep's window with the capacities
+      // of the TileNarrow512 layout (both fit the Euler sweep's window)
       s.SL = sweep_layout<TileNarrow512>(nw, bud);
       s.SL.cap32 = std::min<uint32_t>(s.SL.cap32, kEsCap32);
       s.SL.cap64 = std::min<uint32_t>(s.SL.cap64, kEsCap64);
@@ -2308,6 +2307,11 @@ int pipe_bind(const PipeSpec& s, void* workspace, cudaStream_t st) {
 
 int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, const BwEvent* events,
                  const BwQuery* queries, int64_t* answers, cudaStream_t st, EventSet* timing, int* kernels_out) {
+  // both sweeps stage events with 16-byte copies (cp.async, cp.async.bulk)
+  if (s.E > 0 && (reinterpret_cast<uintptr_t>(events) & 15u) != 0) {
+    std::fprintf(stderr, "bw replay: events must be 16-byte aligned (got %p)\n", static_cast<const void*>(events));
+    return BW_EINVAL;
+  }
   int rc = ensure_attrs();
   if (rc) return rc;
   Layout L;
@@ -2437,8 +2441,7 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
     sp.bits = pp.bits; sp.rlut = pp.rlut; sp.slices = pp.slices; sp.nslices = pp.nslices; sp.carry = pp.carry;
     sp.answers = answers; sp.status = status; sp.bmode = bmode; sp.ticket = misc + M_SWEEP_TICKET;
     const int sgrid = std::min(B, s.ctas_per_sm * s.sms);
-    const bool ev16 = (reinterpret_cast<uintptr_t>(events) & 15u) == 0;
-    if (s.tile == kTileEulerId && ev16) {
+    if (s.tile == kTileEulerId) {
       EsParams ep;
       ep.ev = reinterpret_cast<const uint4*>(events); ep.qs = queries; ep.desc = desc; ep.blocks = blocks;
       ep.order = order; ep.B = B; ep.cap32 = SL.cap32; ep.cap64 = SL.cap64;
@@ -2451,9 +2454,6 @@ int pipe_enqueue(const PipeSpec& s, void* workspace, const int32_t* parent, cons
       return 0;
     }
     switch (s.tile) {
-      case kTileEulerId:   // events not 16-byte aligned: the same slices through k_sweep
-        k_sweep<TileNarrow512><<<sgrid, TileNarrow512::kThreads, SL.bytes, st>>>(sp, SL);
-        break;
       case kTileWideId: k_sweep<TileWide><<<sgrid, TileWide::kThreads, SL.bytes, st>>>(sp, SL); break;
       case kTileNarrow512Id:
         k_sweep<TileNarrow512><<<sgrid, TileNarrow512::kThreads, SL.bytes, st>>>(sp, SL);

@@ -199,7 +199,8 @@ typedef struct {
   const int32_t* parent;     /* device, n_states; parent[0] = -1, parent[v] < v */
   uint32_t n_keys;           /* key domain [0, n_keys); query bounds lie in [0, n_keys] */
   int64_t n_events;
-  const BwEvent* events;     /* device, grouped by state (non-decreasing state) */
+  const BwEvent* events;     /* device, grouped by state (non-decreasing state), 16-byte aligned
+                                (misaligned events are refused: BW_EINVAL) */
   int64_t n_queries;
   const BwQuery* queries;    /* device, grouped by state (non-decreasing state) */
   int64_t* answers;          /* device out, n_queries */

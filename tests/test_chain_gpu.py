@@ -154,6 +154,6 @@ def test_chain_path_selection(bw, torch_cuda):
     assert not bw.Replay(p, 40000, 8000, 1000, chain=True).chain_path(e)
     assert not bw.Replay(p, 4096, 8000, 1000, chain=False).chain_path(e)
     assert not bw.Replay(p, 4096, 8000, 1000, chain=True, path="general").chain_path(e)
-    # events not 16-byte aligned: no bulk copies, general path
+    # events not 16-byte aligned: not the chain path (a launch refuses them: BW_EINVAL)
     e2 = torch.zeros(16002, dtype=torch.int64, device=dev)[1:16001].view(-1, 2)
     assert not bw.Replay(p, 4096, 8000, 1000, chain=True).chain_path(e2)

@@ -99,6 +99,22 @@ def test_forest_heavy_states_all_tiles(bw, torch_cuda, oracle_mod, tile):
     np.testing.assert_array_equal(got, oracle_mod.ev_forest(*F))
 
 
+def test_unaligned_events_refused(bw, torch_cuda):
+    """Events 8 but not 16 bytes aligned are refused on the host (both sweeps stage
+    events with 16-byte copies): the launch fails with BW_EINVAL and nothing runs."""
+    torch = torch_cuda
+    rng = np.random.default_rng(19)
+    soff, eoff, qoff, keys, par, ev, qs = make_forest(rng, 8, max_states=500)
+    p, e, q = evgen.to_device(torch, par, ev, qs)
+    buf = torch.empty(e.numel() + 1, dtype=torch.int64, device="cuda")
+    e8 = buf[1:].view(-1, 2)          # 8-byte offset from a 256-byte-aligned base
+    e8.copy_(e)
+    assert e8.data_ptr() % 16 == 8
+    for tuning in ({"tile": 6}, {"tile": 3}):
+        with pytest.raises(RuntimeError):
+            bw.forest_replay(soff, eoff, qoff, keys, p, e8, q, tuning=tuning)
+
+
 def test_forest_equals_plain_per_tree(bw, torch_cuda):
     rng = np.random.default_rng(12)
     F = make_forest(rng, 16, max_states=2000)
