@@ -580,18 +580,15 @@ __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* s
     }
     if (m.nq > 0) {
       // probes of this warp's queries against the window before the tile; lane shares
-      // stay in registers across the barrier, with both ends of the carried row
+      // stay in registers across the barrier
       HT part[kEsQW];
-      uint64_t carry[kEsQW];
 #pragma unroll
       for (int r = 0; r < kEsQW; ++r) {
         part[r] = 0;
-        carry[r] = 0;
         const int qi = warp + r * kEsNWC;
         if (qi < m.nq) {
           const uint4 q = qr[r];
           const uint32_t lo = q.x, hi = q.y;
-          if (ps.first && ps.crow && lo < hi && lane < 2) carry[r] = (uint64_t)__ldcg(ps.crow + (lane ? hi : lo));
           const uint32_t a = lo > klo ? lo : klo, z = hi < khi ? hi : khi;
           if (a < z) {
             const uint32_t ra = rank_of(a), rb = rank_of(z);
@@ -608,6 +605,9 @@ __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* s
           const uint4 q = qr[r];
           const uint32_t lo = q.x, hi = q.y, pe = q.z & 0xffffu, px = q.z >> 16;
           const uint32_t a = lo > klo ? lo : klo, z = hi < khi ? hi : khi;
+          // both ends of the carried row, in flight during the scan
+          uint64_t carry = 0;
+          if (ps.first && ps.crow && lo < hi && lane < 2) carry = (uint64_t)__ldcg(ps.crow + (lane ? hi : lo));
           HT v = part[r];
           if (a < z) {
             if constexpr (sizeof(HT) == 4) {
@@ -627,13 +627,13 @@ __device__ bool es_consume(const EsParams& p, const EsPass& ps, unsigned char* s
             for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
             total = x;
           }
-          const uint64_t chi = __shfl_down_sync(kFull, carry[r], 1);
+          const uint64_t chi = __shfl_down_sync(kFull, carry, 1);
           if (lane == 0) {
             int64_t* out = p.answers + q.w;
             if (lo >= hi) {
               if (ps.first) *out = 0;
             } else {
-              total += chi - carry[r];
+              total += chi - carry;
               *out = ps.first ? (int64_t)total : (int64_t)((uint64_t)*out + total);
             }
           }
