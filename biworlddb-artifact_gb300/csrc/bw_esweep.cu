@@ -7,22 +7,26 @@
 // path replays a chain (bw_chain.cu), one block at a time per persistent CTA (blocks
 // from the shared queue, largest first):
 //
-//   * one producer warp walks the block's step descriptors (a shared-memory ring
-//     refilled by cp.async 96 steps ahead) and cuts the flattened sequence into tiles
-//     of up to kEsTile events and kEsQB queries.  Consecutive steps whose event ranges
-//     are adjacent in memory -- the enters of a run of consecutive states, or the exits
-//     of such a run, which come in descending state order -- become one cp.async.bulk
-//     copy into the tile's stage, completed on the stage's "full" mbarrier.  Enter
-//     events fill the stage from the front in step order and exit events from the back,
-//     so an event's sign is its side of the stage; a query records how many enter and
-//     exit events of the tile precede it, and its bounds arrive by cp.async tracked by
-//     the same barrier;
-//   * sixteen consumer warps answer the tile's queries, one warp per query: before a
-//     consumer barrier the probe of the window over [lo, hi) as it stood before the
-//     tile (plus the carried key-prefix row of the block), after it the scan of the
-//     tile's events before the query -- overlapping the other warps' updates, since
-//     the scan reads only the stage -- then release the stage on its "empty" mbarrier
-//     and apply their events to the window;
+//   * two producer warps.  The planner walks the block's step descriptors (a
+//     shared-memory ring refilled by cp.async up to 192 steps ahead), 64 steps per
+//     batch (two per lane), and cuts the flattened sequence into tiles of up to
+//     kEsTile events and kEsQB queries; it hands each batch plan to the issuer
+//     through two shared plan buffers and named barriers.  The issuer turns
+//     consecutive steps whose event ranges are adjacent in memory -- the enters of a
+//     run of consecutive states, or the exits of such a run, which come in descending
+//     state order -- into one cp.async.bulk copy into the tile's stage, completed on
+//     the stage's "full" mbarrier.  Enter events fill the stage from the front in step
+//     order and exit events from the back, so an event's sign is its side of the
+//     stage; a query records how many enter and exit events of the tile precede it,
+//     and its bounds arrive by cp.async tracked by the same barrier;
+//   * sixteen consumer warps take a tile: each thread loads its two events (and, for
+//     int32 windows, repacks them as signed (key, delta) pairs), each warp its
+//     queries, and the stage is released on its "empty" mbarrier (int64 windows: after
+//     the scans, which then read the stage itself).  One warp per
+//     query: before a consumer barrier the probe of the window over [lo, hi) as it
+//     stood before the tile, after it the scan of the tile's events before the query
+//     plus the carried key-prefix row of the block -- overlapping the other warps'
+//     updates, since the scan reads only the packed tile -- then the updates;
 //   * the window is a flat histogram in shared memory: over the keys themselves when
 //     the tree's key domain fits it, else over the block's key ranks one rank slice at
 //     a time (popcount rank table of the prepare pass); int32 entries when the block's
@@ -31,8 +35,9 @@
 //
 // Per tile the consumers meet at most twice: before the probes (the previous tiles'
 // updates are complete; the barrier also agrees on lost waits) and after them.  Every
-// mbarrier wait is bounded; a lost wait sets BW_STATUS_TIMEOUT, both roles stop, and
-// the producer waits (bounded) for its copies in flight before the CTA exits.
+// mbarrier wait is bounded; a lost wait sets BW_STATUS_TIMEOUT, every role stops
+// (the planner ends the pass with an empty plan so that the issuer does too), and the
+// issuer waits (bounded) for its copies in flight before the CTA exits.
 #include <cuda_runtime.h>
 #include <cstdint>
 
